@@ -1,0 +1,413 @@
+// hqr_api.cu -- the library's C ABI: the extended device API of hqr_gpu.h and
+// the drop-in Hybrid_* entry points of Hybrid_tile_QR.h.
+//
+// The drop-in functions keep the reference's calling convention (host arrays
+// in tile layout, void return, abort on error -- Hybrid_tile_QR.c:992-999 and
+// friends call MPI_Abort): each call stages its operands in device buffers
+// owned by the library, runs the tile DAG on the GPU and copies results back.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+#include "Hybrid_tile_QR.h"
+#include "hqr_internal.h"
+
+struct hqr_plan {
+  hqr::Geometry g;
+  int precision;
+  double* dT;
+  hqr::DagWorkspace ws;
+};
+
+namespace {
+
+int g_error_mode = HQR_ERRORS_ABORT;
+thread_local int g_last_error = HQR_OK;
+long long g_timeout_ns = 20000LL * 1000000LL;
+std::mutex g_mu;   // serialises the drop-in entry points (they share buffers)
+char g_cuda_msg[256] = "";
+
+int cuda_rc(cudaError_t e) {
+  return e == cudaSuccess ? HQR_OK : hqr::record_cuda_error(e, "CUDA runtime call");
+}
+
+// Device buffers reused across drop-in calls (grow-only).
+struct Staging {
+  double* buf[4] = {nullptr, nullptr, nullptr, nullptr};
+  size_t cap[4] = {0, 0, 0, 0};
+  cudaStream_t stream = nullptr;
+  hqr_plan* plan = nullptr;
+};
+Staging g_stage;
+
+int stage_reserve(int slot, size_t n_doubles, double** out) {
+  if (g_stage.cap[slot] < n_doubles) {
+    if (g_stage.buf[slot]) cudaFree(g_stage.buf[slot]);
+    g_stage.buf[slot] = nullptr;
+    g_stage.cap[slot] = 0;
+    if (cudaMalloc(&g_stage.buf[slot], n_doubles * sizeof(double)) != cudaSuccess)
+      return HQR_ERR_NOMEM;
+    g_stage.cap[slot] = n_doubles;
+  }
+  *out = g_stage.buf[slot];
+  return HQR_OK;
+}
+
+int stage_stream(cudaStream_t* s) {
+  if (!g_stage.stream) {
+    if (cudaStreamCreateWithFlags(&g_stage.stream, cudaStreamNonBlocking) != cudaSuccess)
+      return HQR_ERR_CUDA;
+  }
+  *s = g_stage.stream;
+  return HQR_OK;
+}
+
+// Plan for the drop-in calls, rebuilt when the shape changes.
+int stage_plan(long M, long N, int NB, int IB, hqr_plan** out) {
+  hqr_plan* p = g_stage.plan;
+  if (p && p->g.M == M && p->g.N == N && p->g.NB == NB && p->g.IB == IB) {
+    *out = p;
+    return HQR_OK;
+  }
+  if (p) hqr_plan_destroy(p);
+  g_stage.plan = nullptr;
+  int rc = hqr_plan_create(&g_stage.plan, M, N, NB, IB, HQR_PREC_FP64);
+  *out = g_stage.plan;
+  return rc;
+}
+
+int report(const char* fn, int rc) {
+  g_last_error = rc;
+  if (rc == HQR_OK) return rc;
+  fprintf(stderr, "hybrid3_gb300: %s: %s%s%s\n", fn, hqr_status_string(rc),
+          rc == HQR_ERR_CUDA ? " -- " : "", rc == HQR_ERR_CUDA ? g_cuda_msg : "");
+  if (g_error_mode == HQR_ERRORS_ABORT) {
+    fflush(stderr);
+    exit(1);
+  }
+  return rc;
+}
+
+int check_status(const mat_stat_t* st, int my_rank, int Proc_num) {
+  if (!st) return HQR_ERR_INVALID;
+  if (Proc_num != 1 || my_rank != 0) return HQR_ERR_INVALID;
+  if (st->tile_M != st->tile_N || st->tile_M == 0) return HQR_ERR_INVALID;
+  if (st->my_mat_M != (unsigned long)st->my_tile_M * st->tile_M) return HQR_ERR_INVALID;
+  if (st->my_mat_N != (unsigned long)st->my_tile_N * st->tile_N) return HQR_ERR_INVALID;
+  return HQR_OK;
+}
+
+size_t tau_len(const hqr::Geometry& g) { return (size_t)g.MT * g.NT * g.NB; }
+
+#define TRY(x)                      \
+  do {                              \
+    int _rc = (x);                  \
+    if (_rc != HQR_OK) return _rc;  \
+  } while (0)
+
+int h2d(double* d, const double* h, size_t n, cudaStream_t s) {
+  return cuda_rc(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, s));
+}
+int d2h(double* h, const double* d, size_t n, cudaStream_t s) {
+  return cuda_rc(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+}
+
+}  // namespace
+
+int hqr::record_cuda_error(cudaError_t e, const char* where) {
+  snprintf(g_cuda_msg, sizeof(g_cuda_msg), "%s: %s (%d)", where, cudaGetErrorString(e), (int)e);
+  return HQR_ERR_CUDA;
+}
+
+// ===========================================================================
+// Extended API
+// ===========================================================================
+extern "C" {
+
+const char* hqr_status_string(int s) {
+  switch (s) {
+    case HQR_OK: return "ok";
+    case HQR_ERR_INVALID: return "invalid argument";
+    case HQR_ERR_CUDA: return "CUDA runtime error";
+    case HQR_ERR_TIMEOUT: return "device scheduler wait timed out";
+    case HQR_ERR_NOMEM: return "device allocation failed";
+    case HQR_ERR_UNSUPPORTED: return "unsupported shape";
+    case HQR_ERR_DEVICE: return "device-side consistency check failed";
+    default: return "unknown status";
+  }
+}
+
+void hqr_set_error_mode(int mode) { g_error_mode = mode; }
+int hqr_last_error(void) { return g_last_error; }
+const char* hqr_last_cuda_error(void) { return g_cuda_msg; }
+void hqr_set_timeout_ms(long long ms) { g_timeout_ns = (ms > 0 ? ms : 1) * 1000000LL; }
+
+int hqr_plan_create(hqr_plan_t** plan, long M, long N, int NB, int IB, int precision) {
+  if (!plan) return HQR_ERR_INVALID;
+  *plan = nullptr;
+  if (precision != HQR_PREC_FP64 && precision != HQR_PREC_OZAKI) return HQR_ERR_INVALID;
+  hqr::Geometry g;
+  TRY(hqr::make_geometry(M, N, NB, IB, &g));
+  hqr_plan* p = new hqr_plan();
+  p->g = g;
+  p->precision = precision;
+  p->dT = nullptr;
+  if (cudaMalloc(&p->dT, (size_t)M * N * sizeof(double)) != cudaSuccess) {
+    delete p;
+    return HQR_ERR_NOMEM;
+  }
+  cudaMemset(p->dT, 0, (size_t)M * N * sizeof(double));
+  *plan = p;
+  return HQR_OK;
+}
+
+int hqr_plan_destroy(hqr_plan_t* plan) {
+  if (!plan) return HQR_ERR_INVALID;
+  if (plan->dT) cudaFree(plan->dT);
+  hqr::dag_workspace_free(&plan->ws);
+  delete plan;
+  return HQR_OK;
+}
+
+double* hqr_plan_t_factors(hqr_plan_t* plan) { return plan ? plan->dT : nullptr; }
+
+int hqr_geqrf_async(hqr_plan_t* plan, double* dA, double* dTAU, void* stream) {
+  if (!plan || !dA || !dTAU) return HQR_ERR_INVALID;
+  return hqr::launch_factor(plan->g, &plan->ws, dA, plan->dT, dTAU, g_timeout_ns,
+                            (cudaStream_t)stream);
+}
+
+int hqr_plan_status(hqr_plan_t* plan, void* stream) {
+  if (!plan) return HQR_ERR_INVALID;
+  if (!plan->ws.ctl) return cuda_rc(cudaStreamSynchronize((cudaStream_t)stream));
+  return hqr::dag_status(&plan->ws, (cudaStream_t)stream);
+}
+
+int hqr_geqrf(hqr_plan_t* plan, double* dA, double* dTAU, void* stream) {
+  TRY(hqr_geqrf_async(plan, dA, dTAU, stream));
+  return hqr_plan_status(plan, stream);
+}
+
+int hqr_plan_stats(hqr_plan_t* plan, hqr_stats_t* out, void* stream) {
+  if (!plan || !out || !plan->ws.stats) return HQR_ERR_INVALID;
+  unsigned long long v[10];
+  TRY(hqr::dag_stats(&plan->ws, v, (cudaStream_t)stream));
+  for (int t = 0; t < 5; t++) {
+    out->count[t] = v[2 * t];
+    out->cycles[t] = v[2 * t + 1];
+  }
+  return HQR_OK;
+}
+
+int hqr_make_q_async(hqr_plan_t* plan, double* dQ, double* dRY, const double* dTAU, int use_plan_t,
+                     void* stream) {
+  if (!plan || !dQ || !dRY || !dTAU) return HQR_ERR_INVALID;
+  const hqr::Geometry& g = plan->g;
+  cudaStream_t s = (cudaStream_t)stream;
+  // Hybrid_make_Q.c:91-95 sets the diagonal of the caller-zeroed Q
+  hqr::make_identity(dQ, g.M, g.N, g.NB, false, s);
+  TRY(hqr::launch_apply_qt(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g.NT, !use_plan_t, g_timeout_ns, s));
+  hqr::zero_reflectors(dRY, g.M, g.N, g.NB, s);
+  return cuda_rc(cudaGetLastError());
+}
+
+int hqr_make_q(hqr_plan_t* plan, double* dQ, double* dRY, const double* dTAU, int use_plan_t,
+               void* stream) {
+  TRY(hqr_make_q_async(plan, dQ, dRY, dTAU, use_plan_t, stream));
+  return hqr_plan_status(plan, stream);
+}
+
+int hqr_ormqr_t(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT,
+                int use_plan_t, void* stream) {
+  if (!plan || !dRY || !dTAU || !dC || CT <= 0) return HQR_ERR_INVALID;
+  TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, !use_plan_t,
+                           g_timeout_ns, (cudaStream_t)stream));
+  return hqr_plan_status(plan, stream);
+}
+
+int hqr_dgemm_tn(long N, int NB, const double* dA, const double* dB, double* dC, void* stream) {
+  if (!dA || !dB || !dC || NB < 16 || NB % 16 || N <= 0 || N % NB) return HQR_ERR_INVALID;
+  hqr::dgemm_tn_tiles(dA, dB, dC, N, N, NB, (cudaStream_t)stream);
+  return cuda_rc(cudaGetLastError());
+}
+
+int hqr_make_identity(long M, long N, int NB, double* dQ, void* stream) {
+  if (!dQ || NB <= 0 || M % NB || N % NB) return HQR_ERR_INVALID;
+  hqr::make_identity(dQ, M, N, NB, true, (cudaStream_t)stream);
+  return cuda_rc(cudaGetLastError());
+}
+
+int hqr_fill_uniform(long M, long N, int NB, uint64_t seed, double* dA, void* stream) {
+  if (!dA || NB <= 0 || M % NB || N % NB) return HQR_ERR_INVALID;
+  hqr::fill_uniform(dA, M, N, NB, seed, (cudaStream_t)stream);
+  return cuda_rc(cudaGetLastError());
+}
+
+int hqr_frob2(long M, long N, int NB, const double* dX, const double* dY, double alpha,
+              double* result, void* stream) {
+  if (!dX || !result || NB <= 0 || M % NB || N % NB) return HQR_ERR_INVALID;
+  double* d = nullptr;
+  if (cudaMalloc(&d, sizeof(double)) != cudaSuccess) return HQR_ERR_NOMEM;
+  cudaStream_t s = (cudaStream_t)stream;
+  hqr::frob_diff(dX, dY, alpha, M, N, NB, d, s);
+  int rc = cuda_rc(cudaMemcpyAsync(result, d, sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (rc == HQR_OK) rc = cuda_rc(cudaStreamSynchronize(s));
+  cudaFree(d);
+  return rc;
+}
+
+int hqr_tiles_to_colmajor(long M, long N, int NB, const double* dT, double* dCM, void* stream) {
+  if (!dT || !dCM || NB <= 0 || M % NB || N % NB) return HQR_ERR_INVALID;
+  hqr::tiles_to_colmajor(dT, dCM, M, N, NB, (cudaStream_t)stream);
+  return cuda_rc(cudaGetLastError());
+}
+
+int hqr_colmajor_to_tiles(long M, long N, int NB, const double* dCM, double* dT, void* stream) {
+  if (!dT || !dCM || NB <= 0 || M % NB || N % NB) return HQR_ERR_INVALID;
+  hqr::colmajor_to_tiles(dCM, dT, M, N, NB, (cudaStream_t)stream);
+  return cuda_rc(cudaGetLastError());
+}
+
+int hqr_zero_reflectors(long M, long N, int NB, double* dA, void* stream) {
+  if (!dA || NB <= 0 || M % NB || N % NB) return HQR_ERR_INVALID;
+  hqr::zero_reflectors(dA, M, N, NB, (cudaStream_t)stream);
+  return cuda_rc(cudaGetLastError());
+}
+
+// ===========================================================================
+// Drop-in entry points (Hybrid_tile_QR.h)
+// ===========================================================================
+
+static int do_tile_qr(mat_stat_t* st, double* A, double* TAU, int rank, int P, int ib) {
+  TRY(check_status(st, rank, P));
+  if (!A || !TAU) return HQR_ERR_INVALID;
+  const long M = (long)st->my_mat_M, N = (long)st->my_mat_N;
+  const int NB = (int)st->tile_M;
+  hqr_plan* plan;
+  TRY(stage_plan(M, N, NB, ib, &plan));
+  cudaStream_t s;
+  TRY(stage_stream(&s));
+  double *dA, *dTAU;
+  TRY(stage_reserve(0, (size_t)M * N, &dA));
+  TRY(stage_reserve(1, tau_len(plan->g), &dTAU));
+  TRY(h2d(dA, A, (size_t)M * N, s));
+  TRY(h2d(dTAU, TAU, tau_len(plan->g), s));
+  TRY(hqr_geqrf(plan, dA, dTAU, s));
+  TRY(d2h(A, dA, (size_t)M * N, s));
+  TRY(d2h(TAU, dTAU, tau_len(plan->g), s));
+  return cuda_rc(cudaStreamSynchronize(s));
+}
+
+void Hybrid_tile_QR(mat_stat_t* status, double* A, double* TAU, int my_rank, int Proc_num, int ib) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  report("Hybrid_tile_QR", do_tile_qr(status, A, TAU, my_rank, Proc_num, ib));
+}
+
+void Hybrid_dgeqrf(mat_stat_t* status, double* A, double* TAU, int my_rank, int Proc_num) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  report("Hybrid_dgeqrf",
+         do_tile_qr(status, A, TAU, my_rank, Proc_num, status ? (int)status->tile_N : 0));
+}
+
+// Apply Q^T to a host array C (same grid) after staging RY, TAU; mode:
+// 0 = make_Q (set diagonal, zero V), 1 = dorgqr (C := I first), 2 = dormqr.
+static int do_apply(mat_stat_t* st, double* Q, double* RY, double* TAU, int rank, int P, int ib,
+                    int mode) {
+  TRY(check_status(st, rank, P));
+  if (!Q || !RY || !TAU) return HQR_ERR_INVALID;
+  const long M = (long)st->my_mat_M, N = (long)st->my_mat_N;
+  const int NB = (int)st->tile_M;
+  hqr_plan* plan;
+  TRY(stage_plan(M, N, NB, ib > 0 ? ib : NB, &plan));
+  cudaStream_t s;
+  TRY(stage_stream(&s));
+  double *dQ, *dRY, *dTAU;
+  TRY(stage_reserve(0, (size_t)M * N, &dRY));
+  TRY(stage_reserve(1, tau_len(plan->g), &dTAU));
+  TRY(stage_reserve(2, (size_t)M * N, &dQ));
+  TRY(h2d(dRY, RY, (size_t)M * N, s));
+  TRY(h2d(dTAU, TAU, tau_len(plan->g), s));
+  if (mode == 1) {
+    hqr::make_identity(dQ, M, N, NB, true, s);
+  } else {
+    TRY(h2d(dQ, Q, (size_t)M * N, s));
+    if (mode == 0) hqr::make_identity(dQ, M, N, NB, false, s);
+  }
+  TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dQ, plan->g.NT, true,
+                           g_timeout_ns, s));
+  TRY(hqr_plan_status(plan, s));
+  if (mode == 0) {
+    hqr::zero_reflectors(dRY, M, N, NB, s);
+    TRY(d2h(RY, dRY, (size_t)M * N, s));
+  }
+  TRY(d2h(Q, dQ, (size_t)M * N, s));
+  return cuda_rc(cudaStreamSynchronize(s));
+}
+
+void Hybrid_make_Q(mat_stat_t* status, double* Q, double* RY, double* TAU, int my_rank,
+                   int Proc_num, int ib) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  report("Hybrid_make_Q", do_apply(status, Q, RY, TAU, my_rank, Proc_num, ib, 0));
+}
+
+void Hybrid_dorgqr(mat_stat_t* status, double* Q, double* RY, double* TAU, int my_rank,
+                   int Proc_num) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  report("Hybrid_dorgqr", do_apply(status, Q, RY, TAU, my_rank, Proc_num, 0, 1));
+}
+
+void Hybrid_dormqr(mat_stat_t* status, double* RY, double* TAU, double* C, int my_rank,
+                   int Proc_num) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  report("Hybrid_dormqr", do_apply(status, C, RY, TAU, my_rank, Proc_num, 0, 2));
+}
+
+static int do_simple(mat_stat_t* st, int rank, int P, int op, double* A, double* B, double* C) {
+  TRY(check_status(st, rank, P));
+  const long M = (long)st->my_mat_M, N = (long)st->my_mat_N;
+  const int NB = (int)st->tile_M;
+  if (op == 2 && M != N) return HQR_ERR_UNSUPPORTED;
+  cudaStream_t s;
+  TRY(stage_stream(&s));
+  double *d0, *d1, *d2;
+  TRY(stage_reserve(0, (size_t)M * N, &d0));
+  if (op == 0) {            // identity
+    if (!A) return HQR_ERR_INVALID;
+    hqr::make_identity(d0, M, N, NB, true, s);
+    TRY(d2h(A, d0, (size_t)M * N, s));
+  } else if (op == 1) {     // zero reflectors
+    if (!A) return HQR_ERR_INVALID;
+    TRY(h2d(d0, A, (size_t)M * N, s));
+    hqr::zero_reflectors(d0, M, N, NB, s);
+    TRY(d2h(A, d0, (size_t)M * N, s));
+  } else {                  // C = A^T B
+    if (!A || !B || !C) return HQR_ERR_INVALID;
+    if (NB % 16) return HQR_ERR_UNSUPPORTED;
+    TRY(stage_reserve(1, (size_t)M * N, &d1));
+    TRY(stage_reserve(2, (size_t)M * N, &d2));
+    TRY(h2d(d0, A, (size_t)M * N, s));
+    TRY(h2d(d1, B, (size_t)M * N, s));
+    hqr::dgemm_tn_tiles(d0, d1, d2, M, N, NB, s);
+    TRY(d2h(C, d2, (size_t)M * N, s));
+  }
+  TRY(cuda_rc(cudaGetLastError()));
+  return cuda_rc(cudaStreamSynchronize(s));
+}
+
+void Hybrid_make_I(mat_stat_t* status, double* Id, int my_rank, int Proc_num) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  report("Hybrid_make_I", do_simple(status, my_rank, Proc_num, 0, Id, nullptr, nullptr));
+}
+
+void Hybrid_remv_Y(mat_stat_t* status, double* RY, int my_rank, int Proc_num) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  report("Hybrid_remv_Y", do_simple(status, my_rank, Proc_num, 1, RY, nullptr, nullptr));
+}
+
+void Hybrid_dgemm(mat_stat_t* status, double* A, double* B, double* C, int my_rank, int Proc_num) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  report("Hybrid_dgemm", do_simple(status, my_rank, Proc_num, 2, A, B, C));
+}
+
+}  // extern "C"

@@ -1,0 +1,192 @@
+// hqr_dag.cu -- host side of the device DAG: geometry, workspace and launches
+// of the persistent executor for the factorization and the Q^T application.
+#include <algorithm>
+#include <cstdio>
+
+#include "hqr_dag.cuh"
+#include "hqr_internal.h"
+
+namespace hqr {
+
+int make_geometry(long M, long N, int NB, int IB, Geometry* g) {
+  if (NB < 16 || NB > kMaxNB || NB % 16 != 0) return HQR_ERR_UNSUPPORTED;
+  if (M <= 0 || N <= 0 || M % NB != 0 || N % NB != 0) return HQR_ERR_INVALID;
+  if (IB <= 0 || IB > NB) return HQR_ERR_INVALID;
+  g->M = M;
+  g->N = N;
+  g->NB = NB;
+  g->IB = IB;
+  g->MT = (int)(M / NB);
+  g->NT = (int)(N / NB);
+  g->steps = std::min(g->MT, g->NT);
+  // inner block: the largest divisor of NB that is <= min(IB, 32) and a multiple of 8
+  int w = std::min(IB, kMaxW);
+  w -= w % 8;
+  while (w > 8 && NB % w != 0) w -= 8;
+  if (w < 8) w = 8;
+  g->w = w;
+  // column block of the update tasks: the widest multiple of 8 dividing NB,
+  // at most 64 and at most NB*CB*8 <= 64 KiB, whose shared-memory plan fits
+  const size_t smem_cap = 227 * 1024 - 256;   // leave room for static shared memory
+  int cb = (8192 / NB) > 64 ? 64 : 8192 / NB;
+  if (cb > NB) cb = NB;
+  cb -= cb % 8;
+  for (; cb >= 8; cb -= 8) {
+    if (NB % cb != 0) continue;
+    TileShape sh{NB, w, cb, NB >= 512 ? 64 : kRC};
+    if ((size_t)SmemPlan::make(sh).total * sizeof(double) <= smem_cap) break;
+  }
+  if (cb < 8) return HQR_ERR_UNSUPPORTED;
+  g->CB = cb;
+  g->NC = NB / cb;
+  TileShape sh{NB, w, cb, NB >= 512 ? 64 : kRC};
+  SmemPlan sp = SmemPlan::make(sh);
+  g->smem_bytes = (size_t)sp.total * sizeof(double);
+  if (g->smem_bytes > smem_cap) return HQR_ERR_UNSUPPORTED;
+  if ((long long)g->steps * g->MT + (long long)g->steps * g->NT * g->MT * g->NC > 0x3fffffffLL)
+    return HQR_ERR_UNSUPPORTED;
+  return HQR_OK;
+}
+
+static TileShape shape_of(const Geometry& g) {
+  return TileShape{g.NB, g.w, g.CB, g.NB >= 512 ? 64 : kRC};
+}
+
+int dag_workspace_reserve(DagWorkspace* ws, size_t n_ids) {
+  if (ws->cap_ids >= n_ids && ws->ctl) return HQR_OK;
+  dag_workspace_free(ws);
+  if (cudaMalloc(&ws->cnt, n_ids * sizeof(int)) != cudaSuccess) return HQR_ERR_NOMEM;
+  if (cudaMalloc(&ws->qhi, n_ids * sizeof(int)) != cudaSuccess) return HQR_ERR_NOMEM;
+  if (cudaMalloc(&ws->qlo, n_ids * sizeof(int)) != cudaSuccess) return HQR_ERR_NOMEM;
+  if (cudaMalloc(&ws->ctl, kCtlWords * sizeof(unsigned)) != cudaSuccess) return HQR_ERR_NOMEM;
+  if (cudaMalloc(&ws->stats, 2 * kNumTypes * sizeof(unsigned long long)) != cudaSuccess)
+    return HQR_ERR_NOMEM;
+  if (cudaMemset(ws->ctl, 0, kCtlWords * sizeof(unsigned)) != cudaSuccess) return HQR_ERR_CUDA;
+  ws->cap_ids = n_ids;
+  return HQR_OK;
+}
+
+void dag_workspace_free(DagWorkspace* ws) {
+  if (ws->cnt) cudaFree(ws->cnt);
+  if (ws->qhi) cudaFree(ws->qhi);
+  if (ws->qlo) cudaFree(ws->qlo);
+  if (ws->ctl) cudaFree(ws->ctl);
+  if (ws->stats) cudaFree(ws->stats);
+  *ws = DagWorkspace{};
+}
+
+int dag_sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+static int run_dag(DagParams& p, DagWorkspace* ws, const Geometry& g, cudaStream_t stream) {
+  p.sh = shape_of(g);
+  p.sp = SmemPlan::make(p.sh);
+  p.n_ids = p.steps * p.MT + p.steps * p.J * p.MT * p.NC;
+  int rc = dag_workspace_reserve(ws, (size_t)p.n_ids);
+  if (rc != HQR_OK) return rc;
+  p.cnt = ws->cnt;
+  p.qhi = ws->qhi;
+  p.qlo = ws->qlo;
+  p.ctl = ws->ctl;
+  p.stats = ws->stats;
+  // control words: queue heads/tails and the done counter start at zero; the
+  // error word is kept (cleared by dag_status) so a failure is never lost.
+  cudaError_t e0 = cudaMemsetAsync(ws->ctl, 0, kErr * sizeof(unsigned), stream);
+  if (e0 == cudaSuccess)
+    e0 = cudaMemsetAsync(ws->stats, 0, 2 * kNumTypes * sizeof(unsigned long long), stream);
+  if (e0 != cudaSuccess) return record_cuda_error(e0, "DAG workspace reset");
+  const int blocks = (p.n_ids + 255) / 256;
+  dag_init_kernel<<<blocks, 256, 0, stream>>>(p);
+  dag_seed_kernel<<<blocks, 256, 0, stream>>>(p);
+  static size_t attr_bytes = 0;   // dynamic shared memory opted in so far
+  if (g.smem_bytes > attr_bytes) {
+    cudaError_t e = cudaFuncSetAttribute(dag_exec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)g.smem_bytes);
+    if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(dag_exec_kernel)");
+    attr_bytes = g.smem_bytes;
+  }
+  const int grid = std::min(dag_sm_count(), std::max(1, p.n_tasks));
+  dag_exec_kernel<<<grid, kThreads, g.smem_bytes, stream>>>(p);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return record_cuda_error(e, "dag_exec_kernel launch");
+  return HQR_OK;
+}
+
+int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, double* dTAU,
+                  long long timeout_ns, cudaStream_t stream) {
+  DagParams p{};
+  p.mode = kModeFactor;
+  p.MT = g.MT;
+  p.NT = g.NT;
+  p.CT = g.NT;
+  p.NC = g.NC;
+  p.steps = g.steps;
+  p.J = g.NT;
+  p.A = dA;
+  p.T = dT;
+  p.TAU = dTAU;
+  p.C = dA;
+  p.timeout_ns = timeout_ns;
+  // tasks: per step i, 1 GEQRT + (MT-1-i) TSQRT + NC*(NT-1-i)*(MT-i) updates
+  long long n = 0;
+  for (int i = 0; i < g.steps; i++)
+    n += (g.MT - i) + (long long)g.NC * (g.NT - 1 - i) * (g.MT - i);
+  p.n_tasks = (int)n;
+  return run_dag(p, ws, g, stream);
+}
+
+int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT,
+                    const double* dTAU, double* dC, int CT, bool rebuild_t, long long timeout_ns,
+                    cudaStream_t stream) {
+  if (CT <= 0) return HQR_ERR_INVALID;
+  DagParams p{};
+  p.mode = kModeApplyQt;
+  p.MT = g.MT;
+  p.NT = g.NT;
+  p.CT = CT;
+  p.NC = g.NC;
+  p.steps = g.steps;
+  p.J = CT;
+  p.A = const_cast<double*>(dA);
+  p.T = dT;
+  p.TAU = const_cast<double*>(dTAU);
+  p.C = dC;
+  p.timeout_ns = timeout_ns;
+  long long n = 0;
+  for (int i = 0; i < g.steps; i++) n += (g.MT - i) + (long long)g.NC * CT * (g.MT - i);
+  p.n_tasks = (int)n;
+  (void)rebuild_t;   // T-build tasks always run: they cost O(NB^2 w) per panel tile
+  return run_dag(p, ws, g, stream);
+}
+
+int dag_status(DagWorkspace* ws, cudaStream_t stream) {
+  cudaError_t e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return record_cuda_error(e, "DAG execution (stream synchronize)");
+  unsigned ctl[kCtlWords];
+  e = cudaMemcpy(ctl, ws->ctl, sizeof(ctl), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return record_cuda_error(e, "DAG status read");
+  if (ctl[kErr] != 0u) {
+    cudaMemset(ws->ctl + kErr, 0, sizeof(unsigned));
+    if (ctl[kErr] & kErrTimeout) return HQR_ERR_TIMEOUT;
+    return HQR_ERR_DEVICE;
+  }
+  return HQR_OK;
+}
+
+int dag_stats(DagWorkspace* ws, unsigned long long out[10], cudaStream_t stream) {
+  if (cudaStreamSynchronize(stream) != cudaSuccess) return HQR_ERR_CUDA;
+  if (cudaMemcpy(out, ws->stats, 10 * sizeof(unsigned long long), cudaMemcpyDeviceToHost) !=
+      cudaSuccess)
+    return HQR_ERR_CUDA;
+  return HQR_OK;
+}
+
+}  // namespace hqr

@@ -1,0 +1,318 @@
+// hqr_dag.cuh -- the device-resident tile DAG: dependency counters, ready
+// queues and the persistent executor kernel.
+//
+// This replaces, on the GPU, the reference's OpenMP task machinery:
+//   * prog_table (Hybrid_tile_QR.c:23,36-40,515-580): one byte per task
+//     (i,j,k) whose MEM/LIN/YTM bits become ready at 0x7.  Here each task owns
+//     an int counter initialised to its number of unmet inputs and a task is
+//     ready when an atomic decrement brings it to zero:
+//       MEM  -- the tile was updated by the previous step's SSRFB,
+//       LIN  -- the previous task of the same column chain is done,
+//       YTM  -- the panel reflector (Y, T) the update needs is available.
+//   * the TileSch FIFO (TileSch.c:10-61) under omp critical becomes two
+//     lock-free FIFOs in global memory, one for the critical path (panel tasks
+//     and the next panel column's updates) and one for the rest.  Each queue
+//     has room for every task (each task is pushed exactly once), so a push
+//     never waits.
+//   * the Y/T ring glob_YT with its tickets (Hybrid_tile_QR.c:379-390) is not
+//     needed: V stays in place in A and every panel tile's T is kept in HBM.
+//   * the worker loop (Hybrid_tile_QR.c:905-1461) becomes a persistent kernel
+//     with one CTA per SM; thread 0 pops, the CTA runs the task, thread 0
+//     releases its dependents.
+//
+// LARFB and SSRFB tasks are split into NC column blocks (the columns of a
+// trailing tile are independent), which multiplies the parallelism of a step
+// by NC.  Every wait is bounded in time: when a wait runs out the kernel sets
+// an error bit and every CTA returns, so a broken DAG never hangs the GPU.
+#pragma once
+#include "hqr_tile_fp64.cuh"
+
+namespace hqr {
+
+enum DagMode : int {
+  kModeFactor = 0,    // Hybrid_tile_QR: GEQRT/TSQRT panels + LARFB/SSRFB updates of A
+  kModeApplyQt = 1,   // C <- Q^T C: T-build panels + LARFB/SSRFB updates of C
+};
+
+enum TaskType : int { kGEQRT = 0, kTSQRT = 1, kLARFB = 2, kSSRFB = 3, kTBUILD = 4, kNumTypes = 5 };
+
+// Control words of the scheduler (one cache line each is not needed: the
+// counters are touched once per task).
+enum Ctl : int { kHiHead = 0, kHiTail = 1, kLoHead = 2, kLoTail = 3, kDone = 4, kErr = 5, kCtlWords = 8 };
+
+struct DagParams {
+  int mode;
+  int MT, NT, CT, NC, steps, J;   // J = tile columns spanned by update ids
+  TileShape sh;
+  SmemPlan sp;
+  double* A;        // factored matrix: R above, V below the diagonal
+  double* T;        // T tiles (same tile layout as A)
+  double* TAU;
+  double* C;        // target of the update tasks (A itself when factoring)
+  int* cnt;         // dependency counters, one per task id
+  int* qhi;         // ready FIFOs, capacity n_ids each
+  int* qlo;
+  unsigned* ctl;
+  int n_ids;        // size of the task-id space
+  int n_tasks;      // number of real tasks
+  long long timeout_ns;
+  unsigned long long* stats;   // [type][0] = count, [type][1] = SM cycles
+};
+
+constexpr int kNever = 0x3fffffff;
+
+// --- task ids ----------------------------------------------------------------
+//   panel  (i, k)        : i*MT + k                         (k >= i)
+//   update (i, j, k, c)  : P0 + ((i*J + j)*MT + k)*NC + c   (k >= i)
+__host__ __device__ __forceinline__ int panel_id(const DagParams& p, int i, int k) {
+  return i * p.MT + k;
+}
+__host__ __device__ __forceinline__ int update_id(const DagParams& p, int i, int j, int k, int c) {
+  return p.steps * p.MT + ((i * p.J + j) * p.MT + k) * p.NC + c;
+}
+
+struct TaskDesc {
+  int type, i, j, k, c;
+};
+
+__device__ __forceinline__ TaskDesc decode(const DagParams& p, int id) {
+  TaskDesc t;
+  const int P0 = p.steps * p.MT;
+  if (id < P0) {
+    t.i = id / p.MT;
+    t.k = id % p.MT;
+    t.j = t.i;
+    t.c = 0;
+    t.type = (p.mode == kModeFactor) ? (t.k == t.i ? kGEQRT : kTSQRT) : kTBUILD;
+  } else {
+    int u = id - P0;
+    t.c = u % p.NC; u /= p.NC;
+    t.k = u % p.MT; u /= p.MT;
+    t.j = u % p.J;
+    t.i = u / p.J;
+    t.type = (t.k == t.i) ? kLARFB : kSSRFB;
+  }
+  return t;
+}
+
+__device__ __forceinline__ bool update_valid(const DagParams& p, int i, int j) {
+  return (p.mode == kModeFactor) ? (j > i && j < p.NT) : (j < p.CT);
+}
+
+__device__ __forceinline__ bool is_high_priority(const DagParams& p, int id) {
+  const TaskDesc t = decode(p, id);
+  if (t.type == kGEQRT || t.type == kTSQRT || t.type == kTBUILD) return true;
+  return p.mode == kModeFactor && t.j == t.i + 1;   // look-ahead: next panel column
+}
+
+// --- queues -------------------------------------------------------------------
+__device__ __forceinline__ void push_ready(const DagParams& p, int id) {
+  const bool hi = is_high_priority(p, id);
+  int* q = hi ? p.qhi : p.qlo;
+  const unsigned slot = atomicAdd(p.ctl + (hi ? kHiTail : kLoTail), 1u);
+  if ((int)slot < p.n_ids) {
+    atomicExch(q + slot, id);
+  } else {
+    atomicOr((int*)(p.ctl + kErr), kErrBadTask);
+  }
+}
+
+__device__ __forceinline__ void release(const DagParams& p, int id) {
+  __threadfence();
+  if (atomicSub(p.cnt + id, 1) == 1) push_ready(p, id);
+}
+
+// Wait (bounded) until slot of queue q has been written; returns the id or -1.
+__device__ int wait_slot(const DagParams& p, int* q, unsigned slot) {
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    const int v = *((volatile int*)(q + slot));
+    if (v >= 0) return v;
+    if ((long long)(global_ns() - t0) > p.timeout_ns) {
+      atomicOr((int*)(p.ctl + kErr), kErrTimeout);
+      return -1;
+    }
+    __nanosleep(64);
+  }
+}
+
+__device__ __forceinline__ int try_claim(const DagParams& p, int* q, int head, int tail) {
+  volatile unsigned* ctl = p.ctl;
+  unsigned h = ctl[head];
+  while (h < ctl[tail]) {
+    const unsigned prev = atomicCAS(p.ctl + head, h, h + 1);
+    if (prev == h) return wait_slot(p, q, h);
+    h = prev;
+  }
+  return -2;   // nothing to claim
+}
+
+// Thread 0: next task id, or -1 when the DAG is done or failed.
+__device__ int pop_task(const DagParams& p) {
+  volatile unsigned* ctl = p.ctl;
+  uint64_t t0 = global_ns();
+  unsigned ns = 32;
+  for (;;) {
+    if (ctl[kErr] != 0u) return -1;
+    if ((int)ctl[kDone] >= p.n_tasks) return -1;
+    int id = try_claim(p, p.qhi, kHiHead, kHiTail);
+    if (id == -2) id = try_claim(p, p.qlo, kLoHead, kLoTail);
+    if (id >= 0) {
+      __threadfence();   // acquire: the producers' tile writes are visible
+      return id;
+    }
+    if (id == -1) return -1;
+    if ((long long)(global_ns() - t0) > p.timeout_ns) {
+      atomicOr((int*)(p.ctl + kErr), kErrTimeout);
+      return -1;
+    }
+    __nanosleep(ns);
+    if (ns < 1024) ns <<= 1;
+  }
+}
+
+// --- dependency initialisation (one thread per id) --------------------------------
+__global__ void dag_init_kernel(DagParams p) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= p.n_ids) return;
+  p.qhi[id] = -1;
+  p.qlo[id] = -1;
+  int deps = kNever;
+  const int P0 = p.steps * p.MT;
+  if (id < P0) {
+    const int i = id / p.MT, k = id % p.MT;
+    if (k >= i) {
+      if (p.mode == kModeFactor)
+        deps = (k == i ? 0 : 1) + (i > 0 ? p.NC : 0);
+      else
+        deps = 0;
+    }
+  } else {
+    int u = id - P0;
+    const int c = u % p.NC; u /= p.NC;
+    const int k = u % p.MT; u /= p.MT;
+    const int j = u % p.J;
+    const int i = u / p.J;
+    (void)c;
+    if (k >= i && i < p.steps && update_valid(p, i, j))
+      deps = 1 + (k > i ? 1 : 0) + (i > 0 ? 1 : 0);
+  }
+  p.cnt[id] = deps;
+}
+
+__global__ void dag_seed_kernel(DagParams p) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= p.n_ids) return;
+  if (p.cnt[id] == 0) push_ready(p, id);
+}
+
+// --- releases after a task ---------------------------------------------------------
+__device__ void release_dependents(const DagParams& p, const TaskDesc& t) {
+  if (t.type == kGEQRT || t.type == kTSQRT || t.type == kTBUILD) {
+    const int j0 = (p.mode == kModeFactor) ? t.i + 1 : 0;
+    const int j1 = (p.mode == kModeFactor) ? p.NT : p.CT;
+    for (int j = j0; j < j1; j++)
+      for (int c = 0; c < p.NC; c++) release(p, update_id(p, t.i, j, t.k, c));
+    if (p.mode == kModeFactor && t.k + 1 < p.MT) release(p, panel_id(p, t.i, t.k + 1));
+    return;
+  }
+  // LARFB / SSRFB: LIN to the next task of this column chain
+  if (t.k + 1 < p.MT) release(p, update_id(p, t.i, t.j, t.k + 1, t.c));
+  // MEM to the next step (only SSRFB: LARFB's tile row is final)
+  if (t.type == kSSRFB && t.i + 1 < p.steps) {
+    if (p.mode == kModeFactor && t.j == t.i + 1)
+      release(p, panel_id(p, t.i + 1, t.k));
+    else
+      release(p, update_id(p, t.i + 1, t.j, t.k, t.c));
+  }
+}
+
+// --- T build for the Q^T application (diagonal w x w blocks from V, TAU) -------
+__device__ void task_tbuild(const double* V, const double* tau_g, double* T, bool unit,
+                            const TileShape& sh, double* smem, const SmemPlan& sp) {
+  const int NB = sh.NB, w = sh.w;
+  double* sP = smem + sp.off_c1;
+  double* sTau = smem + sp.off_tau;
+  double* sG = smem + sp.off_g;
+  double* sTb = smem + sp.off_t;
+  for (int i0 = 0; i0 < NB; i0 += w) {
+    const int m = unit ? NB - i0 : NB;
+    const double* src = unit ? V + i0 + (size_t)i0 * NB : V + (size_t)i0 * NB;
+    __syncthreads();
+    load_block(sP, NB, src, NB, m, w);
+    for (int e = threadIdx.x; e < w; e += kThreads) sTau[e] = ldg_cg(tau_g + i0 + e);
+    __syncthreads();
+    build_t_block(sP, NB, m, w, unit, sTau, sG, sTb);
+    store_block(T + i0 + (size_t)i0 * NB, NB, sTb, w, w, w);
+  }
+  __syncthreads();
+}
+
+// --- the persistent executor ---------------------------------------------------------
+__global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
+  extern __shared__ double smem[];
+  __shared__ int s_id;
+  const int NB = p.sh.NB;
+  const size_t tsz = (size_t)NB * NB;
+  unsigned long long local_cnt[kNumTypes] = {0, 0, 0, 0, 0};
+  unsigned long long local_cyc[kNumTypes] = {0, 0, 0, 0, 0};
+  for (;;) {
+    if (threadIdx.x == 0) s_id = pop_task(p);
+    __syncthreads();
+    const int id = s_id;
+    __syncthreads();
+    if (id < 0) break;
+    const TaskDesc t = decode(p, id);
+    const long long c0 = clock64();
+    switch (t.type) {
+      case kGEQRT: {
+        const size_t o = tile_off(t.i, t.i, p.MT, NB);
+        task_geqrt(p.A + o, p.T + o, p.TAU + tau_off(t.i, t.i, p.MT, NB), p.sh, smem, p.sp);
+        break;
+      }
+      case kTSQRT: {
+        const size_t o1 = tile_off(t.i, t.i, p.MT, NB), o2 = tile_off(t.k, t.i, p.MT, NB);
+        task_tsqrt(p.A + o1, p.A + o2, p.T + o2, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.sh, smem, p.sp);
+        break;
+      }
+      case kTBUILD: {
+        const size_t o = tile_off(t.k, t.i, p.MT, NB);
+        task_tbuild(p.A + o, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.T + o, t.k == t.i, p.sh, smem, p.sp);
+        break;
+      }
+      case kLARFB: {
+        const size_t ov = tile_off(t.i, t.i, p.MT, NB), oc = tile_off(t.i, t.j, p.MT, NB);
+        task_larfb(p.A + ov, p.T + ov, p.C + oc, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp);
+        break;
+      }
+      case kSSRFB: {
+        const size_t ov = tile_off(t.k, t.i, p.MT, NB);
+        const size_t o1 = tile_off(t.i, t.j, p.MT, NB), o2 = tile_off(t.k, t.j, p.MT, NB);
+        task_ssrfb(p.C + o1, p.C + o2, p.A + ov, p.T + ov, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp);
+        break;
+      }
+      default:
+        if (threadIdx.x == 0) atomicOr((int*)(p.ctl + kErr), kErrBadTask);
+    }
+    (void)tsz;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      local_cnt[t.type]++;
+      local_cyc[t.type] += (unsigned long long)(clock64() - c0);
+      release_dependents(p, t);
+      __threadfence();
+      atomicAdd(p.ctl + kDone, 1u);
+    }
+  }
+  if (threadIdx.x == 0 && p.stats) {
+    for (int ty = 0; ty < kNumTypes; ty++) {
+      if (local_cnt[ty]) {
+        atomicAdd(p.stats + 2 * ty, local_cnt[ty]);
+        atomicAdd(p.stats + 2 * ty + 1, local_cyc[ty]);
+      }
+    }
+  }
+}
+
+}  // namespace hqr

@@ -1,0 +1,68 @@
+// hqr_internal.h -- host-side interfaces shared by the library's translation
+// units (not installed; the public C ABI is in include/).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "hqr_gpu.h"
+
+namespace hqr {
+
+// Geometry of one tiled matrix and the tile-kernel shape used on it.
+struct Geometry {
+  long M, N;       // rows / columns (multiples of NB)
+  int NB, IB;      // tile order / requested inner block
+  int MT, NT;      // tile rows / tile columns
+  int steps;       // min(MT, NT)
+  int w, CB, NC;   // inner block width, column-block width, column blocks per tile
+  size_t smem_bytes;
+};
+
+int make_geometry(long M, long N, int NB, int IB, Geometry* g);
+
+// Remember the text of a failed CUDA call (reported by hqr_last_cuda_error)
+// and return HQR_ERR_CUDA.
+int record_cuda_error(cudaError_t e, const char* where);
+
+// Scheduler workspace (dependency counters, queues, control words, stats).
+struct DagWorkspace {
+  int* cnt = nullptr;
+  int* qhi = nullptr;
+  int* qlo = nullptr;
+  unsigned* ctl = nullptr;
+  unsigned long long* stats = nullptr;
+  size_t cap_ids = 0;
+};
+
+int dag_workspace_reserve(DagWorkspace* ws, size_t n_ids);
+void dag_workspace_free(DagWorkspace* ws);
+
+// Enqueue a factorization DAG on `stream` (no synchronisation).
+int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, double* dTAU,
+                  long long timeout_ns, cudaStream_t stream);
+// Enqueue C <- Q^T C (C has CT tile columns, same MT/NB as A); rebuild_t: build
+// the diagonal T blocks from V/TAU first (T-build tasks), else use dT as is.
+int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT,
+                    const double* dTAU, double* dC, int CT, bool rebuild_t, long long timeout_ns,
+                    cudaStream_t stream);
+// Read and clear the scheduler's error word (synchronises `stream`).
+int dag_status(DagWorkspace* ws, cudaStream_t stream);
+int dag_stats(DagWorkspace* ws, unsigned long long out[10], cudaStream_t stream);
+int dag_sm_count();
+
+// Utility kernels (hqr_util.cu)
+void fill_uniform(double* dA, long M, long N, int NB, uint64_t seed, cudaStream_t s);
+void make_identity(double* dQ, long M, long N, int NB, bool zero_first, cudaStream_t s);
+void zero_reflectors(double* dA, long M, long N, int NB, cudaStream_t s);
+void dgemm_tn_tiles(const double* dA, const double* dB, double* dC, long M, long N, int NB,
+                    cudaStream_t s);
+// sum of squares of (X - alpha*I - Y) over the tile array (Y may be null);
+// result written to *d_out (device double).
+void frob_diff(const double* dX, const double* dY, double alpha_identity, long M, long N, int NB,
+               double* d_out, cudaStream_t s);
+void tiles_to_colmajor(const double* dT, double* dOut, long M, long N, int NB, cudaStream_t s);
+void colmajor_to_tiles(const double* dIn, double* dT, long M, long N, int NB, cudaStream_t s);
+void max_col_abs_sum(const double* dColMajor, long M, long N, double* d_out, cudaStream_t s);
+
+}  // namespace hqr

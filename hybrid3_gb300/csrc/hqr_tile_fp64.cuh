@@ -1,0 +1,490 @@
+// hqr_tile_fp64.cuh -- FP64 tile kernels of the tiled Householder QR, run by
+// one CTA of kThreads threads on CUDA cores.
+//
+// These restate, as block-cooperative CUDA, the four PLASMA CORE kernels that
+// Hybrid_tile_QR calls (Hybrid_tile_QR.c:985 CORE_dgeqrt, :1135 CORE_dtsqrt,
+// :1276 CORE_dormqr, :1356 CORE_dtsmqr):
+//   * reflectors follow LAPACK dlarfg: beta = -sign(alpha)*||[alpha; x]||,
+//     tau = 0 when x = 0, with the safe-minimum rescaling for tiny columns;
+//   * the factorization and its updates run in w-column inner blocks
+//     (w = min(IB, 32)); each block's w x w upper-triangular T is stored as a
+//     diagonal block of the panel tile's NB x NB T (the full T, whose diagonal
+//     w x w blocks are exactly the IB-blocked T of the LAPACK dgeqrt layout);
+//   * a block reflector is applied as W = V^T C, W = T^T W, C -= V W.
+//
+// Shared memory holds the panel / the column block being updated; V and T are
+// streamed from global memory (L2) in row chunks.  FP64 throughput on GB300 is
+// ~1 TFLOP/s per GPU, so the kernels are FP64-issue bound and favour simple
+// conflict-free shared-memory access over register blocking.
+#pragma once
+#include <cfloat>
+#include "hqr_common.cuh"
+
+namespace hqr {
+
+constexpr int kMaxW = 32;      // inner block width
+constexpr int kRC = 128;       // V row chunk staged per pass
+
+// Shape of the tile kernels for one (NB, IB) configuration.
+struct TileShape {
+  int NB;   // tile order
+  int w;    // inner block width = min(IB, kMaxW)
+  int CB;   // columns per LARFB/SSRFB column-block task
+  int RC;   // V row chunk
+};
+
+// Shared-memory carve-up, in doubles.  Computed identically on host and device.
+struct SmemPlan {
+  int off_c1, off_c2, off_vb, off_vt, off_t, off_g, off_w, off_w2, off_part, off_red, off_tau;
+  int total;
+  __host__ __device__ static SmemPlan make(const TileShape& s) {
+    SmemPlan p;
+    const int NB = s.NB, w = s.w, CB = s.CB;
+    // One region serves, one at a time: the GEQRT/TSQRT panel (NB x w), the
+    // LARFB column block (NB x CB), the SSRFB pair A1|A2 (2 x NB x CB) and the
+    // TSQRT trailing chunk R-rows|A2 (w x CB + NB x CB).
+    int region = NB * w;
+    if (2 * NB * CB > region) region = 2 * NB * CB;
+    if (w * CB + NB * CB > region) region = w * CB + NB * CB;
+    int o = 0;
+    p.off_c1 = o;
+    p.off_c2 = o + NB * CB;                // SSRFB A2
+    o += region;
+    p.off_vb = o; o += (s.RC + 1) * w;     // V row chunk (ld RC+1)
+    p.off_vt = o; o += w * w;              // unit-lower top of V / TSQRT R block
+    p.off_t = o; o += w * w;               // T block
+    p.off_g = o; o += w * w;               // Gram scratch of the T-block build
+    p.off_w = o; o += w * CB;
+    p.off_w2 = o; o += w * CB;
+    p.off_part = o; o += 2048;             // split-K partials (<= 256 items x 8)
+    p.off_red = o; o += 16;                // block reductions / broadcasts
+    p.off_tau = o; o += kMaxW;
+    p.total = o;
+    return p;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Reflector generation (LAPACK dlarfg), block-cooperative.
+// alpha: shared scalar; x: shared vector of n elements (unit stride).
+// On return *alpha = beta, x is scaled to v(1:n), *tau_out = tau.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double block_max(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < kWarps; i++) s = fmax(s, red[i]);
+  return s;
+}
+
+__device__ void block_larfg(double* alpha, double* x, int n, double* tau_out, double* red) {
+  double ss = 0.0;
+  for (int r = threadIdx.x; r < n; r += kThreads) {
+    const double v = x[r];
+    ss = fma(v, v, ss);
+  }
+  ss = block_sum(ss, red);
+  double xnorm;
+  if (ss == 0.0) {
+    xnorm = 0.0;
+  } else if (ss >= 1e-290 && ss <= 1e290) {
+    xnorm = sqrt(ss);
+  } else {  // scaled norm, as LAPACK dnrm2 does, for tiny or huge columns
+    double amax = 0.0;
+    for (int r = threadIdx.x; r < n; r += kThreads) amax = fmax(amax, fabs(x[r]));
+    amax = block_max(amax, red);
+    double s2 = 0.0;
+    for (int r = threadIdx.x; r < n; r += kThreads) {
+      const double v = x[r] / amax;
+      s2 = fma(v, v, s2);
+    }
+    s2 = block_sum(s2, red);
+    xnorm = amax * sqrt(s2);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = *alpha, tau = 0.0, beta = a, scal = 1.0;
+    int knt = 0;
+    if (xnorm != 0.0) {
+      const double safmin = DBL_MIN / (DBL_EPSILON * 0.5);
+      const double rsafmn = 1.0 / safmin;
+      double xn = xnorm;
+      beta = -copysign(hypot(a, xn), a);
+      while (fabs(beta) < safmin && knt < 20) {
+        knt++;
+        a *= rsafmn;
+        xn *= rsafmn;
+        beta = -copysign(hypot(a, xn), a);
+      }
+      tau = (beta - a) / beta;
+      scal = 1.0 / (a - beta);
+      for (int j = 0; j < knt; j++) beta *= safmin;
+    }
+    red[8] = tau;
+    red[9] = scal;
+    red[10] = (double)knt;
+    red[11] = beta;
+  }
+  __syncthreads();
+  const double tau = red[8], scal = red[9];
+  const int knt = (int)red[10];
+  if (tau != 0.0) {
+    const double rsafmn = 1.0 / (DBL_MIN / (DBL_EPSILON * 0.5));
+    for (int r = threadIdx.x; r < n; r += kThreads) {
+      double v = x[r];
+      for (int j = 0; j < knt; j++) v *= rsafmn;
+      x[r] = v * scal;
+    }
+  }
+  if (threadIdx.x == 0) {
+    *alpha = red[11];
+    *tau_out = tau;
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Unblocked QR of a shared panel (dgeqr2 semantics): P is m x w, ld ldp.
+// ---------------------------------------------------------------------------
+__device__ void panel_qr_ge(double* P, int ldp, int m, int w, double* tau, double* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int c = 0; c < w && c < m; c++) {
+    double* pc = P + (size_t)c * ldp;
+    block_larfg(pc + c, pc + c + 1, m - c - 1, tau + c, red);
+    const double t = tau[c];
+    if (t != 0.0) {
+      for (int j = c + 1 + warp; j < w; j += kWarps) {
+        double* pj = P + (size_t)j * ldp;
+        const double pcj = pj[c];
+        double s = 0.0;
+        for (int r = c + 1 + lane; r < m; r += 32) s = fma(pc[r], pj[r], s);
+        s = (warp_sum(s) + pcj) * t;
+        if (lane == 0) pj[c] = pcj - s;
+        for (int r = c + 1 + lane; r < m; r += 32) pj[r] = fma(-s, pc[r], pj[r]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Unblocked QR of the triangle-on-square panel [R; A]: R is w x w (upper part
+// used), A is m x w (dense).  Column c's reflector acts on [R(c,c); A(:,c)];
+// A(:, c) becomes v_c.  This is the per-column loop of CORE_dtsqrt.
+__device__ void panel_qr_ts(double* R, int ldr, double* A, int lda, int m, int w, double* tau,
+                            double* red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int c = 0; c < w; c++) {
+    double* ac = A + (size_t)c * lda;
+    block_larfg(R + c + (size_t)c * ldr, ac, m, tau + c, red);
+    const double t = tau[c];
+    if (t != 0.0) {
+      for (int j = c + 1 + warp; j < w; j += kWarps) {
+        double* aj = A + (size_t)j * lda;
+        double* rcj = R + c + (size_t)j * ldr;
+        const double r0 = *rcj;
+        double s = 0.0;
+        for (int r = lane; r < m; r += 32) s = fma(ac[r], aj[r], s);
+        s = (warp_sum(s) + r0) * t;
+        if (lane == 0) *rcj = r0 - s;
+        for (int r = lane; r < m; r += 32) aj[r] = fma(-s, ac[r], aj[r]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// T block (dlarft 'F','C') of a w-column block whose V is stored in shared
+// memory.  unit: V is unit lower (rows 0..w-1 hold the unit triangle, V(c,c)
+// = 1 implicit); otherwise V is dense (TS block, top part = identity).
+// G (w x w scratch) receives the needed Gram entries.  T (w x w, ld w) output.
+__device__ void build_t_block(const double* V, int ldv, int m, int w, bool unit, const double* tau,
+                              double* G, double* T) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int npairs = w * (w - 1) / 2;
+  for (int p = warp; p < npairs; p += kWarps) {
+    // decode p -> (a, c) with a < c
+    int c = 1, base = 0;
+    while (base + c <= p) { base += c; c++; }
+    const int a = p - base;
+    const double* va = V + (size_t)a * ldv;
+    const double* vc = V + (size_t)c * ldv;
+    double s = 0.0;
+    const int r0 = unit ? c + 1 : 0;
+    for (int r = r0 + lane; r < m; r += 32) s = fma(va[r], vc[r], s);
+    s = warp_sum(s);
+    if (lane == 0) G[a + c * w] = unit ? s + va[c] : s;
+  }
+  __syncthreads();
+  for (int c = 0; c < w; c++) {
+    const double tc = tau[c];
+    const int a = threadIdx.x;
+    if (a < c) {
+      double s = 0.0;
+      for (int b = a; b < c; b++) s = fma(T[a + b * w], G[b + c * w], s);
+      T[a + c * w] = (tc == 0.0) ? 0.0 : -tc * s;
+    } else if (a == c) {
+      T[c + c * w] = tc;
+    } else if (a < w) {
+      T[a + c * w] = 0.0;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Apply the transpose of one w-column block reflector H = I - V T V^T,
+// V = [Vt; Vb], to [Ct; Cb] held in shared memory:
+//     W = Vt^T Ct + Vb^T Cb;  W = T^T W;  Ct -= Vt W;  Cb -= Vb W.
+// Vt: w x w unit lower (unit_top) or the identity; Vb: mb x w.  V and T are
+// read from global memory (ld ldv / ldt).  ncol must be a multiple of 8.
+// ---------------------------------------------------------------------------
+__device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off,
+                              const double* __restrict__ gT, int ldt, int w, int mb, bool unit_top,
+                              double* Ct, int ldct, double* Cb, int ldcb, int ncol, double* smem,
+                              const SmemPlan& sp, int RC) {
+  double* sVb = smem + sp.off_vb;
+  double* sVt = smem + sp.off_vt;
+  double* sT = smem + sp.off_t;
+  double* sW = smem + sp.off_w;
+  double* sW2 = smem + sp.off_w2;
+  double* sPart = smem + sp.off_part;
+  const int tid = threadIdx.x;
+  const int ldvs = RC + 1;
+
+  // T block and the unit-lower top of V
+  for (int e = tid; e < w * w; e += kThreads) {
+    const int r = e % w, c = e / w;
+    sT[e] = (r <= c) ? ldg_cg(gT + r + (size_t)c * ldt) : 0.0;
+    if (unit_top) sVt[e] = (r > c) ? ldg_cg(gV + r + (size_t)c * ldv) : (r == c ? 1.0 : 0.0);
+  }
+
+  // ---- W = Vt^T Ct + Vb^T Cb -------------------------------------------
+  const int G8 = ncol >> 3;
+  const int outs = w * G8;                       // items per split
+  int S = kThreads / (outs > 0 ? outs : 1);
+  if (S < 1) S = 1;
+  const int item = tid;
+  const int a = item % w;
+  const int g = (item / w) % (G8 > 0 ? G8 : 1);
+  const int s = item / outs;
+  const bool active = (outs > 0) && (item < outs * S) && (s < S);
+  double acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) acc[q] = 0.0;
+  for (int r0 = 0; r0 < mb; r0 += RC) {
+    const int rc = min(RC, mb - r0);
+    __syncthreads();
+    for (int e = tid; e < rc * w; e += kThreads) {
+      const int r = e % rc, c = e / rc;
+      sVb[r + c * ldvs] = ldg_cg(gV + mb_off + r0 + r + (size_t)c * ldv);
+    }
+    __syncthreads();
+    if (active) {
+      const double* cb = Cb + r0 + (size_t)(8 * g) * ldcb;
+      for (int r = s; r < rc; r += S) {
+        const double v = sVb[r + a * ldvs];
+#pragma unroll
+        for (int q = 0; q < 8; q++) acc[q] = fma(v, cb[r + (size_t)q * ldcb], acc[q]);
+      }
+    }
+  }
+  __syncthreads();
+  if (active) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) sPart[(s * w + a) * 8 * G8 + g * 8 + q] = acc[q];
+  }
+  __syncthreads();
+  for (int e = tid; e < w * ncol; e += kThreads) {
+    const int aa = e % w, j = e / w;
+    double v = 0.0;
+    for (int ss = 0; ss < S; ss++) v += sPart[(ss * w + aa) * 8 * G8 + j];
+    double top = Ct[aa + (size_t)j * ldct];
+    if (unit_top)
+      for (int r = aa + 1; r < w; r++) top = fma(sVt[r + aa * w], Ct[r + (size_t)j * ldct], top);
+    sW[aa + j * w] = v + top;
+  }
+  __syncthreads();
+
+  // ---- W2 = T^T W ---------------------------------------------------------
+  for (int e = tid; e < w * ncol; e += kThreads) {
+    const int aa = e % w, j = e / w;
+    double v = 0.0;
+    for (int b = 0; b <= aa; b++) v = fma(sT[b + aa * w], sW[b + j * w], v);
+    sW2[aa + j * w] = v;
+  }
+  __syncthreads();
+
+  // ---- Ct -= Vt W2 ----------------------------------------------------------
+  for (int e = tid; e < w * ncol; e += kThreads) {
+    const int aa = e % w, j = e / w;
+    double v = sW2[aa + j * w];
+    if (unit_top)
+      for (int b = 0; b < aa; b++) v = fma(sVt[aa + b * w], sW2[b + j * w], v);
+    Ct[aa + (size_t)j * ldct] -= v;
+  }
+
+  // ---- Cb -= Vb W2 ----------------------------------------------------------
+  for (int r0 = 0; r0 < mb; r0 += RC) {
+    const int rc = min(RC, mb - r0);
+    __syncthreads();
+    for (int e = tid; e < rc * w; e += kThreads) {
+      const int r = e % rc, c = e / rc;
+      sVb[r + c * ldvs] = ldg_cg(gV + mb_off + r0 + r + (size_t)c * ldv);
+    }
+    __syncthreads();
+    for (int e = tid; e < rc * G8; e += kThreads) {
+      const int r = e % rc, gg = e / rc;
+      double acc2[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) acc2[q] = 0.0;
+      for (int b = 0; b < w; b++) {
+        const double v = sVb[r + b * ldvs];
+#pragma unroll
+        for (int q = 0; q < 8; q++) acc2[q] = fma(v, sW2[b + (8 * gg + q) * w], acc2[q]);
+      }
+      double* cb = Cb + r0 + r + (size_t)(8 * gg) * ldcb;
+#pragma unroll
+      for (int q = 0; q < 8; q++) cb[(size_t)q * ldcb] -= acc2[q];
+    }
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Task bodies.  All tile pointers are global (ld = NB).  T tiles are NB x NB;
+// the factorization writes their diagonal w x w blocks.
+// ---------------------------------------------------------------------------
+
+__device__ void load_block(double* s, int lds, const double* g, int ldg, int m, int n) {
+  for (int e = threadIdx.x; e < m * n; e += kThreads) {
+    const int r = e % m, c = e / m;
+    s[r + (size_t)c * lds] = ldg_cg(g + r + (size_t)c * ldg);
+  }
+}
+__device__ void store_block(double* g, int ldg, const double* s, int lds, int m, int n) {
+  for (int e = threadIdx.x; e < m * n; e += kThreads) {
+    const int r = e % m, c = e / m;
+    stg_cg(g + r + (size_t)c * ldg, s[r + (size_t)c * lds]);
+  }
+}
+
+// CORE_dgeqrt(NB, NB, IB, A, NB, T, NB, TAU)
+__device__ void task_geqrt(double* A, double* T, double* tau_g, const TileShape& sh, double* smem,
+                           const SmemPlan& sp) {
+  const int NB = sh.NB, w = sh.w;
+  double* sP = smem + sp.off_c1;
+  double* sTau = smem + sp.off_tau;
+  double* red = smem + sp.off_red;
+  double* sG = smem + sp.off_g;
+  double* sTb = smem + sp.off_t;
+  for (int i0 = 0; i0 < NB; i0 += w) {
+    const int m = NB - i0;
+    __syncthreads();
+    load_block(sP, NB, A + i0 + (size_t)i0 * NB, NB, m, w);
+    __syncthreads();
+    panel_qr_ge(sP, NB, m, w, sTau, red);
+    build_t_block(sP, NB, m, w, true, sTau, sG, sTb);
+    store_block(A + i0 + (size_t)i0 * NB, NB, sP, NB, m, w);
+    store_block(T + i0 + (size_t)i0 * NB, NB, sTb, w, w, w);
+    for (int e = threadIdx.x; e < w; e += kThreads) stg_cg(tau_g + i0 + e, sTau[e]);
+    __syncthreads();
+    for (int c0 = i0 + w; c0 < NB; c0 += sh.CB) {
+      const int ncol = min(sh.CB, NB - c0);
+      double* sC = smem + sp.off_c1;
+      __syncthreads();
+      load_block(sC, NB, A + i0 + (size_t)c0 * NB, NB, m, ncol);
+      __syncthreads();
+      apply_block_t(A + i0 + (size_t)i0 * NB, NB, w, T + i0 + (size_t)i0 * NB, NB, w, m - w, true,
+                    sC, NB, sC + w, NB, ncol, smem, sp, sh.RC);
+      store_block(A + i0 + (size_t)c0 * NB, NB, sC, NB, m, ncol);
+    }
+  }
+  __syncthreads();
+}
+
+// CORE_dtsqrt(NB, NB, IB, A1, NB, A2, NB, T, NB, TAU): A1 holds R (upper part)
+// above the GEQRT's V (strict lower part, left untouched).
+__device__ void task_tsqrt(double* A1, double* A2, double* T, double* tau_g, const TileShape& sh,
+                           double* smem, const SmemPlan& sp) {
+  const int NB = sh.NB, w = sh.w;
+  double* sA = smem + sp.off_c1;     // NB x w panel of A2
+  double* sR = smem + sp.off_vt;     // w x w block of R
+  double* sTau = smem + sp.off_tau;
+  double* red = smem + sp.off_red;
+  double* sG = smem + sp.off_g;
+  double* sTb = smem + sp.off_t;
+  for (int i0 = 0; i0 < NB; i0 += w) {
+    __syncthreads();
+    load_block(sA, NB, A2 + (size_t)i0 * NB, NB, NB, w);
+    load_block(sR, w, A1 + i0 + (size_t)i0 * NB, NB, w, w);
+    __syncthreads();
+    panel_qr_ts(sR, w, sA, NB, NB, w, sTau, red);
+    build_t_block(sA, NB, NB, w, false, sTau, sG, sTb);
+    store_block(A2 + (size_t)i0 * NB, NB, sA, NB, NB, w);
+    for (int e = threadIdx.x; e < w * w; e += kThreads) {
+      const int r = e % w, c = e / w;
+      if (r <= c) stg_cg(A1 + i0 + r + (size_t)(i0 + c) * NB, sR[r + c * w]);
+    }
+    store_block(T + i0 + (size_t)i0 * NB, NB, sTb, w, w, w);
+    for (int e = threadIdx.x; e < w; e += kThreads) stg_cg(tau_g + i0 + e, sTau[e]);
+    __syncthreads();
+    for (int c0 = i0 + w; c0 < NB; c0 += sh.CB) {
+      const int ncol = min(sh.CB, NB - c0);
+      double* sCt = smem + sp.off_c1;  // w x ncol rows of R (the panel area is free now)
+      double* sCb = smem + sp.off_c1 + w * sh.CB;  // NB x ncol of A2 after the R rows
+      __syncthreads();
+      load_block(sCt, w, A1 + i0 + (size_t)c0 * NB, NB, w, ncol);
+      load_block(sCb, NB, A2 + (size_t)c0 * NB, NB, NB, ncol);
+      __syncthreads();
+      apply_block_t(A2 + (size_t)i0 * NB, NB, 0, T + i0 + (size_t)i0 * NB, NB, w, NB, false, sCt, w,
+                    sCb, NB, ncol, smem, sp, sh.RC);
+      store_block(A1 + i0 + (size_t)c0 * NB, NB, sCt, w, w, ncol);
+      store_block(A2 + (size_t)c0 * NB, NB, sCb, NB, NB, ncol);
+    }
+  }
+  __syncthreads();
+}
+
+// CORE_dormqr(Left, Trans, NB, ncol, NB, IB, V, NB, T, NB, C, NB) on columns
+// [c0, c0+ncol) of C.
+__device__ void task_larfb(const double* V, const double* T, double* C, int c0, int ncol,
+                           const TileShape& sh, double* smem, const SmemPlan& sp) {
+  const int NB = sh.NB, w = sh.w;
+  double* sC = smem + sp.off_c1;
+  __syncthreads();
+  load_block(sC, NB, C + (size_t)c0 * NB, NB, NB, ncol);
+  __syncthreads();
+  for (int i0 = 0; i0 < NB; i0 += w) {
+    apply_block_t(V + i0 + (size_t)i0 * NB, NB, w, T + i0 + (size_t)i0 * NB, NB, w, NB - i0 - w, true,
+                  sC + i0, NB, sC + i0 + w, NB, ncol, smem, sp, sh.RC);
+  }
+  store_block(C + (size_t)c0 * NB, NB, sC, NB, NB, ncol);
+  __syncthreads();
+}
+
+// CORE_dtsmqr(Left, Trans, NB, ncol, NB, ncol, NB, IB, A1, NB, A2, NB, V, NB,
+// T, NB) on columns [c0, c0+ncol) of A1 and A2.
+__device__ void task_ssrfb(double* A1, double* A2, const double* V, const double* T, int c0,
+                           int ncol, const TileShape& sh, double* smem, const SmemPlan& sp) {
+  const int NB = sh.NB, w = sh.w;
+  double* s1 = smem + sp.off_c1;
+  double* s2 = smem + sp.off_c2;
+  __syncthreads();
+  load_block(s1, NB, A1 + (size_t)c0 * NB, NB, NB, ncol);
+  load_block(s2, NB, A2 + (size_t)c0 * NB, NB, NB, ncol);
+  __syncthreads();
+  for (int i0 = 0; i0 < NB; i0 += w) {
+    apply_block_t(V + (size_t)i0 * NB, NB, 0, T + i0 + (size_t)i0 * NB, NB, w, NB, false, s1 + i0, NB,
+                  s2, NB, ncol, smem, sp, sh.RC);
+  }
+  store_block(A1 + (size_t)c0 * NB, NB, s1, NB, NB, ncol);
+  store_block(A2 + (size_t)c0 * NB, NB, s2, NB, NB, ncol);
+  __syncthreads();
+}
+
+}  // namespace hqr

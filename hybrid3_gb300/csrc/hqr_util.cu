@@ -1,0 +1,206 @@
+// hqr_util.cu -- data-preparation and verification kernels around the QR path:
+// the seeded uniform generator, identity / reflector-zeroing (Hybrid_make_I,
+// the V zeroing of Hybrid_make_Q), the tile-wise C = A^T B of Hybrid_dgemm,
+// Frobenius-norm reductions and the max column abs-sum of mat_comp3.
+#include "hqr_common.cuh"
+#include "hqr_internal.h"
+
+namespace hqr {
+
+// splitmix64 of (seed, column-major index) -> 53-bit uniform in [0,1) -> 2u-1.
+__device__ __forceinline__ double uniform_pm1(uint64_t seed, uint64_t idx) {
+  uint64_t z = idx + seed * 0x9E3779B97F4A7C15ull + 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z = z ^ (z >> 31);
+  const double u = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+  return 2.0 * u - 1.0;
+}
+
+// Element e of the tile array -> (row, column) of the matrix.
+__device__ __forceinline__ void tile_rc(size_t e, int MT, int NB, long* r, long* c) {
+  const size_t t2 = (size_t)NB * NB;
+  const size_t tile = e / t2, in = e % t2;
+  const int ti = (int)(tile % MT), tj = (int)(tile / MT);
+  *r = (long)ti * NB + (long)(in % NB);
+  *c = (long)tj * NB + (long)(in / NB);
+}
+
+__global__ void k_fill_uniform(double* A, long M, long N, int NB, uint64_t seed) {
+  const int MT = (int)(M / NB);
+  const size_t n = (size_t)M * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    long r, c;
+    tile_rc(e, MT, NB, &r, &c);
+    A[e] = uniform_pm1(seed, (uint64_t)c * (uint64_t)M + (uint64_t)r);
+  }
+}
+
+__global__ void k_identity(double* Q, long M, long N, int NB, int zero_first) {
+  const int MT = (int)(M / NB);
+  const size_t n = (size_t)M * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    long r, c;
+    tile_rc(e, MT, NB, &r, &c);
+    if (r == c) Q[e] = 1.0;
+    else if (zero_first) Q[e] = 0.0;
+  }
+}
+
+// Zero V: the strictly lower part of the diagonal tiles (i,i) and every tile
+// (k,i), k > i, of the first min(MT, NT) tile columns.
+__global__ void k_zero_reflectors(double* A, long M, long N, int NB) {
+  const int MT = (int)(M / NB), NT = (int)(N / NB);
+  const int steps = MT < NT ? MT : NT;
+  const size_t n = (size_t)M * (size_t)steps * NB;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    long r, c;
+    tile_rc(e, MT, NB, &r, &c);
+    const long ti = r / NB, tj = c / NB;
+    if (ti > tj || (ti == tj && r > c)) A[e] = 0.0;
+  }
+}
+
+// C(i,j) = sum_k A(k,i)^T B(k,j) for tiles: one CTA per 64 x 64 output block.
+constexpr int kGB = 64, kGK = 16;
+__global__ void __launch_bounds__(256) k_dgemm_tn(const double* __restrict__ A, const double* __restrict__ B,
+                                                  double* __restrict__ C, long M, long N, int NB) {
+  const int MT = (int)(M / NB), NT = (int)(N / NB);
+  const int bpt = NB / kGB > 0 ? NB / kGB : 1;          // 64-blocks per tile side
+  const int nb_blk = (NB < kGB) ? NB : kGB;
+  const int ti = blockIdx.y / bpt, bi = blockIdx.y % bpt;
+  const int tj = blockIdx.x / bpt, bj = blockIdx.x % bpt;
+  if (ti >= NT || tj >= NT) return;
+  __shared__ double sA[kGK][kGB + 1];
+  __shared__ double sB[kGK][kGB + 1];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double acc[4][4] = {};
+  for (int tk = 0; tk < MT; tk++) {
+    const double* a = A + ((size_t)tk + (size_t)ti * MT) * NB * NB + (size_t)bi * nb_blk * NB;
+    const double* b = B + ((size_t)tk + (size_t)tj * MT) * NB * NB + (size_t)bj * nb_blk * NB;
+    for (int k0 = 0; k0 < NB; k0 += kGK) {
+      __syncthreads();
+      for (int e = threadIdx.x; e < kGK * kGB; e += 256) {
+        const int kk = e % kGK, col = e / kGK;
+        sA[kk][col] = (col < nb_blk) ? a[(size_t)col * NB + k0 + kk] : 0.0;
+        sB[kk][col] = (col < nb_blk) ? b[(size_t)col * NB + k0 + kk] : 0.0;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < kGK; kk++) {
+        double av[4], bv[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) { av[q] = sA[kk][ty + 16 * q]; bv[q] = sB[kk][tx + 16 * q]; }
+#pragma unroll
+        for (int p = 0; p < 4; p++)
+#pragma unroll
+          for (int q = 0; q < 4; q++) acc[p][q] = fma(av[p], bv[q], acc[p][q]);
+      }
+    }
+  }
+  double* c = C + ((size_t)ti + (size_t)tj * MT) * NB * NB + (size_t)bj * nb_blk * NB + (size_t)bi * nb_blk;
+#pragma unroll
+  for (int p = 0; p < 4; p++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int r = ty + 16 * p, col = tx + 16 * q;
+      if (r < nb_blk && col < nb_blk) c[(size_t)col * NB + r] = acc[p][q];
+    }
+}
+
+__global__ void k_frob_diff(const double* X, const double* Y, double alpha, long M, long N, int NB,
+                            double* out) {
+  const int MT = (int)(M / NB);
+  const size_t n = (size_t)M * N;
+  double s = 0.0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    double v = X[e];
+    if (Y) v -= Y[e];
+    if (alpha != 0.0) {
+      long r, c;
+      tile_rc(e, MT, NB, &r, &c);
+      if (r == c) v -= alpha;
+    }
+    s = fma(v, v, s);
+  }
+  s = warp_sum(s);
+  __shared__ double red[32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) atomicAdd(out, v);
+  }
+}
+
+__global__ void k_tiles_to_colmajor(const double* T, double* out, long M, long N, int NB, int to_cm) {
+  const int MT = (int)(M / NB);
+  const size_t n = (size_t)M * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    long r, c;
+    tile_rc(e, MT, NB, &r, &c);
+    const size_t cm = (size_t)c * M + r;
+    if (to_cm) out[cm] = T[e]; else out[e] = T[cm];
+  }
+}
+
+__global__ void k_max_col_abs_sum(const double* X, long M, long N, unsigned long long* out_bits) {
+  for (long c = blockIdx.x; c < N; c += gridDim.x) {
+    double s = 0.0;
+    for (long r = threadIdx.x; r < M; r += blockDim.x) s += fabs(X[(size_t)c * M + r]);
+    s = warp_sum(s);
+    __shared__ double red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); i++) t += red[i];
+      // non-negative doubles order like their bit patterns; NaN (all ones
+      // exponent, non-zero mantissa) sorts above +inf and so propagates.
+      atomicMax(out_bits, (unsigned long long)__double_as_longlong(t));
+    }
+    __syncthreads();
+  }
+}
+
+static int grid_for(size_t n) {
+  size_t g = (n + 255) / 256;
+  if (g > 152 * 32) g = 152 * 32;
+  return (int)(g ? g : 1);
+}
+
+void fill_uniform(double* dA, long M, long N, int NB, uint64_t seed, cudaStream_t s) {
+  k_fill_uniform<<<grid_for((size_t)M * N), 256, 0, s>>>(dA, M, N, NB, seed);
+}
+void make_identity(double* dQ, long M, long N, int NB, bool zero_first, cudaStream_t s) {
+  k_identity<<<grid_for((size_t)M * N), 256, 0, s>>>(dQ, M, N, NB, zero_first ? 1 : 0);
+}
+void zero_reflectors(double* dA, long M, long N, int NB, cudaStream_t s) {
+  k_zero_reflectors<<<grid_for((size_t)M * N), 256, 0, s>>>(dA, M, N, NB);
+}
+void dgemm_tn_tiles(const double* dA, const double* dB, double* dC, long M, long N, int NB,
+                    cudaStream_t s) {
+  const int NT = (int)(N / NB);
+  const int bpt = NB / kGB > 0 ? NB / kGB : 1;
+  dim3 grid(NT * bpt, NT * bpt);
+  k_dgemm_tn<<<grid, 256, 0, s>>>(dA, dB, dC, M, N, NB);
+}
+void frob_diff(const double* dX, const double* dY, double alpha_identity, long M, long N, int NB,
+               double* d_out, cudaStream_t s) {
+  cudaMemsetAsync(d_out, 0, sizeof(double), s);
+  k_frob_diff<<<grid_for((size_t)M * N), 256, 0, s>>>(dX, dY, alpha_identity, M, N, NB, d_out);
+}
+void tiles_to_colmajor(const double* dT, double* dOut, long M, long N, int NB, cudaStream_t s) {
+  k_tiles_to_colmajor<<<grid_for((size_t)M * N), 256, 0, s>>>(dT, dOut, M, N, NB, 1);
+}
+void colmajor_to_tiles(const double* dIn, double* dT, long M, long N, int NB, cudaStream_t s) {
+  k_tiles_to_colmajor<<<grid_for((size_t)M * N), 256, 0, s>>>(dIn, dT, M, N, NB, 0);
+}
+void max_col_abs_sum(const double* dColMajor, long M, long N, double* d_out, cudaStream_t s) {
+  cudaMemsetAsync(d_out, 0, sizeof(double), s);
+  int g = (int)(N < 152 * 8 ? N : 152 * 8);
+  k_max_col_abs_sum<<<g > 0 ? g : 1, 256, 0, s>>>(dColMajor, M, N, (unsigned long long*)d_out);
+}
+
+}  // namespace hqr

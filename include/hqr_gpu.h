@@ -1,0 +1,113 @@
+/*
+ * hqr_gpu.h -- extended C ABI of the GB300 tiled Householder QR.
+ *
+ * The drop-in entry points (Hybrid_tile_QR.h) take host arrays and end the
+ * process on error, as the reference does.  This interface is what they are
+ * built on: device pointers, CUDA streams (passed as void*), integer status
+ * codes, persisted T factors and a choice of arithmetic for the trailing
+ * updates.  All matrices use the tile layout of mat_prod.h (tile (i,j) of an
+ * MT x NT grid of NB x NB column-major tiles at (i + j*MT)*NB*NB; TAU block of
+ * tile (i,j) at (i + j*MT)*NB).
+ */
+#ifndef HYBRID3_GB300_HQR_GPU_H_
+#define HYBRID3_GB300_HQR_GPU_H_
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+/* Status codes. */
+#define HQR_OK 0
+#define HQR_ERR_INVALID (-1)     /* bad argument (shape, pointer, rank count) */
+#define HQR_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define HQR_ERR_TIMEOUT (-3)     /* a bounded device wait ran out (scheduler) */
+#define HQR_ERR_NOMEM (-4)       /* device allocation failed */
+#define HQR_ERR_UNSUPPORTED (-5) /* shape outside what the kernels support */
+#define HQR_ERR_DEVICE (-6)      /* a device-side consistency check failed */
+
+/* Arithmetic of the trailing updates (panels are always FP64). */
+#define HQR_PREC_FP64 0    /* FP64 on CUDA cores */
+#define HQR_PREC_OZAKI 1   /* split-precision slices on the tensor cores, FP64 recombination */
+
+/* Error behaviour of the drop-in (Hybrid_*, tile_*) entry points. */
+#define HQR_ERRORS_ABORT 0   /* print to stderr and exit(1) (the reference's MPI_Abort) */
+#define HQR_ERRORS_RETURN 1  /* print to stderr and return; see hqr_last_error() */
+
+typedef struct hqr_plan hqr_plan_t;
+
+/* Per-task-type execution counters of the last DAG run (device clock cycles
+ * summed over CTAs).  Index: 0 GEQRT, 1 TSQRT, 2 LARFB, 3 SSRFB, 4 T-build. */
+typedef struct {
+    unsigned long long count[5];
+    unsigned long long cycles[5];
+} hqr_stats_t;
+
+const char *hqr_status_string(int status);
+void hqr_set_error_mode(int mode);
+int hqr_last_error(void);
+/* Text of the last failed CUDA runtime call ("" if none). */
+const char *hqr_last_cuda_error(void);
+/* Device-side wait limit of the scheduler, in milliseconds (default 20000). */
+void hqr_set_timeout_ms(long long ms);
+
+/* A plan owns the device workspace for one (M, N, NB, IB, precision) shape:
+ * T factors of every panel tile (M*N doubles), the DAG's dependency counters
+ * and ready queues.  M and N must be multiples of NB; NB a multiple of 16 up
+ * to 512; IB a divisor of NB (inner blocks of min(IB, 32) columns are used). */
+int hqr_plan_create(hqr_plan_t **plan, long M, long N, int NB, int IB, int precision);
+int hqr_plan_destroy(hqr_plan_t *plan);
+/* Device T factors of the last factorization: NB x NB upper-triangular tile
+ * per panel tile, same tile layout as A (only the w x w diagonal blocks are
+ * written by the factorization). */
+double *hqr_plan_t_factors(hqr_plan_t *plan);
+
+/* In-place factorization of dA (device), TAU to dTAU (MT*NT*NB doubles).
+ * hqr_geqrf waits for completion and reports device-side errors;
+ * hqr_geqrf_async only enqueues (check with hqr_plan_status). */
+int hqr_geqrf(hqr_plan_t *plan, double *dA, double *dTAU, void *stream);
+int hqr_geqrf_async(hqr_plan_t *plan, double *dA, double *dTAU, void *stream);
+/* Synchronise `stream`, then read and clear the scheduler's error word. */
+int hqr_plan_status(hqr_plan_t *plan, void *stream);
+int hqr_plan_stats(hqr_plan_t *plan, hqr_stats_t *out, void *stream);
+
+/* Hybrid_make_Q semantics on device arrays: dQ (M x N) <- Q^T I; the
+ * reflectors of dRY are zeroed (dRY becomes R).  use_plan_t: 1 reuses the T
+ * factors persisted by the last hqr_geqrf on this plan, 0 rebuilds them from
+ * V and TAU. */
+int hqr_make_q(hqr_plan_t *plan, double *dQ, double *dRY, const double *dTAU, int use_plan_t,
+               void *stream);
+int hqr_make_q_async(hqr_plan_t *plan, double *dQ, double *dRY, const double *dTAU,
+                     int use_plan_t, void *stream);
+/* Hybrid_dormqr semantics: dC <- Q^T dC, dC an MT x CT tile grid (CT tile
+ * columns of NB, e.g. CT = 1 for up to NB right-hand sides padded to NB). */
+int hqr_ormqr_t(hqr_plan_t *plan, const double *dRY, const double *dTAU, double *dC, int CT,
+                int use_plan_t, void *stream);
+
+/* Tile-wise C = A^T B of square tiled matrices (Hybrid_dgemm). */
+int hqr_dgemm_tn(long N, int NB, const double *dA, const double *dB, double *dC, void *stream);
+/* Identity in tile layout (Hybrid_make_I). */
+int hqr_make_identity(long M, long N, int NB, double *dQ, void *stream);
+/* Seeded i.i.d. uniform[-1,1) matrix in tile layout: element (r, c) is
+ * 2u-1, u = top 53 bits of splitmix64(r + c*M + (seed+1)*0x9E3779B97F4A7C15). */
+int hqr_fill_uniform(long M, long N, int NB, uint64_t seed, double *dA, void *stream);
+/* ||X - Y - alpha*I||_F^2 over tiled arrays (Y may be NULL), result on the host. */
+int hqr_frob2(long M, long N, int NB, const double *dX, const double *dY, double alpha,
+              double *result, void *stream);
+/* Tile layout <-> column-major (ld = M). */
+int hqr_tiles_to_colmajor(long M, long N, int NB, const double *dT, double *dCM, void *stream);
+int hqr_colmajor_to_tiles(long M, long N, int NB, const double *dCM, double *dT, void *stream);
+/* Zero the reflectors below the diagonal (Hybrid_remv_Y). */
+int hqr_zero_reflectors(long M, long N, int NB, double *dA, void *stream);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#ifdef __cplusplus
+}
+#endif
+#endif
