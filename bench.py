@@ -1,0 +1,388 @@
+#!/usr/bin/env python3
+"""Tiled Householder QR benchmark: factorization + explicit Q generation.
+
+Workload (one step): A (n x n, i.i.d. uniform[-1,1) from a fixed seed, tile
+layout, NB x NB tiles) is factored in place (Hybrid_tile_QR semantics) and the
+explicit Q is generated (Hybrid_make_Q semantics: Q^T into a zeroed array, the
+reflectors removed from A).  Throughput counts algorithmic flops only:
+factorization 2mn^2 - 2n^3/3 plus Q generation (LAPACK dorgqr count with
+k = n) 4mnk - 2(m+n)k^2 + 4k^3/3 -- 8/3 n^3 for a square matrix.
+
+Arms:
+  default            the GB300 library, inputs resident in HBM (`value`), and
+                     the same workload end to end through the drop-in C entry
+                     points with pinned host buffers (`e2e`)
+  --impl reference   the reference's CPU implementation of the path on this
+                     host's cores, on a bounded sample of the same workload
+
+Multi-GPU (torchrun): one independent replica per GPU ("replicas only": the
+path has no exchange step); value = all ranks' flops / max over ranks of time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "tile-QR TFLOP/s at FP64-level backward error: split-precision vs plain FP64"
+DP = ctypes.POINTER(ctypes.c_double)
+
+
+def qr_flops(m: int, n: int) -> float:
+    return 2.0 * m * n * n - 2.0 * n ** 3 / 3.0
+
+
+def orgqr_flops(m: int, n: int, k: int) -> float:
+    return 4.0 * m * n * k - 2.0 * (m + n) * k * k + 4.0 * k ** 3 / 3.0
+
+
+def step_flops(m: int, n: int) -> float:
+    return qr_flops(m, n) + orgqr_flops(m, n, n)
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the reference's algorithm on the host cores)
+# ---------------------------------------------------------------------------
+def cpu_sample(n: int, NB: int, IB: int, threads: int):
+    """One factorization + Q generation of an n x n sample on the host.
+    Uses the reference's own build when it can be loaded here, else the
+    oracle's task-DAG restatement.  Returns (seconds, kind)."""
+    import oracle as O
+    A = O.to_tiles(O.uniform_matrix(n, n, 20151130), NB)
+    kind = "port"
+    if O.ref_available() and os.environ.get("OMP_NUM_THREADS", "").startswith("1,"):
+        try:
+            O.ref_lib()
+            kind = "reference"
+        except OSError:
+            kind = "port"
+    if kind == "reference":
+        t0 = time.perf_counter()
+        a, tau = O.ref_tile_qr(A, n, n, NB, IB)
+        O.ref_make_Q(a, tau, n, n, NB, IB)
+        return time.perf_counter() - t0, kind
+    L = O.lib()
+    L.orc_tile_qr_dag.restype = ctypes.c_int
+    L.orc_tile_qr_dag.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_int, ctypes.c_int, DP, DP]
+    L.orc_make_Q_dag.restype = None
+    L.orc_make_Q_dag.argtypes = [ctypes.c_long, ctypes.c_long, ctypes.c_int, DP, DP, DP]
+    O.set_threads(threads)
+    a = A.copy()
+    tau = np.zeros((n // NB) ** 2 * NB)
+    q = np.zeros(n * n)
+    t0 = time.perf_counter()
+    L.orc_tile_qr_dag(n, n, NB, IB, O.ptr(a), O.ptr(tau))
+    L.orc_make_Q_dag(n, n, NB, O.ptr(q), O.ptr(a), O.ptr(tau))
+    return time.perf_counter() - t0, kind
+
+
+def run_reference(args, rank: int):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n = args.cpu_n
+    for _ in range(args.warmup):
+        cpu_sample(n, args.nb, args.ib, threads)
+    times = []
+    kind = "port"
+    for _ in range(args.steps):
+        t, kind = cpu_sample(n, args.nb, args.ib, threads)
+        times.append(t)
+    total = sum(times)
+    value = args.steps * step_flops(n, n) / total / 1e12
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": "TFLOP/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"tiled QR + Q generation, sample n={n} of the n={args.n} "
+                               f"workload, NB={args.nb}, IB={args.ib}, uniform[-1,1) seed 20151130",
+                   "n": args.n, "sample_n": n, "NB": args.nb, "IB": args.ib},
+        "cpu_baseline": {"value": round(value, 6), "unit": "TFLOP/s", "cores": threads,
+                         "kind": kind, "sample": f"{n}x{n} factorization + make_Q per step"},
+        "e2e": {"value": round(value, 6), "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# the GB300 arm
+# ---------------------------------------------------------------------------
+def load_traffic(n: int, NB: int):
+    """DRAM bytes per factorization launch from the committed ncu summary
+    (captured on a smaller case and scaled by the flop ratio, see profiles/)."""
+    p = os.path.join(ROOT, "profiles", "dag_exec_kernel_traffic.json")
+    if not os.path.exists(p):
+        return None
+    try:
+        d = json.load(open(p))
+        cap_n = d["n"]
+        scale = qr_flops(n, n) / qr_flops(cap_n, cap_n)
+        return int(d["dram_bytes_per_factor_launch"] * scale)
+    except Exception:
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--nb", type=int, default=256)
+    ap.add_argument("--ib", type=int, default=32)
+    ap.add_argument("--precision", default="fp64", choices=["fp64"])
+    ap.add_argument("--cpu-n", type=int, default=4096, help="CPU sample order")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+    import hybrid3_gb300 as H
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA device")
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    L = H.lib()
+    L.hqr_set_error_mode(H.HQR_ERRORS_RETURN)
+
+    n, NB, IB = args.n, args.nb, args.ib
+    M = N = n
+    ntau = (M // NB) * (N // NB) * NB
+    stream = torch.cuda.Stream()
+    s = stream.cuda_stream
+    f64 = torch.float64
+    dA0 = torch.empty(M * N, dtype=f64, device="cuda")
+    dA = torch.empty_like(dA0)
+    dQ = torch.empty_like(dA0)
+    dTAU = torch.zeros(ntau, dtype=f64, device="cuda")
+    H.check(L.hqr_fill_uniform(M, N, NB, 20151130, dA0.data_ptr(), s), "fill")
+    plan = H.Plan(M, N, NB, IB, H.HQR_PREC_FP64)
+
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def step(rec=None):
+        with torch.cuda.stream(stream):
+            dA.copy_(dA0, non_blocking=True)
+            if rec:
+                rec[0].record(stream)
+            H.check(L.hqr_geqrf_async(plan.h, dA.data_ptr(), dTAU.data_ptr(), s), "geqrf")
+            if rec:
+                rec[1].record(stream)
+            dQ.zero_()
+            if rec:
+                rec[2].record(stream)
+            H.check(L.hqr_make_q_async(plan.h, dQ.data_ptr(), dA.data_ptr(), dTAU.data_ptr(), 1, s),
+                    "make_q")
+            if rec:
+                rec[3].record(stream)
+
+    peak_fp64 = L.hqr_fp64_peak_tflops(s)
+    for _ in range(args.warmup):
+        step()
+    H.check(L.hqr_plan_status(plan.h, s), "warm-up run")
+
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    recs = [[ev(), ev(), ev(), ev()] for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_start, t_end = ev(), ev()
+    with torch.cuda.stream(stream):
+        t_start.record(stream)
+    for r in recs:
+        step(r)
+    with torch.cuda.stream(stream):
+        t_end.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    H.check(L.hqr_plan_status(plan.h, s), "timed run")
+    elapsed = t_start.elapsed_time(t_end) / 1e3
+    if dist:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    fact_s = [r[0].elapsed_time(r[1]) / 1e3 for r in recs]
+    mq_s = [r[2].elapsed_time(r[3]) / 1e3 for r in recs]
+    flops = step_flops(M, N)
+    value = world * args.steps * flops / elapsed / 1e12
+    stats = plan.stats(s)
+
+    # accuracy of the last step (on the device, FP64): ||A - Q R||_F / ||A||_F and
+    # ||I - Q Q^T||_F from the Q^T array, as main.c:201-258 checks them
+    acc = {}
+    if not args.no_check:
+        dW = torch.empty_like(dA0)
+        r2 = ctypes.c_double()
+        H.check(L.hqr_dgemm_tn(N, NB, dQ.data_ptr(), dA.data_ptr(), dW.data_ptr(), s), "QR")
+        H.check(L.hqr_frob2(M, N, NB, dW.data_ptr(), dA0.data_ptr(), 0.0, ctypes.byref(r2), s), "frob")
+        a2 = ctypes.c_double()
+        H.check(L.hqr_frob2(M, N, NB, dA0.data_ptr(), None, 0.0, ctypes.byref(a2), s), "frob")
+        acc["resid_fro_rel"] = float(np.sqrt(r2.value / a2.value))
+        H.check(L.hqr_dgemm_tn(N, NB, dQ.data_ptr(), dQ.data_ptr(), dW.data_ptr(), s), "QQt")
+        H.check(L.hqr_frob2(M, N, NB, dW.data_ptr(), None, 1.0, ctypes.byref(r2), s), "frob")
+        acc["orth_fro"] = float(np.sqrt(r2.value))
+        del dW
+
+    # end to end through the drop-in C entry points with pinned host buffers
+    e2e = None
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else args.steps
+    if e2e_steps > 0:
+        hA0 = torch.empty(M * N, dtype=f64, pin_memory=True)
+        hA0.copy_(dA0.cpu())
+        hA = torch.empty_like(hA0).pin_memory()
+        hQ = torch.empty_like(hA0).pin_memory()
+        hTAU = torch.zeros((M // 2) * (N // 2), dtype=f64).pin_memory()
+        st = H.status(M, N, NB)
+        pa = ctypes.cast(hA.data_ptr(), DP)
+        pq = ctypes.cast(hQ.data_ptr(), DP)
+        pt = ctypes.cast(hTAU.data_ptr(), DP)
+        del dA, dQ
+        torch.cuda.empty_cache()
+        times = []
+        for it in range(1 + e2e_steps):
+            hA.copy_(hA0)
+            hQ.zero_()
+            t0 = time.perf_counter()
+            L.Hybrid_tile_QR(ctypes.byref(st), pa, pt, 0, 1, IB)
+            H.check(L.hqr_last_error(), "Hybrid_tile_QR")
+            L.Hybrid_make_Q(ctypes.byref(st), pq, pa, pt, 0, 1, IB)
+            H.check(L.hqr_last_error(), "Hybrid_make_Q")
+            if it > 0:
+                times.append(time.perf_counter() - t0)
+        t_e2e = sum(times)
+        if dist:
+            t = torch.tensor([t_e2e], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            t_e2e = float(t.item())
+        nbytes = M * N * 8
+        tau_b = ntau * 8
+        e2e = {"value": round(world * e2e_steps * flops / t_e2e / 1e12, 6), "unit": "TFLOP/s",
+               # Hybrid_tile_QR: A, TAU in and out; Hybrid_make_Q: RY, TAU, Q in, Q and RY out
+               "h2d_bytes_per_step": 2 * nbytes + tau_b + nbytes + tau_b + nbytes,
+               "d2h_bytes_per_step": nbytes + tau_b + nbytes + nbytes,
+               "steps": e2e_steps, "warmup": 1, "api": "Hybrid_tile_QR + Hybrid_make_Q (host arrays)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        t, kind = cpu_sample(args.cpu_n, NB, IB, os.cpu_count() or 1)
+        cpu = {"value": round(step_flops(args.cpu_n, args.cpu_n) / t / 1e12, 6), "unit": "TFLOP/s",
+               "cores": os.cpu_count() or 1, "kind": kind,
+               "sample": f"one {args.cpu_n}x{args.cpu_n} factorization + make_Q (NB={NB}, IB={IB})"}
+
+    fact_mean = float(np.mean(fact_s))
+    achieved = qr_flops(M, N) / fact_mean / 1e12
+    roofline = {"kernel": "dag_exec_kernel (factorization launch)", "bound": "fp64",
+                "achieved": round(achieved, 4), "peak": round(peak_fp64, 4), "unit": "TFLOP/s",
+                "frac": round(achieved / peak_fp64, 4) if peak_fp64 > 0 else None,
+                "peak_source": "FP64 FMA issue rate measured in this run (hqr_fp64_peak_tflops); "
+                               "MEASURED_PEAKS.json holds no FP64 figure",
+                "traffic": load_traffic(n, NB),
+                "algorithmic_flops_per_launch": qr_flops(M, N)}
+    launches_per_step = 3 + 5
+    line = {
+        "metric": METRIC, "value": round(value, 6), "unit": "TFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * elapsed / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"tiled QR + Q generation (make_Q), n={n} square, NB={NB}, IB={IB}, "
+                               "uniform[-1,1) seed 20151130",
+                   "n": n, "NB": NB, "IB": IB, "precision": "fp64 (plain)",
+                   "l2": "inputs (2 GiB per matrix) exceed the 129 MB L2; no flush",
+                   "parallelism": f"replicas x{world}"},
+        "phases_ms": {"factor": round(1e3 * fact_mean, 3), "make_q": round(1e3 * float(np.mean(mq_s)), 3)},
+        "accuracy": acc,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clk,
+        "task_counts": stats["count"],
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    plan.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -106,6 +106,7 @@ SIGNATURES = {
     "hqr_tiles_to_colmajor": (_I, [_L, _L, _I, _vp, _vp, _vp]),
     "hqr_colmajor_to_tiles": (_I, [_L, _L, _I, _vp, _vp, _vp]),
     "hqr_zero_reflectors": (_I, [_L, _L, _I, _vp, _vp]),
+    "hqr_fp64_peak_tflops": (_D, [_vp]),
 }
 
 _lib = None

@@ -269,6 +269,10 @@ int hqr_colmajor_to_tiles(long M, long N, int NB, const double* dCM, double* dT,
   return cuda_rc(cudaGetLastError());
 }
 
+double hqr_fp64_peak_tflops(void* stream) {
+  return hqr::measure_fp64_peak_tflops((cudaStream_t)stream);
+}
+
 int hqr_zero_reflectors(long M, long N, int NB, double* dA, void* stream) {
   if (!dA || NB <= 0 || M % NB || N % NB) return HQR_ERR_INVALID;
   hqr::zero_reflectors(dA, M, N, NB, (cudaStream_t)stream);

@@ -64,5 +64,6 @@ void frob_diff(const double* dX, const double* dY, double alpha_identity, long M
 void tiles_to_colmajor(const double* dT, double* dOut, long M, long N, int NB, cudaStream_t s);
 void colmajor_to_tiles(const double* dIn, double* dT, long M, long N, int NB, cudaStream_t s);
 void max_col_abs_sum(const double* dColMajor, long M, long N, double* d_out, cudaStream_t s);
+double measure_fp64_peak_tflops(cudaStream_t s);
 
 }  // namespace hqr

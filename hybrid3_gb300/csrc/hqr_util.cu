@@ -164,6 +164,44 @@ __global__ void k_max_col_abs_sum(const double* X, long M, long N, unsigned long
   }
 }
 
+// FP64 FMA issue-rate probe: the roofline denominator of the FP64 tile kernels
+// (independent FMA chains, no memory traffic).
+constexpr int kPeakIter = 2048;
+__global__ void k_fp64_peak(double* out, double b, double c) {
+  double a0 = threadIdx.x, a1 = a0 + 1, a2 = a0 + 2, a3 = a0 + 3, a4 = a0 + 4, a5 = a0 + 5,
+         a6 = a0 + 6, a7 = a0 + 7;
+  for (int i = 0; i < kPeakIter; i++) {
+    a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+    a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+double measure_fp64_peak_tflops(cudaStream_t s) {
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = nsm * 8, threads = 256;
+  double* out = nullptr;
+  if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return -1.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_fp64_peak<<<blocks, threads, 0, s>>>(out, 1.0000001, 1e-9);   // warm-up
+  cudaEventRecord(e0, s);
+  const int reps = 5;
+  for (int r = 0; r < reps; r++) k_fp64_peak<<<blocks, threads, 0, s>>>(out, 1.0000001, 1e-9);
+  cudaEventRecord(e1, s);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  const double flops = (double)reps * blocks * threads * kPeakIter * 8 * 2.0;
+  return ms > 0 ? flops / (ms * 1e-3) / 1e12 : -1.0;
+}
+
 static int grid_for(size_t n) {
   size_t g = (n + 255) / 256;
   if (g > 152 * 32) g = 152 * 32;

@@ -101,6 +101,9 @@ int hqr_frob2(long M, long N, int NB, const double *dX, const double *dY, double
 /* Tile layout <-> column-major (ld = M). */
 int hqr_tiles_to_colmajor(long M, long N, int NB, const double *dT, double *dCM, void *stream);
 int hqr_colmajor_to_tiles(long M, long N, int NB, const double *dCM, double *dT, void *stream);
+/* Measured FP64 FMA issue rate of this GPU in TFLOP/s (a ~10 ms probe of
+ * independent FMA chains): the roofline denominator of the FP64 kernels. */
+double hqr_fp64_peak_tflops(void *stream);
 /* Zero the reflectors below the diagonal (Hybrid_remv_Y). */
 int hqr_zero_reflectors(long M, long N, int NB, double *dA, void *stream);
 

@@ -180,6 +180,7 @@ static void orc_dlarfb_lt(int m, int n, int k, const double *V, int ldv,
         for (int a = 0; a < k; a++) {
             const double *va = V + (long)a * ldv;
             double s = c[a];                 /* unit diagonal */
+            #pragma omp simd reduction(+:s)
             for (int r = a + 1; r < m; r++) s += va[r] * c[r];
             W[a + (long)j * k] = s;
         }
@@ -220,6 +221,7 @@ static void orc_tsrfb_lt(int k, int n, int m2, double *A1, int lda1,
         for (int a = 0; a < k; a++) {
             const double *va = V + (long)a * ldv;
             double s = a1[a];
+            #pragma omp simd reduction(+:s)
             for (int r = 0; r < m2; r++) s += va[r] * a2[r];
             W[a + (long)j * k] = s;
         }
@@ -938,4 +940,114 @@ ORC_EXPORT void orc_dormqr(long M, long N, int NB, const double *RY, const doubl
     }
     free(Y);
     free(T);
+}
+
+/* ---------------------------------------------------------------------------
+ * Task-parallel drivers (the CPU baseline).  The same tile kernels as above,
+ * scheduled like the reference's dynamic DAG (Hybrid_tile_QR.c:905-1461):
+ * OpenMP task dependences on tiles stand for its MEM/LIN/YTM bits, and the
+ * GEQRT tile is copied for its LARFB row (the reference's glob_YT copy,
+ * Hybrid_tile_QR.c:1066-1071) so that the TS chain does not wait for that row.
+ * ------------------------------------------------------------------------- */
+ORC_EXPORT int orc_tile_qr_dag(long M, long N, int NB, int IB, double *A, double *TAU)
+{
+    int MT = (int)(M / NB), NT = (int)(N / NB);
+    int steps = imin(MT, NT);
+    const size_t t2 = (size_t)NB * NB;
+    double *Tall = (double *)calloc((size_t)M * (size_t)N, sizeof(double));
+    double *Ycopy = (double *)calloc((size_t)steps * t2, sizeof(double));
+    double *Tcopy = (double *)calloc((size_t)steps * t2, sizeof(double));
+    if (!Tall || !Ycopy || !Tcopy) { free(Tall); free(Ycopy); free(Tcopy); return -1; }
+    #pragma omp parallel num_threads(orc_nthreads)
+    #pragma omp single
+    for (int i = 0; i < steps; i++) {
+        double *aii = TILE(A, i, i), *tii = TILE(Tall, i, i);
+        double *yc = Ycopy + (size_t)i * t2, *tc = Tcopy + (size_t)i * t2;
+        #pragma omp task depend(inout: aii[0]) depend(out: yc[0]) firstprivate(aii, tii, yc, tc, i)
+        {
+            orc_core_dgeqrt(NB, NB, IB, aii, NB, tii, NB, TAUP(TAU, i, i));
+            memcpy(yc, aii, sizeof(double) * t2);
+            memcpy(tc, tii, sizeof(double) * t2);
+        }
+        for (int j = i + 1; j < NT; j++) {
+            double *aij = TILE(A, i, j);
+            #pragma omp task depend(in: yc[0]) depend(inout: aij[0]) firstprivate(aij, yc, tc)
+            orc_core_dormqr(NB, NB, NB, IB, yc, NB, tc, NB, aij, NB);
+        }
+        for (int k = i + 1; k < MT; k++) {
+            double *aki = TILE(A, k, i), *tki = TILE(Tall, k, i);
+            #pragma omp task depend(inout: aii[0], aki[0]) firstprivate(aii, aki, tki, k, i)
+            orc_core_dtsqrt(NB, NB, IB, aii, NB, aki, NB, tki, NB, TAUP(TAU, k, i));
+            for (int j = i + 1; j < NT; j++) {
+                double *aij = TILE(A, i, j), *akj = TILE(A, k, j);
+                #pragma omp task depend(in: aki[0]) depend(inout: aij[0], akj[0]) firstprivate(aij, akj, aki, tki)
+                orc_core_dtsmqr(NB, NB, NB, NB, NB, IB, aij, NB, akj, NB, aki, NB, tki, NB);
+            }
+        }
+    }
+    free(Tall);
+    free(Ycopy);
+    free(Tcopy);
+    return 0;
+}
+
+/* Hybrid_make_Q (Hybrid_make_Q.c:56-237) as a task DAG: the full-NB T of
+ * every panel tile is built as a task, then each Q tile column runs its own
+ * chain of LARFB/SSRFB tasks; V is zeroed at the end. */
+ORC_EXPORT void orc_make_Q_dag(long M, long N, int NB, double *Q, double *RY, double *TAU)
+{
+    int MT = (int)(M / NB), NT = (int)(N / NB);
+    int steps = imin(MT, NT);
+    const size_t t2 = (size_t)NB * NB;
+    double *Tall = (double *)calloc((size_t)M * (size_t)N, sizeof(double));
+    double *Yd = (double *)calloc((size_t)steps * t2, sizeof(double));
+    for (int c = 0; c < NT; c++) {
+        double *q = TILE(Q, c, c);
+        for (int r = 0; r < NB; r++) q[r + (long)r * NB] = 1.0;
+    }
+    #pragma omp parallel num_threads(orc_nthreads)
+    #pragma omp single
+    {
+        for (int gi = 0; gi < steps; gi++) {
+            double *ry = TILE(RY, gi, gi), *y = Yd + (size_t)gi * t2, *t = TILE(Tall, gi, gi);
+            #pragma omp task depend(out: t[0]) firstprivate(ry, y, t, gi)
+            {
+                for (int ii = 0; ii < NB - 1; ii++) {
+                    for (int r = ii + 1; r < NB; r++) y[r + (long)ii * NB] = ry[r + (long)ii * NB];
+                    y[ii + (long)ii * NB] = 1.0;
+                }
+                y[t2 - 1] = 0.0;
+                orc_dlarft_fc(NB, NB, y, NB, TAUP(TAU, gi, gi), t, NB);
+            }
+            for (int k = gi + 1; k < MT; k++) {
+                double *v = TILE(RY, k, gi), *tk = TILE(Tall, k, gi);
+                #pragma omp task depend(out: tk[0]) firstprivate(v, tk, k, gi)
+                orc_dtsrft(NB, NB, NB, v, NB, TAUP(TAU, k, gi), tk, NB);
+            }
+        }
+        for (int gi = 0; gi < steps; gi++) {
+            double *y = Yd + (size_t)gi * t2, *t = TILE(Tall, gi, gi);
+            for (int j = 0; j < NT; j++) {
+                double *qij = TILE(Q, gi, j);
+                #pragma omp task depend(in: t[0]) depend(inout: qij[0]) firstprivate(y, t, qij)
+                orc_core_dormqr(NB, NB, NB, NB, y, NB, t, NB, qij, NB);
+            }
+            for (int k = gi + 1; k < MT; k++) {
+                double *v = TILE(RY, k, gi), *tk = TILE(Tall, k, gi);
+                for (int j = 0; j < NT; j++) {
+                    double *qij = TILE(Q, gi, j), *qkj = TILE(Q, k, j);
+                    #pragma omp task depend(in: tk[0]) depend(inout: qij[0], qkj[0]) firstprivate(v, tk, qij, qkj)
+                    orc_core_dtsmqr(NB, NB, NB, NB, NB, NB, qij, NB, qkj, NB, v, NB, tk, NB);
+                }
+            }
+        }
+    }
+    for (int gi = 0; gi < steps; gi++) {
+        double *ry = TILE(RY, gi, gi);
+        for (int c = 0; c < NB; c++)
+            for (int r = c + 1; r < NB; r++) ry[r + (long)c * NB] = 0.0;
+        for (int k = gi + 1; k < MT; k++) memset(TILE(RY, k, gi), 0, sizeof(double) * t2);
+    }
+    free(Tall);
+    free(Yd);
 }
