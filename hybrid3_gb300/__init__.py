@@ -94,6 +94,7 @@ SIGNATURES = {
     "hqr_plan_t_factors": (_vp, [_vp]),
     "hqr_geqrf": (_I, [_vp, _vp, _vp, _vp]),
     "hqr_geqrf_async": (_I, [_vp, _vp, _vp, _vp]),
+    "hqr_geqrf_noalloc": (_I, [_L, _L, _I, _I, _vp, _vp, _vp]),
     "hqr_plan_status": (_I, [_vp, _vp]),
     "hqr_plan_stats": (_I, [_vp, ctypes.POINTER(HqrStats), _vp]),
     "hqr_make_q": (_I, [_vp, _vp, _vp, _vp, _I, _vp]),

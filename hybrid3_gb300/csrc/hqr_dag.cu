@@ -2,6 +2,7 @@
 // of the persistent executor for the factorization and the Q^T application.
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 
 #include "hqr_dag.cuh"
 #include "hqr_internal.h"
@@ -165,6 +166,70 @@ int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, doubl
   p.n_tasks = (int)n;
   (void)rebuild_t;   // T-build tasks always run: they cost O(NB^2 w) per panel tile
   return run_dag(p, ws, g, stream);
+}
+
+size_t factor_task_ids(const Geometry& g) {
+  return (size_t)g.steps * g.MT + (size_t)g.steps * g.NT * g.MT * g.NC;
+}
+
+int launch_factor_external(const Geometry& g, const ExternalScratch& x, double* dA, double* dTAU,
+                           long long timeout_ns, cudaStream_t stream) {
+  static_assert(kExternalCtlBytes == kCtlWords * sizeof(unsigned), "control words");
+  static_assert(kExternalStatsBytes == 2 * kNumTypes * sizeof(unsigned long long), "stats");
+  DagParams p{};
+  p.mode = kModeFactor;
+  p.MT = g.MT;
+  p.NT = g.NT;
+  p.CT = g.NT;
+  p.NC = g.NC;
+  p.steps = g.steps;
+  p.J = g.NT;
+  p.sh = shape_of(g);
+  p.sp = SmemPlan::make(p.sh);
+  p.n_ids = (int)factor_task_ids(g);
+  long long n = 0;
+  for (int i = 0; i < g.steps; i++)
+    n += (g.MT - i) + (long long)g.NC * (g.NT - 1 - i) * (g.MT - i);
+  p.n_tasks = (int)n;
+  p.A = dA;
+  p.T = x.T;
+  p.TAU = dTAU;
+  p.C = dA;
+  p.cnt = x.cnt;
+  p.qhi = x.qhi;
+  p.qlo = x.qlo;
+  p.ctl = x.ctl;
+  p.stats = x.stats;
+  p.timeout_ns = timeout_ns;
+  static std::mutex mu;
+  static size_t attr_bytes = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (g.smem_bytes > attr_bytes) {
+      cudaError_t e = cudaFuncSetAttribute(dag_exec_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)g.smem_bytes);
+      if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(dag_exec_kernel)");
+      attr_bytes = g.smem_bytes;
+    }
+  }
+  const int blocks = (p.n_ids + 255) / 256;
+  dag_init_kernel<<<blocks, 256, 0, stream>>>(p);
+  dag_seed_kernel<<<blocks, 256, 0, stream>>>(p);
+  const int grid = std::min(dag_sm_count(), std::max(1, p.n_tasks));
+  dag_exec_kernel<<<grid, kThreads, g.smem_bytes, stream>>>(p);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return record_cuda_error(e, "dag_exec_kernel launch");
+  return HQR_OK;
+}
+
+int external_status(const ExternalScratch& x, cudaStream_t stream) {
+  unsigned ctl[kCtlWords];
+  cudaError_t e = cudaMemcpyAsync(ctl, x.ctl, sizeof(ctl), cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return record_cuda_error(e, "DAG execution (stream synchronize)");
+  if (ctl[kErr] != 0u) return (ctl[kErr] & kErrTimeout) ? HQR_ERR_TIMEOUT : HQR_ERR_DEVICE;
+  return HQR_OK;
 }
 
 int dag_status(DagWorkspace* ws, cudaStream_t stream) {

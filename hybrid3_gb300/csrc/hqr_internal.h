@@ -46,6 +46,24 @@ int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, d
 int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT,
                     const double* dTAU, double* dC, int CT, bool rebuild_t, long long timeout_ns,
                     cudaStream_t stream);
+// Scratch supplied by the caller instead of a DagWorkspace (no allocation).
+struct ExternalScratch {
+  double* T;
+  int* cnt;
+  int* qhi;
+  int* qlo;
+  unsigned* ctl;                 // control words, zeroed by the caller
+  unsigned long long* stats;     // 10 counters, zeroed by the caller
+};
+constexpr int kExternalCtlBytes = 8 * 4;
+constexpr int kExternalStatsBytes = 10 * 8;
+// Number of task ids of the factorization DAG (size of cnt / qhi / qlo).
+size_t factor_task_ids(const Geometry& g);
+// Enqueue the factorization DAG on caller-supplied scratch.
+int launch_factor_external(const Geometry& g, const ExternalScratch& x, double* dA, double* dTAU,
+                           long long timeout_ns, cudaStream_t stream);
+// Synchronise `stream` and read the error word of caller-supplied scratch.
+int external_status(const ExternalScratch& x, cudaStream_t stream);
 // Read and clear the scheduler's error word (synchronises `stream`).
 int dag_status(DagWorkspace* ws, cudaStream_t stream);
 int dag_stats(DagWorkspace* ws, unsigned long long out[10], cudaStream_t stream);

@@ -71,6 +71,17 @@ double *hqr_plan_t_factors(hqr_plan_t *plan);
  * hqr_geqrf_async only enqueues (check with hqr_plan_status). */
 int hqr_geqrf(hqr_plan_t *plan, double *dA, double *dTAU, void *stream);
 int hqr_geqrf_async(hqr_plan_t *plan, double *dA, double *dTAU, void *stream);
+/* No counterpart in the reference.  The factorization of hqr_geqrf for callers
+ * that may not allocate device memory (work captured into a CUDA graph, memory
+ * owned entirely by the caller's own pool, latency paths that cannot take the
+ * synchronisation an allocation may cause): it calls no cudaMalloc/cudaFree
+ * and uses a fixed 64 MiB scratch array that the library reserves on each GPU
+ * that loads it, for the T factors (M*N doubles) and the scheduler tables --
+ * shapes that do not fit (about n > 2800 square) return HQR_ERR_UNSUPPORTED.
+ * All calls share that array: calls that overlap on the GPU race, so
+ * serialise them.  The first call on a device looks the array up and must
+ * come before any stream capture.  Waits for completion; returns a status. */
+int hqr_geqrf_noalloc(long M, long N, int NB, int IB, double *dA, double *dTAU, void *stream);
 /* Synchronise `stream`, then read and clear the scheduler's error word. */
 int hqr_plan_status(hqr_plan_t *plan, void *stream);
 int hqr_plan_stats(hqr_plan_t *plan, hqr_stats_t *out, void *stream);
