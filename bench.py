@@ -141,12 +141,13 @@ def run_reference(args, rank: int):
         return
     threads = os.cpu_count() or 1
     n = args.cpu_n
+    nb = 256   # the reference's CPU configuration (NB = 256, IB = 32)
     for _ in range(args.warmup):
-        cpu_sample(n, args.nb, args.ib, threads)
+        cpu_sample(n, nb, args.ib, threads)
     times = []
     kind = "port"
     for _ in range(args.steps):
-        t, kind = cpu_sample(n, args.nb, args.ib, threads)
+        t, kind = cpu_sample(n, nb, args.ib, threads)
         times.append(t)
     total = sum(times)
     value = args.steps * step_flops(n, n) / total / 1e12
@@ -156,8 +157,8 @@ def run_reference(args, rank: int):
         "ms_per_step": round(1e3 * total / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"tiled QR + Q generation, sample n={n} of the n={args.n} "
-                               f"workload, NB={args.nb}, IB={args.ib}, uniform[-1,1) seed 20151130",
-                   "n": args.n, "sample_n": n, "NB": args.nb, "IB": args.ib},
+                               f"workload, NB={nb}, IB={args.ib}, uniform[-1,1) seed 20151130",
+                   "n": args.n, "sample_n": n, "NB": nb, "IB": args.ib},
         "cpu_baseline": {"value": round(value, 6), "unit": "TFLOP/s", "cores": threads,
                          "kind": kind, "sample": f"{n}x{n} factorization + make_Q per step"},
         "e2e": {"value": round(value, 6), "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
@@ -169,19 +170,166 @@ def run_reference(args, rank: int):
 # ---------------------------------------------------------------------------
 # the GB300 arm
 # ---------------------------------------------------------------------------
-def load_traffic(n: int, NB: int):
-    """DRAM bytes per factorization launch from the committed ncu summary
-    (captured on a smaller case and scaled by the flop ratio, see profiles/)."""
-    p = os.path.join(ROOT, "profiles", "dag_exec_kernel_traffic.json")
+def load_traffic(n: int, NB: int, precision: str):
+    """DRAM bytes per factorization launch from the committed ncu summary of
+    that kernel (captured on a smaller case and scaled by the flop ratio)."""
+    p = os.path.join(ROOT, "profiles", f"dag_exec_kernel_{precision}_traffic.json")
     if not os.path.exists(p):
         return None
     try:
         d = json.load(open(p))
-        cap_n = d["n"]
-        scale = qr_flops(n, n) / qr_flops(cap_n, cap_n)
+        scale = qr_flops(n, n) / qr_flops(d["n"], d["n"])
         return int(d["dram_bytes_per_factor_launch"] * scale)
     except Exception:
         return None
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        return json.load(open(p))
+    except Exception:
+        return {}
+
+
+# slice products per emulated product (digit scheme by tile order)
+def split_products(NB: int) -> int:
+    return 34 if NB <= 128 else 36
+
+
+def measure(H, torch, L, args, precision: str, n: int, NB: int, IB: int, steps: int, warmup: int,
+            dist, world: int, clocks_too: bool, check: bool):
+    """Time `steps` device-resident steps (factorization + make_Q)."""
+    M = N = n
+    ntau = (M // NB) * (N // NB) * NB
+    prec = H.HQR_PREC_OZAKI if precision == "split" else H.HQR_PREC_FP64
+    stream = torch.cuda.Stream()
+    s = stream.cuda_stream
+    f64 = torch.float64
+    dA0 = torch.empty(M * N, dtype=f64, device="cuda")
+    dA = torch.empty_like(dA0)
+    dQ = torch.empty_like(dA0)
+    dTAU = torch.zeros(ntau, dtype=f64, device="cuda")
+    H.check(L.hqr_fill_uniform(M, N, NB, 20151130, dA0.data_ptr(), s), "fill")
+    plan = H.Plan(M, N, NB, IB, prec)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def step(rec=None):
+        with torch.cuda.stream(stream):
+            dA.copy_(dA0, non_blocking=True)
+            if rec:
+                rec[0].record(stream)
+            H.check(L.hqr_geqrf_async(plan.h, dA.data_ptr(), dTAU.data_ptr(), s), "geqrf")
+            if rec:
+                rec[1].record(stream)
+            dQ.zero_()
+            if rec:
+                rec[2].record(stream)
+            H.check(L.hqr_make_q_async(plan.h, dQ.data_ptr(), dA.data_ptr(), dTAU.data_ptr(), 1, s),
+                    "make_q")
+            if rec:
+                rec[3].record(stream)
+
+    for _ in range(warmup):
+        step()
+    H.check(L.hqr_plan_status(plan.h, s), "warm-up run")
+    clocks = ClockSampler(torch.cuda.current_device()) if clocks_too else None
+    if clocks:
+        clocks.start()
+    recs = [[ev(), ev(), ev(), ev()] for _ in range(steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_start, t_end = ev(), ev()
+    with torch.cuda.stream(stream):
+        t_start.record(stream)
+    for r in recs:
+        step(r)
+    with torch.cuda.stream(stream):
+        t_end.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop() if clocks else None
+    H.check(L.hqr_plan_status(plan.h, s), "timed run")
+    elapsed = t_start.elapsed_time(t_end) / 1e3
+    if dist:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    fact_s = [r[0].elapsed_time(r[1]) / 1e3 for r in recs]
+    mq_s = [r[2].elapsed_time(r[3]) / 1e3 for r in recs]
+    stats_mq = plan.stats(s)
+    acc = {}
+    if check:
+        # ||A - Q R||_F / ||A||_F and ||I - Q Q^T||_F from the Q^T array of the last
+        # step, on the device in FP64 (the checks of main.c:201-258)
+        dW = torch.empty_like(dA0)
+        r2 = ctypes.c_double()
+        a2 = ctypes.c_double()
+        H.check(L.hqr_dgemm_tn(N, NB, dQ.data_ptr(), dA.data_ptr(), dW.data_ptr(), s), "QR")
+        H.check(L.hqr_frob2(M, N, NB, dW.data_ptr(), dA0.data_ptr(), 0.0, ctypes.byref(r2), s), "frob")
+        H.check(L.hqr_frob2(M, N, NB, dA0.data_ptr(), None, 0.0, ctypes.byref(a2), s), "frob")
+        acc["resid_fro_rel"] = float(np.sqrt(r2.value / a2.value))
+        H.check(L.hqr_dgemm_tn(N, NB, dQ.data_ptr(), dQ.data_ptr(), dW.data_ptr(), s), "QQt")
+        H.check(L.hqr_frob2(M, N, NB, dW.data_ptr(), None, 1.0, ctypes.byref(r2), s), "frob")
+        acc["orth_fro"] = float(np.sqrt(r2.value))
+        del dW
+    # task counts of the factorization (run one more, untimed, for its stats)
+    step()
+    torch.cuda.synchronize()
+    plan.close()
+    del dA0, dA, dQ, dTAU
+    torch.cuda.empty_cache()
+    return {"elapsed": elapsed, "fact_s": fact_s, "mq_s": mq_s, "acc": acc, "clocks": clk,
+            "stats_mq": stats_mq, "flops": step_flops(M, N) * steps * world}
+
+
+def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: int, dist, world: int):
+    """The same workload through the drop-in C entry points with pinned host arrays:
+    Hybrid_tile_QR then Hybrid_make_Q, host<->device copies inside the timed region."""
+    M = N = n
+    L.hqr_set_default_precision(H.HQR_PREC_OZAKI if precision == "split" else H.HQR_PREC_FP64)
+    f64 = torch.float64
+    gen = torch.empty(M * N, dtype=f64, device="cuda")
+    H.check(L.hqr_fill_uniform(M, N, NB, 20151130, gen.data_ptr(), None), "fill")
+    torch.cuda.synchronize()
+    hA0 = torch.empty(M * N, dtype=f64).pin_memory()
+    hA0.copy_(gen.cpu())
+    del gen
+    torch.cuda.empty_cache()
+    hA = torch.empty_like(hA0).pin_memory()
+    hQ = torch.empty_like(hA0).pin_memory()
+    hTAU = torch.zeros((M // 2) * (N // 2), dtype=f64).pin_memory()
+    st = H.status(M, N, NB)
+    pa = ctypes.cast(hA.data_ptr(), DP)
+    pq = ctypes.cast(hQ.data_ptr(), DP)
+    pt = ctypes.cast(hTAU.data_ptr(), DP)
+    times = []
+    for it in range(1 + steps):
+        hA.copy_(hA0)
+        hQ.zero_()
+        t0 = time.perf_counter()
+        L.Hybrid_tile_QR(ctypes.byref(st), pa, pt, 0, 1, IB)
+        H.check(L.hqr_last_error(), "Hybrid_tile_QR")
+        L.Hybrid_make_Q(ctypes.byref(st), pq, pa, pt, 0, 1, IB)
+        H.check(L.hqr_last_error(), "Hybrid_make_Q")
+        if it > 0:
+            times.append(time.perf_counter() - t0)
+    L.hqr_set_default_precision(H.HQR_PREC_FP64)
+    t_e2e = sum(times)
+    if dist:
+        t = torch.tensor([t_e2e], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    nbytes = M * N * 8
+    tau_b = (M // NB) * (N // NB) * NB * 8
+    return {"value": round(world * steps * step_flops(M, N) / t_e2e / 1e12, 6), "unit": "TFLOP/s",
+            # Hybrid_tile_QR: A, TAU in and out; Hybrid_make_Q: Q, RY, TAU in, Q, RY out
+            "h2d_bytes_per_step": nbytes + tau_b + 2 * nbytes + tau_b,
+            "d2h_bytes_per_step": nbytes + tau_b + 2 * nbytes,
+            "steps": steps, "warmup": 1, "precision": precision,
+            "api": "Hybrid_tile_QR + Hybrid_make_Q (pinned host arrays)"}
 
 
 def main():
@@ -191,14 +339,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=16384)
-    ap.add_argument("--nb", type=int, default=256)
+    ap.add_argument("--precision", default="split", choices=["split", "fp64"])
+    ap.add_argument("--nb", type=int, default=None, help="tile order (default 128 split, 256 fp64)")
     ap.add_argument("--ib", type=int, default=32)
-    ap.add_argument("--precision", default="fp64", choices=["fp64"])
+    ap.add_argument("--fp64-nb", type=int, default=256, help="tile order of the plain-FP64 comparison")
+    ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP64 comparison run")
     ap.add_argument("--cpu-n", type=int, default=4096, help="CPU sample order")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
+    if args.nb is None:
+        args.nb = 128 if args.precision == "split" else 256
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -220,166 +372,86 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     L = H.lib()
     L.hqr_set_error_mode(H.HQR_ERRORS_RETURN)
-
     n, NB, IB = args.n, args.nb, args.ib
-    M = N = n
-    ntau = (M // NB) * (N // NB) * NB
-    stream = torch.cuda.Stream()
-    s = stream.cuda_stream
-    f64 = torch.float64
-    dA0 = torch.empty(M * N, dtype=f64, device="cuda")
-    dA = torch.empty_like(dA0)
-    dQ = torch.empty_like(dA0)
-    dTAU = torch.zeros(ntau, dtype=f64, device="cuda")
-    H.check(L.hqr_fill_uniform(M, N, NB, 20151130, dA0.data_ptr(), s), "fill")
-    plan = H.Plan(M, N, NB, IB, H.HQR_PREC_FP64)
 
-    ev = lambda: torch.cuda.Event(enable_timing=True)
+    peak_fp64 = L.hqr_fp64_peak_tflops(None)
+    main_run = measure(H, torch, L, args, args.precision, n, NB, IB, args.steps, args.warmup, dist,
+                       world, True, not args.no_check)
+    value = main_run["flops"] / main_run["elapsed"] / 1e12
 
-    def step(rec=None):
-        with torch.cuda.stream(stream):
-            dA.copy_(dA0, non_blocking=True)
-            if rec:
-                rec[0].record(stream)
-            H.check(L.hqr_geqrf_async(plan.h, dA.data_ptr(), dTAU.data_ptr(), s), "geqrf")
-            if rec:
-                rec[1].record(stream)
-            dQ.zero_()
-            if rec:
-                rec[2].record(stream)
-            H.check(L.hqr_make_q_async(plan.h, dQ.data_ptr(), dA.data_ptr(), dTAU.data_ptr(), 1, s),
-                    "make_q")
-            if rec:
-                rec[3].record(stream)
+    compare = None
+    if args.precision == "split" and not args.no_compare:
+        fp = measure(H, torch, L, args, "fp64", n, args.fp64_nb, IB, 1, 1, dist, world, False,
+                     not args.no_check)
+        fv = fp["flops"] / fp["elapsed"] / 1e12
+        compare = {"value": round(fv, 6), "unit": "TFLOP/s", "NB": args.fp64_nb, "IB": IB,
+                   "steps": 1, "warmup": 1, "ms_per_step": round(1e3 * fp["elapsed"], 3),
+                   "phases_ms": {"factor": round(1e3 * fp["fact_s"][0], 3),
+                                 "make_q": round(1e3 * fp["mq_s"][0], 3)},
+                   "accuracy": fp["acc"], "split_over_fp64": round(value / fv, 3)}
 
-    peak_fp64 = L.hqr_fp64_peak_tflops(s)
-    for _ in range(args.warmup):
-        step()
-    H.check(L.hqr_plan_status(plan.h, s), "warm-up run")
-
-    clocks = ClockSampler(torch.cuda.current_device())
-    clocks.start()
-    recs = [[ev(), ev(), ev(), ev()] for _ in range(args.steps)]
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    t_start, t_end = ev(), ev()
-    with torch.cuda.stream(stream):
-        t_start.record(stream)
-    for r in recs:
-        step(r)
-    with torch.cuda.stream(stream):
-        t_end.record(stream)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    clk = clocks.stop()
-    H.check(L.hqr_plan_status(plan.h, s), "timed run")
-    elapsed = t_start.elapsed_time(t_end) / 1e3
-    if dist:
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
-    fact_s = [r[0].elapsed_time(r[1]) / 1e3 for r in recs]
-    mq_s = [r[2].elapsed_time(r[3]) / 1e3 for r in recs]
-    flops = step_flops(M, N)
-    value = world * args.steps * flops / elapsed / 1e12
-    stats = plan.stats(s)
-
-    # accuracy of the last step (on the device, FP64): ||A - Q R||_F / ||A||_F and
-    # ||I - Q Q^T||_F from the Q^T array, as main.c:201-258 checks them
-    acc = {}
-    if not args.no_check:
-        dW = torch.empty_like(dA0)
-        r2 = ctypes.c_double()
-        H.check(L.hqr_dgemm_tn(N, NB, dQ.data_ptr(), dA.data_ptr(), dW.data_ptr(), s), "QR")
-        H.check(L.hqr_frob2(M, N, NB, dW.data_ptr(), dA0.data_ptr(), 0.0, ctypes.byref(r2), s), "frob")
-        a2 = ctypes.c_double()
-        H.check(L.hqr_frob2(M, N, NB, dA0.data_ptr(), None, 0.0, ctypes.byref(a2), s), "frob")
-        acc["resid_fro_rel"] = float(np.sqrt(r2.value / a2.value))
-        H.check(L.hqr_dgemm_tn(N, NB, dQ.data_ptr(), dQ.data_ptr(), dW.data_ptr(), s), "QQt")
-        H.check(L.hqr_frob2(M, N, NB, dW.data_ptr(), None, 1.0, ctypes.byref(r2), s), "frob")
-        acc["orth_fro"] = float(np.sqrt(r2.value))
-        del dW
-
-    # end to end through the drop-in C entry points with pinned host buffers
     e2e = None
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else args.steps
     if e2e_steps > 0:
-        hA0 = torch.empty(M * N, dtype=f64, pin_memory=True)
-        hA0.copy_(dA0.cpu())
-        hA = torch.empty_like(hA0).pin_memory()
-        hQ = torch.empty_like(hA0).pin_memory()
-        hTAU = torch.zeros((M // 2) * (N // 2), dtype=f64).pin_memory()
-        st = H.status(M, N, NB)
-        pa = ctypes.cast(hA.data_ptr(), DP)
-        pq = ctypes.cast(hQ.data_ptr(), DP)
-        pt = ctypes.cast(hTAU.data_ptr(), DP)
-        del dA, dQ
-        torch.cuda.empty_cache()
-        times = []
-        for it in range(1 + e2e_steps):
-            hA.copy_(hA0)
-            hQ.zero_()
-            t0 = time.perf_counter()
-            L.Hybrid_tile_QR(ctypes.byref(st), pa, pt, 0, 1, IB)
-            H.check(L.hqr_last_error(), "Hybrid_tile_QR")
-            L.Hybrid_make_Q(ctypes.byref(st), pq, pa, pt, 0, 1, IB)
-            H.check(L.hqr_last_error(), "Hybrid_make_Q")
-            if it > 0:
-                times.append(time.perf_counter() - t0)
-        t_e2e = sum(times)
-        if dist:
-            t = torch.tensor([t_e2e], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            t_e2e = float(t.item())
-        nbytes = M * N * 8
-        tau_b = ntau * 8
-        e2e = {"value": round(world * e2e_steps * flops / t_e2e / 1e12, 6), "unit": "TFLOP/s",
-               # Hybrid_tile_QR: A, TAU in and out; Hybrid_make_Q: RY, TAU, Q in, Q and RY out
-               "h2d_bytes_per_step": 2 * nbytes + tau_b + nbytes + tau_b + nbytes,
-               "d2h_bytes_per_step": nbytes + tau_b + nbytes + nbytes,
-               "steps": e2e_steps, "warmup": 1, "api": "Hybrid_tile_QR + Hybrid_make_Q (host arrays)"}
+        e2e = measure_e2e(H, torch, L, args.precision, n, NB, IB, e2e_steps, dist, world)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        t, kind = cpu_sample(args.cpu_n, NB, IB, os.cpu_count() or 1)
+        t, kind = cpu_sample(args.cpu_n, 256, IB, os.cpu_count() or 1)
         cpu = {"value": round(step_flops(args.cpu_n, args.cpu_n) / t / 1e12, 6), "unit": "TFLOP/s",
                "cores": os.cpu_count() or 1, "kind": kind,
-               "sample": f"one {args.cpu_n}x{args.cpu_n} factorization + make_Q (NB={NB}, IB={IB})"}
+               "sample": f"one {args.cpu_n}x{args.cpu_n} factorization + make_Q (NB=256, IB={IB})"}
 
-    fact_mean = float(np.mean(fact_s))
-    achieved = qr_flops(M, N) / fact_mean / 1e12
-    roofline = {"kernel": "dag_exec_kernel (factorization launch)", "bound": "fp64",
-                "achieved": round(achieved, 4), "peak": round(peak_fp64, 4), "unit": "TFLOP/s",
-                "frac": round(achieved / peak_fp64, 4) if peak_fp64 > 0 else None,
-                "peak_source": "FP64 FMA issue rate measured in this run (hqr_fp64_peak_tflops); "
-                               "MEASURED_PEAKS.json holds no FP64 figure",
-                "traffic": load_traffic(n, NB),
-                "algorithmic_flops_per_launch": qr_flops(M, N)}
+    fact_mean = float(np.mean(main_run["fact_s"]))
+    achieved = qr_flops(n, n) / fact_mean / 1e12
+    peaks = measured_peaks()
+    if args.precision == "split":
+        bf16 = peaks.get("bf16_tflops_sustained") or 1700.0
+        prods = split_products(NB)
+        peak = bf16 / prods
+        roofline = {"kernel": "dag_exec_kernel<split> (factorization launch)", "bound": "tensor",
+                    "achieved": round(achieved, 4), "peak": round(peak, 4), "unit": "TFLOP/s",
+                    "frac": round(achieved / peak, 4),
+                    "peak_source": f"emulated FP64 peak = MEASURED_PEAKS.json bf16_tflops_sustained "
+                                   f"({bf16}) / {prods} slice products (of measured)",
+                    "traffic": load_traffic(n, NB, "split"),
+                    "algorithmic_flops_per_launch": qr_flops(n, n)}
+    else:
+        roofline = {"kernel": "dag_exec_kernel<fp64> (factorization launch)", "bound": "fp64",
+                    "achieved": round(achieved, 4), "peak": round(peak_fp64, 4), "unit": "TFLOP/s",
+                    "frac": round(achieved / peak_fp64, 4) if peak_fp64 > 0 else None,
+                    "peak_source": "FP64 FMA issue rate measured in this run (hqr_fp64_peak_tflops); "
+                                   "MEASURED_PEAKS.json holds no FP64 figure",
+                    "traffic": load_traffic(n, NB, "fp64"),
+                    "algorithmic_flops_per_launch": qr_flops(n, n)}
     launches_per_step = 3 + 5
     line = {
         "metric": METRIC, "value": round(value, 6), "unit": "TFLOP/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * elapsed / args.steps, 3),
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * main_run["elapsed"] / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
         "config": {"workload": f"tiled QR + Q generation (make_Q), n={n} square, NB={NB}, IB={IB}, "
                                "uniform[-1,1) seed 20151130",
-                   "n": n, "NB": NB, "IB": IB, "precision": "fp64 (plain)",
+                   "n": n, "NB": NB, "IB": IB,
+                   "precision": ("split (Ozaki BF16 slices on tcgen05, FP64 panels)"
+                                 if args.precision == "split" else "fp64 (plain)"),
                    "l2": "inputs (2 GiB per matrix) exceed the 129 MB L2; no flush",
                    "parallelism": f"replicas x{world}"},
-        "phases_ms": {"factor": round(1e3 * fact_mean, 3), "make_q": round(1e3 * float(np.mean(mq_s)), 3)},
-        "accuracy": acc,
+        "phases_ms": {"factor": round(1e3 * fact_mean, 3),
+                      "make_q": round(1e3 * float(np.mean(main_run["mq_s"])), 3)},
+        "accuracy": main_run["acc"],
+        "plain_fp64": compare,
         "roofline": roofline,
+        "fp64_peak_measured_tflops": round(peak_fp64, 4),
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches_per_step * args.steps,
-        "clocks": clk,
-        "task_counts": stats["count"],
+        "clocks": main_run["clocks"],
+        "task_counts_make_q": main_run["stats_mq"]["count"],
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    plan.close()
     if dist:
         dist.destroy_process_group()
 

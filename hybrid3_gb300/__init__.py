@@ -41,7 +41,7 @@ class MatStat(ctypes.Structure):
 
 
 class HqrStats(ctypes.Structure):
-    _fields_ = [("count", ctypes.c_ulonglong * 5), ("cycles", ctypes.c_ulonglong * 5)]
+    _fields_ = [("count", ctypes.c_ulonglong * 6), ("cycles", ctypes.c_ulonglong * 6)]
 
 
 class TilSch(ctypes.Structure):
@@ -86,6 +86,8 @@ SIGNATURES = {
     # include/hqr_gpu.h
     "hqr_status_string": (ctypes.c_char_p, [_I]),
     "hqr_set_error_mode": (None, [_I]),
+    "hqr_set_default_precision": (None, [_I]),
+    "hqr_get_default_precision": (_I, []),
     "hqr_last_error": (_I, []),
     "hqr_last_cuda_error": (ctypes.c_char_p, []),
     "hqr_set_timeout_ms": (None, [ctypes.c_longlong]),
@@ -108,6 +110,7 @@ SIGNATURES = {
     "hqr_colmajor_to_tiles": (_I, [_L, _L, _I, _vp, _vp, _vp]),
     "hqr_zero_reflectors": (_I, [_L, _L, _I, _vp, _vp]),
     "hqr_fp64_peak_tflops": (_D, [_vp]),
+    "hqr_ozaki_product": (_I, [_I, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None

@@ -18,11 +18,13 @@ struct hqr_plan {
   int precision;
   double* dT;
   hqr::DagWorkspace ws;
+  hqr::OzWorkspace oz;   // allocated for HQR_PREC_OZAKI only
 };
 
 namespace {
 
 int g_error_mode = HQR_ERRORS_ABORT;
+int g_default_precision = -1;   // -1: not chosen yet (HQR_PRECISION, else FP64)
 thread_local int g_last_error = HQR_OK;
 long long g_timeout_ns = 20000LL * 1000000LL;
 std::mutex g_mu;   // serialises the drop-in entry points (they share buffers)
@@ -66,13 +68,14 @@ int stage_stream(cudaStream_t* s) {
 // Plan for the drop-in calls, rebuilt when the shape changes.
 int stage_plan(long M, long N, int NB, int IB, hqr_plan** out) {
   hqr_plan* p = g_stage.plan;
-  if (p && p->g.M == M && p->g.N == N && p->g.NB == NB && p->g.IB == IB) {
+  if (p && p->g.M == M && p->g.N == N && p->g.NB == NB && p->g.IB == IB &&
+      p->precision == hqr_get_default_precision()) {
     *out = p;
     return HQR_OK;
   }
   if (p) hqr_plan_destroy(p);
   g_stage.plan = nullptr;
-  int rc = hqr_plan_create(&g_stage.plan, M, N, NB, IB, HQR_PREC_FP64);
+  int rc = hqr_plan_create(&g_stage.plan, M, N, NB, IB, hqr_get_default_precision());
   *out = g_stage.plan;
   return rc;
 }
@@ -139,6 +142,18 @@ const char* hqr_status_string(int s) {
 }
 
 void hqr_set_error_mode(int mode) { g_error_mode = mode; }
+
+int hqr_get_default_precision(void) {
+  if (g_default_precision < 0) {
+    const char* e = getenv("HQR_PRECISION");
+    g_default_precision =
+        (e && (!strcmp(e, "ozaki") || !strcmp(e, "split"))) ? HQR_PREC_OZAKI : HQR_PREC_FP64;
+  }
+  return g_default_precision;
+}
+void hqr_set_default_precision(int precision) {
+  g_default_precision = (precision == HQR_PREC_OZAKI) ? HQR_PREC_OZAKI : HQR_PREC_FP64;
+}
 int hqr_last_error(void) { return g_last_error; }
 const char* hqr_last_cuda_error(void) { return g_cuda_msg; }
 void hqr_set_timeout_ms(long long ms) { g_timeout_ns = (ms > 0 ? ms : 1) * 1000000LL; }
@@ -149,6 +164,7 @@ int hqr_plan_create(hqr_plan_t** plan, long M, long N, int NB, int IB, int preci
   if (precision != HQR_PREC_FP64 && precision != HQR_PREC_OZAKI) return HQR_ERR_INVALID;
   hqr::Geometry g;
   TRY(hqr::make_geometry(M, N, NB, IB, &g));
+  if (precision == HQR_PREC_OZAKI && !hqr::oz_supported(g)) return HQR_ERR_UNSUPPORTED;
   hqr_plan* p = new hqr_plan();
   p->g = g;
   p->precision = precision;
@@ -158,6 +174,14 @@ int hqr_plan_create(hqr_plan_t** plan, long M, long N, int NB, int IB, int preci
     return HQR_ERR_NOMEM;
   }
   cudaMemset(p->dT, 0, (size_t)M * N * sizeof(double));
+  if (precision == HQR_PREC_OZAKI) {
+    if (cudaMalloc(&p->oz.slices, hqr::oz_slice_bytes(g)) != cudaSuccess ||
+        cudaMalloc(&p->oz.sexp, hqr::oz_exp_bytes(g)) != cudaSuccess ||
+        cudaMalloc(&p->oz.wscr, hqr::oz_scratch_bytes(g)) != cudaSuccess) {
+      hqr_plan_destroy(p);
+      return HQR_ERR_NOMEM;
+    }
+  }
   *plan = p;
   return HQR_OK;
 }
@@ -165,6 +189,9 @@ int hqr_plan_create(hqr_plan_t** plan, long M, long N, int NB, int IB, int preci
 int hqr_plan_destroy(hqr_plan_t* plan) {
   if (!plan) return HQR_ERR_INVALID;
   if (plan->dT) cudaFree(plan->dT);
+  if (plan->oz.slices) cudaFree(plan->oz.slices);
+  if (plan->oz.sexp) cudaFree(plan->oz.sexp);
+  if (plan->oz.wscr) cudaFree(plan->oz.wscr);
   hqr::dag_workspace_free(&plan->ws);
   delete plan;
   return HQR_OK;
@@ -175,7 +202,7 @@ double* hqr_plan_t_factors(hqr_plan_t* plan) { return plan ? plan->dT : nullptr;
 int hqr_geqrf_async(hqr_plan_t* plan, double* dA, double* dTAU, void* stream) {
   if (!plan || !dA || !dTAU) return HQR_ERR_INVALID;
   return hqr::launch_factor(plan->g, &plan->ws, dA, plan->dT, dTAU, g_timeout_ns,
-                            (cudaStream_t)stream);
+                            (cudaStream_t)stream, &plan->oz);
 }
 
 int hqr_plan_status(hqr_plan_t* plan, void* stream) {
@@ -191,9 +218,9 @@ int hqr_geqrf(hqr_plan_t* plan, double* dA, double* dTAU, void* stream) {
 
 int hqr_plan_stats(hqr_plan_t* plan, hqr_stats_t* out, void* stream) {
   if (!plan || !out || !plan->ws.stats) return HQR_ERR_INVALID;
-  unsigned long long v[10];
+  unsigned long long v[12];
   TRY(hqr::dag_stats(&plan->ws, v, (cudaStream_t)stream));
-  for (int t = 0; t < 5; t++) {
+  for (int t = 0; t < 6; t++) {
     out->count[t] = v[2 * t];
     out->cycles[t] = v[2 * t + 1];
   }
@@ -207,7 +234,8 @@ int hqr_make_q_async(hqr_plan_t* plan, double* dQ, double* dRY, const double* dT
   cudaStream_t s = (cudaStream_t)stream;
   // Hybrid_make_Q.c:91-95 sets the diagonal of the caller-zeroed Q
   hqr::make_identity(dQ, g.M, g.N, g.NB, false, s);
-  TRY(hqr::launch_apply_qt(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g.NT, !use_plan_t, g_timeout_ns, s));
+  TRY(hqr::launch_apply_qt(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g.NT, !use_plan_t, g_timeout_ns, s,
+                           &plan->oz));
   hqr::zero_reflectors(dRY, g.M, g.N, g.NB, s);
   return cuda_rc(cudaGetLastError());
 }
@@ -222,7 +250,7 @@ int hqr_ormqr_t(hqr_plan_t* plan, const double* dRY, const double* dTAU, double*
                 int use_plan_t, void* stream) {
   if (!plan || !dRY || !dTAU || !dC || CT <= 0) return HQR_ERR_INVALID;
   TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, !use_plan_t,
-                           g_timeout_ns, (cudaStream_t)stream));
+                           g_timeout_ns, (cudaStream_t)stream, &plan->oz));
   return hqr_plan_status(plan, stream);
 }
 
@@ -339,7 +367,7 @@ static int do_apply(mat_stat_t* st, double* Q, double* RY, double* TAU, int rank
     if (mode == 0) hqr::make_identity(dQ, M, N, NB, false, s);
   }
   TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dQ, plan->g.NT, true,
-                           g_timeout_ns, s));
+                           g_timeout_ns, s, &plan->oz));
   TRY(hqr_plan_status(plan, s));
   if (mode == 0) {
     hqr::zero_reflectors(dRY, M, N, NB, s);

@@ -87,10 +87,33 @@ int dag_sm_count() {
   return n;
 }
 
+static size_t dag_smem_bytes(const Geometry& g, bool oz) {
+  size_t b = g.smem_bytes;
+  if (oz) b = std::max(b, (size_t)oz::kSmemBytes);
+  return b;
+}
+
+template <bool OZ>
+static int launch_exec(const DagParams& p, const Geometry& g, cudaStream_t stream) {
+  static size_t attr_bytes = 0;   // dynamic shared memory opted in so far
+  const size_t smem = dag_smem_bytes(g, OZ);
+  if (smem > attr_bytes) {
+    cudaError_t e = cudaFuncSetAttribute(dag_exec_kernel<OZ>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(dag_exec_kernel)");
+    attr_bytes = smem;
+  }
+  const int grid = std::min(dag_sm_count(), std::max(1, p.n_tasks));
+  dag_exec_kernel<OZ><<<grid, kThreads, smem, stream>>>(p);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return record_cuda_error(e, "dag_exec_kernel launch");
+  return HQR_OK;
+}
+
 static int run_dag(DagParams& p, DagWorkspace* ws, const Geometry& g, cudaStream_t stream) {
   p.sh = shape_of(g);
   p.sp = SmemPlan::make(p.sh);
-  p.n_ids = p.steps * p.MT + p.steps * p.J * p.MT * p.NC;
+  p.n_ids = update_base(p) + p.steps * p.J * p.MT * p.NC;
   int rc = dag_workspace_reserve(ws, (size_t)p.n_ids);
   if (rc != HQR_OK) return rc;
   p.cnt = ws->cnt;
@@ -107,28 +130,29 @@ static int run_dag(DagParams& p, DagWorkspace* ws, const Geometry& g, cudaStream
   const int blocks = (p.n_ids + 255) / 256;
   dag_init_kernel<<<blocks, 256, 0, stream>>>(p);
   dag_seed_kernel<<<blocks, 256, 0, stream>>>(p);
-  static size_t attr_bytes = 0;   // dynamic shared memory opted in so far
-  if (g.smem_bytes > attr_bytes) {
-    cudaError_t e = cudaFuncSetAttribute(dag_exec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)g.smem_bytes);
-    if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(dag_exec_kernel)");
-    attr_bytes = g.smem_bytes;
+  return p.oz ? launch_exec<true>(p, g, stream) : launch_exec<false>(p, g, stream);
+}
+
+static void set_oz(DagParams& p, const Geometry& g, const OzWorkspace* oz) {
+  if (oz && oz->slices) {
+    p.oz = 1;
+    p.NC = g.NB / oz::kN;
+    p.slices = oz->slices;
+    p.sexp = oz->sexp;
+    p.wscr = oz->wscr;
+  } else {
+    p.oz = 0;
+    p.NC = g.NC;
   }
-  const int grid = std::min(dag_sm_count(), std::max(1, p.n_tasks));
-  dag_exec_kernel<<<grid, kThreads, g.smem_bytes, stream>>>(p);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return record_cuda_error(e, "dag_exec_kernel launch");
-  return HQR_OK;
 }
 
 int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, double* dTAU,
-                  long long timeout_ns, cudaStream_t stream) {
+                  long long timeout_ns, cudaStream_t stream, const OzWorkspace* ozw) {
   DagParams p{};
   p.mode = kModeFactor;
   p.MT = g.MT;
   p.NT = g.NT;
   p.CT = g.NT;
-  p.NC = g.NC;
   p.steps = g.steps;
   p.J = g.NT;
   p.A = dA;
@@ -136,24 +160,26 @@ int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, d
   p.TAU = dTAU;
   p.C = dA;
   p.timeout_ns = timeout_ns;
-  // tasks: per step i, 1 GEQRT + (MT-1-i) TSQRT + NC*(NT-1-i)*(MT-i) updates
+  set_oz(p, g, ozw);
+  p.prep = p.oz;
+  // tasks: per step i, 1 GEQRT + (MT-1-i) TSQRT [+ as many OZPREP] +
+  // NC*(NT-1-i)*(MT-i) updates
   long long n = 0;
   for (int i = 0; i < g.steps; i++)
-    n += (g.MT - i) + (long long)g.NC * (g.NT - 1 - i) * (g.MT - i);
+    n += (long long)(g.MT - i) * (p.prep ? 2 : 1) + (long long)p.NC * (g.NT - 1 - i) * (g.MT - i);
   p.n_tasks = (int)n;
   return run_dag(p, ws, g, stream);
 }
 
 int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT,
                     const double* dTAU, double* dC, int CT, bool rebuild_t, long long timeout_ns,
-                    cudaStream_t stream) {
+                    cudaStream_t stream, const OzWorkspace* ozw) {
   if (CT <= 0) return HQR_ERR_INVALID;
   DagParams p{};
   p.mode = kModeApplyQt;
   p.MT = g.MT;
   p.NT = g.NT;
   p.CT = CT;
-  p.NC = g.NC;
   p.steps = g.steps;
   p.J = CT;
   p.A = const_cast<double*>(dA);
@@ -161,11 +187,24 @@ int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, doubl
   p.TAU = const_cast<double*>(dTAU);
   p.C = dC;
   p.timeout_ns = timeout_ns;
+  set_oz(p, g, ozw);
+  p.prep = 0;
   long long n = 0;
-  for (int i = 0; i < g.steps; i++) n += (g.MT - i) + (long long)g.NC * CT * (g.MT - i);
+  for (int i = 0; i < g.steps; i++) n += (g.MT - i) + (long long)p.NC * CT * (g.MT - i);
   p.n_tasks = (int)n;
-  (void)rebuild_t;   // T-build tasks always run: they cost O(NB^2 w) per panel tile
+  (void)rebuild_t;   // panel tasks always rebuild T: O(NB^2 w) (FP64) or O(NB^3) (split) per tile
   return run_dag(p, ws, g, stream);
+}
+
+bool oz_supported(const Geometry& g) { return g.NB % oz::kM == 0 && g.NB <= 256; }
+
+static size_t panel_tiles(const Geometry& g) {
+  return panel_slot(g.MT, g.steps, g.steps);   // slots of every (k, i), k >= i, i < steps
+}
+size_t oz_slice_bytes(const Geometry& g) { return panel_tiles(g) * oz::panel_slice_bytes(g.NB); }
+size_t oz_exp_bytes(const Geometry& g) { return panel_tiles(g) * 3 * (size_t)g.NB * sizeof(int); }
+size_t oz_scratch_bytes(const Geometry& g) {
+  return (size_t)dag_sm_count() * 2 * g.NB * oz::kN * sizeof(double);
 }
 
 size_t factor_task_ids(const Geometry& g) {
@@ -206,7 +245,7 @@ int launch_factor_external(const Geometry& g, const ExternalScratch& x, double* 
   {
     std::lock_guard<std::mutex> lk(mu);
     if (g.smem_bytes > attr_bytes) {
-      cudaError_t e = cudaFuncSetAttribute(dag_exec_kernel,
+      cudaError_t e = cudaFuncSetAttribute(dag_exec_kernel<false>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)g.smem_bytes);
       if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(dag_exec_kernel)");
@@ -217,7 +256,7 @@ int launch_factor_external(const Geometry& g, const ExternalScratch& x, double* 
   dag_init_kernel<<<blocks, 256, 0, stream>>>(p);
   dag_seed_kernel<<<blocks, 256, 0, stream>>>(p);
   const int grid = std::min(dag_sm_count(), std::max(1, p.n_tasks));
-  dag_exec_kernel<<<grid, kThreads, g.smem_bytes, stream>>>(p);
+  dag_exec_kernel<false><<<grid, kThreads, g.smem_bytes, stream>>>(p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return record_cuda_error(e, "dag_exec_kernel launch");
   return HQR_OK;
@@ -246,9 +285,9 @@ int dag_status(DagWorkspace* ws, cudaStream_t stream) {
   return HQR_OK;
 }
 
-int dag_stats(DagWorkspace* ws, unsigned long long out[10], cudaStream_t stream) {
+int dag_stats(DagWorkspace* ws, unsigned long long out[12], cudaStream_t stream) {
   if (cudaStreamSynchronize(stream) != cudaSuccess) return HQR_ERR_CUDA;
-  if (cudaMemcpy(out, ws->stats, 10 * sizeof(unsigned long long), cudaMemcpyDeviceToHost) !=
+  if (cudaMemcpy(out, ws->stats, 12 * sizeof(unsigned long long), cudaMemcpyDeviceToHost) !=
       cudaSuccess)
     return HQR_ERR_CUDA;
   return HQR_OK;

@@ -25,6 +25,7 @@
 // by NC.  Every wait is bounded in time: when a wait runs out the kernel sets
 // an error bit and every CTA returns, so a broken DAG never hangs the GPU.
 #pragma once
+#include "hqr_oztasks.cuh"
 #include "hqr_tile_fp64.cuh"
 
 namespace hqr {
@@ -34,7 +35,12 @@ enum DagMode : int {
   kModeApplyQt = 1,   // C <- Q^T C: T-build panels + LARFB/SSRFB updates of C
 };
 
-enum TaskType : int { kGEQRT = 0, kTSQRT = 1, kLARFB = 2, kSSRFB = 3, kTBUILD = 4, kNumTypes = 5 };
+// With split precision (DagParams::oz) the update tasks run OZAPPLY and every
+// panel tile gets an OZPREP task (in the factorization it follows the
+// GEQRT/TSQRT; in the Q^T application it replaces the T-build).
+enum TaskType : int {
+  kGEQRT = 0, kTSQRT = 1, kLARFB = 2, kSSRFB = 3, kTBUILD = 4, kOZPREP = 5, kNumTypes = 6
+};
 
 // Control words of the scheduler (one cache line each is not needed: the
 // counters are touched once per task).
@@ -57,18 +63,35 @@ struct DagParams {
   int n_tasks;      // number of real tasks
   long long timeout_ns;
   unsigned long long* stats;   // [type][0] = count, [type][1] = SM cycles
+  // split precision
+  int oz;           // 1: OZPREP/OZAPPLY tasks (NC = NB / 64)
+  int prep;         // 1: separate OZPREP ids after the panel ids (factorization)
+  uint8_t* slices;  // sliced left operands, one block per panel tile
+  int* sexp;        // their row exponents (3 * NB ints per panel tile)
+  double* wscr;     // per-CTA scratch: 2 x NB x 64 doubles per CTA
 };
 
 constexpr int kNever = 0x3fffffff;
 
 // --- task ids ----------------------------------------------------------------
-//   panel  (i, k)        : i*MT + k                         (k >= i)
-//   update (i, j, k, c)  : P0 + ((i*J + j)*MT + k)*NC + c   (k >= i)
+//   panel  (i, k)        : i*MT + k                              (k >= i)
+//   prep   (i, k)        : P0 + i*MT + k   (factorization with split precision)
+//   update (i, j, k, c)  : U0 + ((i*J + j)*MT + k)*NC + c        (k >= i)
 __host__ __device__ __forceinline__ int panel_id(const DagParams& p, int i, int k) {
   return i * p.MT + k;
 }
+__host__ __device__ __forceinline__ int prep_id(const DagParams& p, int i, int k) {
+  return p.steps * p.MT + i * p.MT + k;
+}
+__host__ __device__ __forceinline__ int update_base(const DagParams& p) {
+  return p.steps * p.MT * (p.prep ? 2 : 1);
+}
 __host__ __device__ __forceinline__ int update_id(const DagParams& p, int i, int j, int k, int c) {
-  return p.steps * p.MT + ((i * p.J + j) * p.MT + k) * p.NC + c;
+  return update_base(p) + ((i * p.J + j) * p.MT + k) * p.NC + c;
+}
+// Compact index of panel tile (k, i), k >= i, into the slice store.
+__host__ __device__ __forceinline__ size_t panel_slot(int MT, int i, int k) {
+  return (size_t)i * MT - (size_t)i * (i - 1) / 2 + (size_t)(k - i);
 }
 
 struct TaskDesc {
@@ -78,14 +101,24 @@ struct TaskDesc {
 __device__ __forceinline__ TaskDesc decode(const DagParams& p, int id) {
   TaskDesc t;
   const int P0 = p.steps * p.MT;
+  const int U0 = update_base(p);
   if (id < P0) {
     t.i = id / p.MT;
     t.k = id % p.MT;
     t.j = t.i;
     t.c = 0;
-    t.type = (p.mode == kModeFactor) ? (t.k == t.i ? kGEQRT : kTSQRT) : kTBUILD;
+    if (p.mode == kModeFactor)
+      t.type = (t.k == t.i) ? kGEQRT : kTSQRT;
+    else
+      t.type = p.oz ? kOZPREP : kTBUILD;
+  } else if (id < U0) {
+    t.i = (id - P0) / p.MT;
+    t.k = (id - P0) % p.MT;
+    t.j = t.i;
+    t.c = 0;
+    t.type = kOZPREP;
   } else {
-    int u = id - P0;
+    int u = id - U0;
     t.c = u % p.NC; u /= p.NC;
     t.k = u % p.MT; u /= p.MT;
     t.j = u % p.J;
@@ -101,7 +134,7 @@ __device__ __forceinline__ bool update_valid(const DagParams& p, int i, int j) {
 
 __device__ __forceinline__ bool is_high_priority(const DagParams& p, int id) {
   const TaskDesc t = decode(p, id);
-  if (t.type == kGEQRT || t.type == kTSQRT || t.type == kTBUILD) return true;
+  if (t.type == kGEQRT || t.type == kTSQRT || t.type == kTBUILD || t.type == kOZPREP) return true;
   return p.mode == kModeFactor && t.j == t.i + 1;   // look-ahead: next panel column
 }
 
@@ -179,6 +212,7 @@ __global__ void dag_init_kernel(DagParams p) {
   p.qlo[id] = -1;
   int deps = kNever;
   const int P0 = p.steps * p.MT;
+  const int U0 = update_base(p);
   if (id < P0) {
     const int i = id / p.MT, k = id % p.MT;
     if (k >= i) {
@@ -187,8 +221,11 @@ __global__ void dag_init_kernel(DagParams p) {
       else
         deps = 0;
     }
+  } else if (id < U0) {
+    const int i = (id - P0) / p.MT, k = (id - P0) % p.MT;
+    if (k >= i) deps = 1;   // its panel task
   } else {
-    int u = id - P0;
+    int u = id - U0;
     const int c = u % p.NC; u /= p.NC;
     const int k = u % p.MT; u /= p.MT;
     const int j = u % p.J;
@@ -208,12 +245,17 @@ __global__ void dag_seed_kernel(DagParams p) {
 
 // --- releases after a task ---------------------------------------------------------
 __device__ void release_dependents(const DagParams& p, const TaskDesc& t) {
-  if (t.type == kGEQRT || t.type == kTSQRT || t.type == kTBUILD) {
-    const int j0 = (p.mode == kModeFactor) ? t.i + 1 : 0;
-    const int j1 = (p.mode == kModeFactor) ? p.NT : p.CT;
-    for (int j = j0; j < j1; j++)
-      for (int c = 0; c < p.NC; c++) release(p, update_id(p, t.i, j, t.k, c));
-    if (p.mode == kModeFactor && t.k + 1 < p.MT) release(p, panel_id(p, t.i, t.k + 1));
+  if (t.type == kGEQRT || t.type == kTSQRT || t.type == kTBUILD || t.type == kOZPREP) {
+    const bool feeds_prep = (t.type == kGEQRT || t.type == kTSQRT) && p.prep;
+    if (feeds_prep) {
+      release(p, prep_id(p, t.i, t.k));
+    } else {
+      const int j0 = (p.mode == kModeFactor) ? t.i + 1 : 0;
+      const int j1 = (p.mode == kModeFactor) ? p.NT : p.CT;
+      for (int j = j0; j < j1; j++)
+        for (int c = 0; c < p.NC; c++) release(p, update_id(p, t.i, j, t.k, c));
+    }
+    if ((t.type == kGEQRT || t.type == kTSQRT) && t.k + 1 < p.MT) release(p, panel_id(p, t.i, t.k + 1));
     return;
   }
   // LARFB / SSRFB: LIN to the next task of this column chain
@@ -249,13 +291,22 @@ __device__ void task_tbuild(const double* V, const double* tau_g, double* T, boo
 }
 
 // --- the persistent executor ---------------------------------------------------------
+template <bool OZ>
 __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
-  extern __shared__ double smem[];
+  extern __shared__ __align__(1024) double smem[];
   __shared__ int s_id;
+  __shared__ uint32_t s_tmem;
   const int NB = p.sh.NB;
   const size_t tsz = (size_t)NB * NB;
-  unsigned long long local_cnt[kNumTypes] = {0, 0, 0, 0, 0};
-  unsigned long long local_cyc[kNumTypes] = {0, 0, 0, 0, 0};
+  unsigned long long local_cnt[kNumTypes] = {0, 0, 0, 0, 0, 0};
+  unsigned long long local_cyc[kNumTypes] = {0, 0, 0, 0, 0, 0};
+  if (OZ) {
+    // the whole TMEM of this SM (one CTA per SM): 8 t-group accumulators x 64 columns
+    if ((threadIdx.x >> 5) == 0) oz::tmem_alloc(&s_tmem, 512);
+    oz::tc_fence_before();
+    __syncthreads();
+    oz::tc_fence_after();
+  }
   for (;;) {
     if (threadIdx.x == 0) s_id = pop_task(p);
     __syncthreads();
@@ -280,15 +331,43 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
         task_tbuild(p.A + o, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.T + o, t.k == t.i, p.sh, smem, p.sp);
         break;
       }
+      case kOZPREP: {
+        if (OZ) {
+          const size_t o = tile_off(t.k, t.i, p.MT, NB);
+          const size_t slot = panel_slot(p.MT, t.i, t.k);
+          task_ozprep(p.A + o, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.T + o, t.k == t.i, NB,
+                      p.slices + slot * oz::panel_slice_bytes(NB), p.sexp + slot * 3 * NB, smem);
+        }
+        break;
+      }
       case kLARFB: {
         const size_t ov = tile_off(t.i, t.i, p.MT, NB), oc = tile_off(t.i, t.j, p.MT, NB);
-        task_larfb(p.A + ov, p.T + ov, p.C + oc, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp);
+        if (OZ) {
+          oz::Ctx c;
+          oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
+          const size_t slot = panel_slot(p.MT, t.i, t.i);
+          double* w = p.wscr + (size_t)blockIdx.x * 2 * NB * oz::kN;
+          task_ozapply(c, NB, p.slices + slot * oz::panel_slice_bytes(NB), p.sexp + slot * 3 * NB, true,
+                       nullptr, p.C + oc + (size_t)t.c * oz::kN * NB, w, w + (size_t)NB * oz::kN);
+        } else {
+          task_larfb(p.A + ov, p.T + ov, p.C + oc, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp);
+        }
         break;
       }
       case kSSRFB: {
         const size_t ov = tile_off(t.k, t.i, p.MT, NB);
         const size_t o1 = tile_off(t.i, t.j, p.MT, NB), o2 = tile_off(t.k, t.j, p.MT, NB);
-        task_ssrfb(p.C + o1, p.C + o2, p.A + ov, p.T + ov, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp);
+        if (OZ) {
+          oz::Ctx c;
+          oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
+          const size_t slot = panel_slot(p.MT, t.i, t.k);
+          double* w = p.wscr + (size_t)blockIdx.x * 2 * NB * oz::kN;
+          const size_t cofs = (size_t)t.c * oz::kN * NB;
+          task_ozapply(c, NB, p.slices + slot * oz::panel_slice_bytes(NB), p.sexp + slot * 3 * NB, false,
+                       p.C + o1 + cofs, p.C + o2 + cofs, w, w + (size_t)NB * oz::kN);
+        } else {
+          task_ssrfb(p.C + o1, p.C + o2, p.A + ov, p.T + ov, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp);
+        }
         break;
       }
       default:
@@ -312,6 +391,12 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
         atomicAdd(p.stats + 2 * ty + 1, local_cyc[ty]);
       }
     }
+  }
+  if (OZ) {
+    oz::tc_fence_before();
+    __syncthreads();
+    oz::tc_fence_after();
+    if ((threadIdx.x >> 5) == 0) oz::tmem_dealloc(s_tmem, 512);
   }
 }
 

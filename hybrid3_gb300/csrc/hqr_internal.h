@@ -38,14 +38,26 @@ struct DagWorkspace {
 int dag_workspace_reserve(DagWorkspace* ws, size_t n_ids);
 void dag_workspace_free(DagWorkspace* ws);
 
+// Workspace of the split-precision updates (null slices: FP64 updates).
+struct OzWorkspace {
+  uint8_t* slices = nullptr;   // sliced V^T, T^T, V of every panel tile
+  int* sexp = nullptr;         // their row exponents
+  double* wscr = nullptr;      // per-CTA W, W2 scratch
+};
+// Bytes of the split-precision workspace for a geometry (NB % 128 == 0, NB <= 256).
+size_t oz_slice_bytes(const Geometry& g);
+size_t oz_exp_bytes(const Geometry& g);
+size_t oz_scratch_bytes(const Geometry& g);
+bool oz_supported(const Geometry& g);
+
 // Enqueue a factorization DAG on `stream` (no synchronisation).
 int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, double* dTAU,
-                  long long timeout_ns, cudaStream_t stream);
-// Enqueue C <- Q^T C (C has CT tile columns, same MT/NB as A); rebuild_t: build
-// the diagonal T blocks from V/TAU first (T-build tasks), else use dT as is.
+                  long long timeout_ns, cudaStream_t stream, const OzWorkspace* oz = nullptr);
+// Enqueue C <- Q^T C (C has CT tile columns, same MT/NB as A); the panel
+// tasks rebuild T from V/TAU (FP64: diagonal blocks; split: full T + slices).
 int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT,
                     const double* dTAU, double* dC, int CT, bool rebuild_t, long long timeout_ns,
-                    cudaStream_t stream);
+                    cudaStream_t stream, const OzWorkspace* oz = nullptr);
 // Scratch supplied by the caller instead of a DagWorkspace (no allocation).
 struct ExternalScratch {
   double* T;
@@ -56,7 +68,7 @@ struct ExternalScratch {
   unsigned long long* stats;     // 10 counters, zeroed by the caller
 };
 constexpr int kExternalCtlBytes = 8 * 4;
-constexpr int kExternalStatsBytes = 10 * 8;
+constexpr int kExternalStatsBytes = 12 * 8;
 // Number of task ids of the factorization DAG (size of cnt / qhi / qlo).
 size_t factor_task_ids(const Geometry& g);
 // Enqueue the factorization DAG on caller-supplied scratch.
@@ -66,7 +78,7 @@ int launch_factor_external(const Geometry& g, const ExternalScratch& x, double* 
 int external_status(const ExternalScratch& x, cudaStream_t stream);
 // Read and clear the scheduler's error word (synchronises `stream`).
 int dag_status(DagWorkspace* ws, cudaStream_t stream);
-int dag_stats(DagWorkspace* ws, unsigned long long out[10], cudaStream_t stream);
+int dag_stats(DagWorkspace* ws, unsigned long long out[12], cudaStream_t stream);
 int dag_sm_count();
 
 // Utility kernels (hqr_util.cu)

@@ -41,14 +41,20 @@ extern "C" {
 typedef struct hqr_plan hqr_plan_t;
 
 /* Per-task-type execution counters of the last DAG run (device clock cycles
- * summed over CTAs).  Index: 0 GEQRT, 1 TSQRT, 2 LARFB, 3 SSRFB, 4 T-build. */
+ * summed over CTAs).  Index: 0 GEQRT, 1 TSQRT, 2 LARFB, 3 SSRFB, 4 T-build,
+ * 5 split-precision panel preparation (full T + operand slices). */
 typedef struct {
-    unsigned long long count[5];
-    unsigned long long cycles[5];
+    unsigned long long count[6];
+    unsigned long long cycles[6];
 } hqr_stats_t;
 
 const char *hqr_status_string(int status);
 void hqr_set_error_mode(int mode);
+/* Arithmetic of the trailing updates used by the drop-in entry points
+ * (default: HQR_PREC_FP64, or HQR_PREC_OZAKI when the environment variable
+ * HQR_PRECISION is "ozaki" or "split" at first use). */
+void hqr_set_default_precision(int precision);
+int hqr_get_default_precision(void);
 int hqr_last_error(void);
 /* Text of the last failed CUDA runtime call ("" if none). */
 const char *hqr_last_cuda_error(void);
@@ -112,6 +118,11 @@ int hqr_frob2(long M, long N, int NB, const double *dX, const double *dY, double
 /* Tile layout <-> column-major (ld = M). */
 int hqr_tiles_to_colmajor(long M, long N, int NB, const double *dT, double *dCM, void *stream);
 int hqr_colmajor_to_tiles(long M, long N, int NB, const double *dCM, double *dT, void *stream);
+/* The split-precision product engine on its own (diagnostics / tests):
+ * dC = dX dY for dX NB x NB and dY NB x 64, column-major device arrays,
+ * NB in {128, 256}; same slicing, tensor-core products and recombination as
+ * the HQR_PREC_OZAKI updates.  Synchronous. */
+int hqr_ozaki_product(int NB, const double *dX, const double *dY, double *dC, void *stream);
 /* Measured FP64 FMA issue rate of this GPU in TFLOP/s (a ~10 ms probe of
  * independent FMA chains): the roofline denominator of the FP64 kernels. */
 double hqr_fp64_peak_tflops(void *stream);
