@@ -176,8 +176,7 @@ int hqr_plan_create(hqr_plan_t** plan, long M, long N, int NB, int IB, int preci
   cudaMemset(p->dT, 0, (size_t)M * N * sizeof(double));
   if (precision == HQR_PREC_OZAKI) {
     if (cudaMalloc(&p->oz.slices, hqr::oz_slice_bytes(g)) != cudaSuccess ||
-        cudaMalloc(&p->oz.sexp, hqr::oz_exp_bytes(g)) != cudaSuccess ||
-        cudaMalloc(&p->oz.wscr, hqr::oz_scratch_bytes(g)) != cudaSuccess) {
+        cudaMalloc(&p->oz.sexp, hqr::oz_exp_bytes(g)) != cudaSuccess) {
       hqr_plan_destroy(p);
       return HQR_ERR_NOMEM;
     }
@@ -191,7 +190,6 @@ int hqr_plan_destroy(hqr_plan_t* plan) {
   if (plan->dT) cudaFree(plan->dT);
   if (plan->oz.slices) cudaFree(plan->oz.slices);
   if (plan->oz.sexp) cudaFree(plan->oz.sexp);
-  if (plan->oz.wscr) cudaFree(plan->oz.wscr);
   hqr::dag_workspace_free(&plan->ws);
   delete plan;
   return HQR_OK;

@@ -139,7 +139,6 @@ static void set_oz(DagParams& p, const Geometry& g, const OzWorkspace* oz) {
     p.NC = g.NB / oz::kN;
     p.slices = oz->slices;
     p.sexp = oz->sexp;
-    p.wscr = oz->wscr;
   } else {
     p.oz = 0;
     p.NC = g.NC;
@@ -196,16 +195,13 @@ int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, doubl
   return run_dag(p, ws, g, stream);
 }
 
-bool oz_supported(const Geometry& g) { return g.NB % oz::kM == 0 && g.NB <= 256; }
+bool oz_supported(const Geometry& g) { return g.NB == oz::kK; }
 
 static size_t panel_tiles(const Geometry& g) {
   return panel_slot(g.MT, g.steps, g.steps);   // slots of every (k, i), k >= i, i < steps
 }
-size_t oz_slice_bytes(const Geometry& g) { return panel_tiles(g) * oz::panel_slice_bytes(g.NB); }
+size_t oz_slice_bytes(const Geometry& g) { return panel_tiles(g) * oz::panel_slice_bytes(); }
 size_t oz_exp_bytes(const Geometry& g) { return panel_tiles(g) * 3 * (size_t)g.NB * sizeof(int); }
-size_t oz_scratch_bytes(const Geometry& g) {
-  return (size_t)dag_sm_count() * 2 * g.NB * oz::kN * sizeof(double);
-}
 
 size_t factor_task_ids(const Geometry& g) {
   return (size_t)g.steps * g.MT + (size_t)g.steps * g.NT * g.MT * g.NC;

@@ -68,7 +68,6 @@ struct DagParams {
   int prep;         // 1: separate OZPREP ids after the panel ids (factorization)
   uint8_t* slices;  // sliced left operands, one block per panel tile
   int* sexp;        // their row exponents (3 * NB ints per panel tile)
-  double* wscr;     // per-CTA scratch: 2 x NB x 64 doubles per CTA
 };
 
 constexpr int kNever = 0x3fffffff;
@@ -335,8 +334,9 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
         if (OZ) {
           const size_t o = tile_off(t.k, t.i, p.MT, NB);
           const size_t slot = panel_slot(p.MT, t.i, t.k);
-          task_ozprep(p.A + o, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.T + o, t.k == t.i, NB,
-                      p.slices + slot * oz::panel_slice_bytes(NB), p.sexp + slot * 3 * NB, smem);
+          task_ozprep(p.A + o, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.T + o, t.k == t.i,
+                      p.slices + slot * oz::panel_slice_bytes(), p.sexp + slot * 3 * NB,
+                      reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
         }
         break;
       }
@@ -346,9 +346,8 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
           oz::Ctx c;
           oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
           const size_t slot = panel_slot(p.MT, t.i, t.i);
-          double* w = p.wscr + (size_t)blockIdx.x * 2 * NB * oz::kN;
-          task_ozapply(c, NB, p.slices + slot * oz::panel_slice_bytes(NB), p.sexp + slot * 3 * NB, true,
-                       nullptr, p.C + oc + (size_t)t.c * oz::kN * NB, w, w + (size_t)NB * oz::kN);
+          task_ozapply(c, p.slices + slot * oz::panel_slice_bytes(), p.sexp + slot * 3 * NB, nullptr,
+                       p.C + oc + (size_t)t.c * oz::kN * NB);
         } else {
           task_larfb(p.A + ov, p.T + ov, p.C + oc, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp);
         }
@@ -361,10 +360,9 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
           oz::Ctx c;
           oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
           const size_t slot = panel_slot(p.MT, t.i, t.k);
-          double* w = p.wscr + (size_t)blockIdx.x * 2 * NB * oz::kN;
           const size_t cofs = (size_t)t.c * oz::kN * NB;
-          task_ozapply(c, NB, p.slices + slot * oz::panel_slice_bytes(NB), p.sexp + slot * 3 * NB, false,
-                       p.C + o1 + cofs, p.C + o2 + cofs, w, w + (size_t)NB * oz::kN);
+          task_ozapply(c, p.slices + slot * oz::panel_slice_bytes(), p.sexp + slot * 3 * NB,
+                       p.C + o1 + cofs, p.C + o2 + cofs);
         } else {
           task_ssrfb(p.C + o1, p.C + o2, p.A + ov, p.T + ov, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp);
         }

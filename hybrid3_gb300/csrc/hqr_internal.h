@@ -42,12 +42,10 @@ void dag_workspace_free(DagWorkspace* ws);
 struct OzWorkspace {
   uint8_t* slices = nullptr;   // sliced V^T, T^T, V of every panel tile
   int* sexp = nullptr;         // their row exponents
-  double* wscr = nullptr;      // per-CTA W, W2 scratch
 };
-// Bytes of the split-precision workspace for a geometry (NB % 128 == 0, NB <= 256).
+// Bytes of the split-precision workspace for a geometry (NB = 128).
 size_t oz_slice_bytes(const Geometry& g);
 size_t oz_exp_bytes(const Geometry& g);
-size_t oz_scratch_bytes(const Geometry& g);
 bool oz_supported(const Geometry& g);
 
 // Enqueue a factorization DAG on `stream` (no synchronisation).

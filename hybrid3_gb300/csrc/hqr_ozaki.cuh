@@ -1,35 +1,35 @@
-// hqr_ozaki.cuh -- split-precision trailing updates on the 5th-generation
-// tensor cores (tcgen05, TMEM accumulators, bulk-TMA operand staging).
+// hqr_ozaki.cuh -- split-precision products on the 5th-generation tensor
+// cores (tcgen05, TMEM accumulators, bulk-TMA operand staging).
 //
-// A block reflector is applied as three products (D = C_top + V^T C_bot,
-// D2 = T^T D, C -= [I|V] D2 -- the CORE_dtsmqr / CORE_dormqr arithmetic with
-// the full NB x NB T), each computed as an Ozaki-style sum of exact slice
-// products (Ozaki, Ogita, Oishi, Rump, "Error-free transformations of matrix
-// multiplication by using fast routines of matrix multiplication and its
-// applications", Numer. Algorithms 59, 2012):
+// Every product is X Y with a 128 x 128 left operand X (a panel tile's V^T,
+// T^T or V) and a 128 x 64 right operand Y (a column block of a trailing
+// tile), computed as an Ozaki-style sum of exact slice products (Ozaki,
+// Ogita, Oishi, Rump, "Error-free transformations of matrix multiplication by
+// using fast routines of matrix multiplication and its applications", Numer.
+// Algorithms 59, 2012):
 //
-//   * every row of the left operand X (and every column of the right
-//     operand Y) is scaled by the power of two of its largest element and
-//     written as a fixed-point integer F with |F| < 2^55;
-//   * F is split into kSlices signed digits of kRho = 7 bits, |d| <= 64,
-//     F = sum_p d_p 2^(56 - 7p); every digit is an exact BF16 value;
-//   * the slice products X_p Y_q with p + q <= kSlices + 1 are exact on the
-//     tensor cores: |d_x d_y| <= 2^12, a K = NB <= 256 sum stays below 2^20,
-//     and the <= 8 products sharing t = p + q (same weight 2^(-7t)) are
-//     accumulated in one FP32 TMEM accumulator, < 2^23 < 2^24;
+//   * every row of X (and every column of Y) is scaled by the power of two of
+//     its largest element and written as a fixed-point integer F, |F| <= 2^55;
+//   * F is split into kS = 7 signed digits of kRho = 8 bits, |d| <= 128,
+//     F = sum_p d_p 2^(8 (6 - p)); every digit is an exact BF16 value;
+//   * the slice products X_p Y_q with p + q <= 7 (0-based; 34 of the 49) are
+//     exact on the tensor cores: |d_x d_y| <= 2^14, a K = 128 sum stays below
+//     2^21, and the <= 7 products sharing t = p + q (weight 2^(-8t)) are
+//     accumulated in one FP32 TMEM accumulator, < 7 * 2^21 < 2^24;
 //   * the 8 t-group accumulators (8 x 64 TMEM columns = the whole TMEM) are
-//     recombined exactly in 64-bit integers (two Horner chains in base 2^7),
-//     converted to FP64 once and scaled back: 2 FP64 operations per output.
+//     recombined exactly in 64-bit integers (two Horner chains in base 2^8)
+//     and turned into FP64 by integer operations on the IEEE 754 encoding.
+//     The dropped products weigh < 2^-64 of rowmax(X) * colmax(Y) * K.
 //
-// The left operands (V^T, T^T, V of a panel tile) are sliced once per panel
-// tile into HBM, already in the tcgen05 K-major core-matrix layout, so an
-// update streams each 16-deep K chunk of all 8 slices with one 32 KiB bulk
-// TMA copy.  The right operand (a 64-column block of the trailing tile) is
-// sliced on the fly by the CTA into shared memory.  MMAs are issued by one
-// thread (M = 128, N = 64, K = 16, BF16 x BF16 -> FP32) into the 8
-// accumulators; the K loop is double-buffered (TMA + slicing of chunk k+1
-// overlap the MMAs of chunk k).  Every mbarrier wait is bounded; on time-out
-// the kernel's error word is set and the task is abandoned.
+// The left operands are sliced once per panel tile into HBM, already in the
+// tcgen05 K-major core-matrix layout, so each 16-deep K chunk of all 7 slices
+// arrives with one 28 KiB bulk TMA copy.  The right operand lives in shared
+// memory (staged from HBM for the first product of an update, written there
+// by the previous product's epilogue otherwise) and is sliced chunk by chunk
+// into a double-buffered stage while the MMAs of the previous chunk run.
+// MMAs are issued by one thread (M = 128, N = 64, K = 16, BF16 x BF16 ->
+// FP32).  Every mbarrier wait is bounded; on time-out the error word is set
+// and the task is abandoned.
 #pragma once
 #include <cstdint>
 #include "hqr_common.cuh"
@@ -37,41 +37,36 @@
 namespace hqr {
 namespace oz {
 
-constexpr int kSlices = 8;         // slice storage per operand (the most a scheme uses)
-constexpr int kN = 64;             // columns per update task (MMA N)
+constexpr int kK = 128;            // the tile order: K (and M) of every product
+constexpr int kN = 64;             // columns of the right operand (MMA N)
 constexpr int kM = 128;            // rows per MMA (one TMEM lane per row)
 constexpr int kKC = 16;            // K per BF16 MMA
-constexpr int kGroups = 8;         // t-group accumulators: t = p + q in [2, 9] (1-based)
+constexpr int kChunks = kK / kKC;  // 8 K chunks per product
+constexpr int kRho = 8;            // bits per digit
+constexpr int kS = 7;              // digits (slices) per element
+constexpr int kGroups = 8;         // t-group accumulators: t = p + q in [0, 7]
+constexpr int kShiftHi = 14;       // X = (hi << kShiftHi) + (lo >> kShiftLo)
+constexpr int kShiftLo = 18;
+constexpr int kExpBias = 1073;     // biased exponent of the scale of X = Ea + Eb - kExpBias
 constexpr int kDC = 8;             // accumulator columns recombined per epilogue pass
-
-// Digit schemes.  F (|F| < 2^55, the fixed-point form of an element relative
-// to its row / column maximum) is written exactly as S digits of RHO bits:
-// F = sum_{p=1..S} d_p 2^(RHO (S - p)), |d_p| <= 2^(RHO-1).  Slice products
-// with p + q <= 9 are kept (8 t-groups, the whole TMEM); relative to
-// rowmax * colmax the dropped ones weigh about 2^(-8 RHO):
-//   Scheme8x7 (K <= 128): 8-bit digits, 7 slices, 34 products, drop < 2^-64;
-//   Scheme7x8 (K <= 256): 7-bit digits, 8 slices, 36 products, drop < 2^-56.
-// Exactness: a t-group holds <= S pairs of K products of |d d| <= 2^(2 RHO - 2),
-// i.e. 7 * 128 * 2^14 < 2^24 and 8 * 256 * 2^12 = 2^23.
-template <int RHO_, int S_, int SHIFT_HI_, int SHIFT_LO_, int EXP_BIAS_>
-struct Scheme {
-  static constexpr int RHO = RHO_;
-  static constexpr int S = S_;
-  static constexpr int SHIFT_HI = SHIFT_HI_;   // X = (hi << SHIFT_HI) + (lo >> SHIFT_LO)
-  static constexpr int SHIFT_LO = SHIFT_LO_;
-  static constexpr int EXP_BIAS = EXP_BIAS_;   // biased exponent of the scale = Ea + Eb - EXP_BIAS
-};
-using Scheme8x7 = Scheme<8, 7, 14, 18, 1073>;
-using Scheme7x8 = Scheme<7, 8, 18, 10, 1072>;
-constexpr int kAChunkBytes = kSlices * kM * kKC * 2;    // 32 KiB: all slices of one K chunk
-constexpr int kBChunkBytes = kSlices * kN * kKC * 2;    // 16 KiB
+constexpr int kLdY = kK + 1;       // leading dimension of the staged right operand
 constexpr int kSliceABytes = kM * kKC * 2;              // 4 KiB
 constexpr int kSliceBBytes = kN * kKC * 2;              // 2 KiB
+constexpr int kAChunkBytes = kS * kSliceABytes;         // 28 KiB: all slices of one K chunk
+constexpr int kBChunkBytes = kS * kSliceBBytes;         // 14 KiB
 constexpr long long kWaitIters = 1LL << 26;             // bounded mbarrier waits
 
-// Bytes of one prepared left operand (NB x NB) and of the three of a panel tile.
-__host__ __device__ constexpr size_t operand_bytes(int NB) { return (size_t)NB * NB * kSlices * 2; }
-__host__ __device__ constexpr size_t panel_slice_bytes(int NB) { return 3 * operand_bytes(NB); }
+// Bytes of one prepared left operand and of the three of a panel tile.
+__host__ __device__ constexpr size_t operand_bytes() { return (size_t)kK * kK * kS * 2; }
+__host__ __device__ constexpr size_t panel_slice_bytes() { return 3 * operand_bytes(); }
+
+// Shared-memory map of the engine.
+constexpr int kOffB = 2 * kAChunkBytes;
+constexpr int kOffBar = kOffB + 2 * kBChunkBytes;
+constexpr int kOffEb = kOffBar + 64;
+constexpr int kOffY = kOffEb + 2 * kN * 4;
+constexpr int kSmemBytes = kOffY + kLdY * kN * 8;
+static_assert(kOffY % 16 == 0, "staged operand alignment");
 
 // ---------------------------------------------------------------------------
 // PTX wrappers
@@ -121,6 +116,11 @@ __device__ __forceinline__ void tma_load_1d(void* dst_smem, const void* src_gmem
 }
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// Orders this thread's generic-proxy global writes (prepared slices) with
+// bulk-TMA reads of them (async proxy).
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
 }
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -196,23 +196,22 @@ __device__ __forceinline__ long long fixed_of(double x, int E) {
     F = (sh > -60) ? ((m + (1LL << (-sh - 1))) >> (-sh)) : 0;
   return (b < 0) ? -F : F;
 }
-// Digits d_1..d_S of F (signed, round to nearest): F = sum d_p 2^(RHO (S - p)).
-template <class SC>
+// Digits d_0..d_6 of F (signed, round to nearest): F = sum d_p 2^(8 (6 - p)).
 __device__ __forceinline__ void digits(long long F, int* d) {
 #pragma unroll
-  for (int p = 0; p < SC::S - 1; p++) {
-    const int u = SC::RHO * (SC::S - 1 - p);
+  for (int p = 0; p < kS - 1; p++) {
+    const int u = kRho * (kS - 1 - p);
     const long long dp = (F + (1LL << (u - 1))) >> u;
     d[p] = (int)dp;
     F -= dp << u;
   }
-  d[SC::S - 1] = (int)F;
+  d[kS - 1] = (int)F;
 }
 __device__ __forceinline__ uint32_t bf16_bits(int d) {
   return __float_as_uint((float)d) >> 16;    // exact: |d| <= 128 has <= 8 significant bits
 }
-// Byte offset of element (row, kk) (kk < 16) inside one K-major slice block
-// of `rows` rows: core matrices [row/8][kk/8][8][16 bytes].
+// Byte offset of element (row, kk) (kk < 16) inside one K-major slice block:
+// core matrices [row/8][kk/8][8][16 bytes].
 __device__ __forceinline__ int core_off(int row, int kk) {
   return ((row >> 3) * 2 + (kk >> 3)) * 128 + (row & 7) * 16 + (kk & 7) * 2;
 }
@@ -224,27 +223,24 @@ struct Ctx {
   uint8_t* sA;          // 2 stages x kAChunkBytes
   uint8_t* sB;          // 2 stages x kBChunkBytes
   uint64_t* bar;        // [0,1] A full, [2,3] MMA done
-  int* sEb;             // kN column exponents of the right operand
-  double* sY;           // the right operand, staged: K x kN doubles, ld K + 1
+  int* sEb;             // 2 x kN column exponents of the right operand
+  double* sY;           // the right operand: kK x kN doubles, ld kLdY
   uint32_t tmem;        // base of the 512 TMEM columns
   uint32_t phase_a[2];  // phase parity per stage (kept identical in every thread)
   uint32_t phase_m[2];
+  int yb;               // which half of sEb describes sY
   unsigned* err;        // scheduler error word
 };
 
-constexpr int kMaxK = 256;
-constexpr int kYBytes = (kMaxK + 1) * kN * 8;
-// Shared-memory bytes the engine needs.
-constexpr int kSmemBytes = 2 * kAChunkBytes + 2 * kBChunkBytes + 64 + kN * 4 + 128 + kYBytes;
-
 __device__ __forceinline__ void ctx_init(Ctx& c, uint8_t* base, uint32_t tmem, unsigned* err) {
   c.sA = base;
-  c.sB = base + 2 * kAChunkBytes;
-  c.bar = reinterpret_cast<uint64_t*>(base + 2 * kAChunkBytes + 2 * kBChunkBytes);
-  c.sEb = reinterpret_cast<int*>(base + 2 * kAChunkBytes + 2 * kBChunkBytes + 64);
-  c.sY = reinterpret_cast<double*>(base + 2 * kAChunkBytes + 2 * kBChunkBytes + 64 + kN * 4 + 128);
+  c.sB = base + kOffB;
+  c.bar = reinterpret_cast<uint64_t*>(base + kOffBar);
+  c.sEb = reinterpret_cast<int*>(base + kOffEb);
+  c.sY = reinterpret_cast<double*>(base + kOffY);
   c.tmem = tmem;
   c.err = err;
+  c.yb = 0;
   if (threadIdx.x == 0) {
     for (int i = 0; i < 4; i++) mbar_init(c.bar + i, 1);
     mbar_fence_init();
@@ -255,48 +251,69 @@ __device__ __forceinline__ void ctx_init(Ctx& c, uint8_t* base, uint32_t tmem, u
   }
   __syncthreads();
 }
+// After the last product of a task: every copy and MMA has completed; the
+// barriers are invalidated so the next task may reuse their shared memory.
+__device__ __forceinline__ void ctx_release(Ctx& c) {
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int i = 0; i < 4; i++)
+      asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(c.bar + i)) : "memory");
+  __syncthreads();
+}
 
 __device__ __forceinline__ void set_err(const Ctx& c) {
   atomicOr(reinterpret_cast<int*>(c.err), kErrTimeout);
 }
 
-// Stage the kN-column right operand Y (K rows, ld ldy, global) in shared
-// memory (ld K + 1: conflict-free column reads) and compute its column
-// exponents (max biased exponent per column).
-inline __device__ void stage_y(Ctx& c, const double* Y, int ldy, int K) {
-  const int lds = K + 1;
-  for (int e = threadIdx.x; e < K * kN / 2; e += kThreads) {
-    const int col = (2 * e) / K, r = (2 * e) % K;               // K is even: pairs stay in a column
-    const double2 v = __ldcg(reinterpret_cast<const double2*>(Y + (size_t)col * ldy + r));
-    c.sY[col * lds + r] = v.x;
-    c.sY[col * lds + r + 1] = v.y;
-  }
-  __syncthreads();
+// Column exponents (max biased exponent) of the staged right operand into
+// sEb[c.yb].
+__device__ __forceinline__ void y_exponents(Ctx& c) {
   const int col = threadIdx.x >> 2, part = threadIdx.x & 3;   // 4 threads per column
   int e = 0;
-  if (col < kN) {
-    const double* y = c.sY + col * lds;
-    for (int r = part; r < K; r += 4) e = max(e, biased_exp(y[r]));
-  }
+  const double* y = c.sY + col * kLdY;
+#pragma unroll 8
+  for (int r = part; r < kK; r += 4) e = max(e, biased_exp(y[r]));
   e = max(e, __shfl_xor_sync(0xffffffffu, e, 1));
   e = max(e, __shfl_xor_sync(0xffffffffu, e, 2));
-  if (col < kN && part == 0) c.sEb[col] = e;
+  if (part == 0) c.sEb[c.yb * kN + col] = e;
   __syncthreads();
 }
 
-// Slice rows [k0, k0+16) of the staged right operand (kN columns) into B stage `s`.
-template <class SC>
-__device__ __forceinline__ void slice_b_chunk(Ctx& c, int s, int K, int k0) {
+// Stage the right operand Y (kK x kN, column-major, ld ldy, global) in
+// shared memory.  unit_col >= 0: Y is the column block starting at column
+// unit_col of a unit-lower V (zero above the diagonal, one on it).
+__device__ __forceinline__ void stage_y(Ctx& c, const double* Y, int ldy, int unit_col) {
+  static_assert(kK * kN / 2 % kThreads == 0, "staging loop");
+  constexpr int kIter = kK * kN / 2 / kThreads;   // 16 pairs per thread
+#pragma unroll 4
+  for (int it = 0; it < kIter; it++) {
+    const int e = threadIdx.x + it * kThreads;
+    const int col = e / (kK / 2), r = 2 * (e % (kK / 2));
+    double2 v = __ldcg(reinterpret_cast<const double2*>(Y + (size_t)col * ldy + r));
+    if (unit_col >= 0) {
+      const int gc = unit_col + col;
+      v.x = (r > gc) ? v.x : (r == gc ? 1.0 : 0.0);
+      v.y = (r + 1 > gc) ? v.y : (r + 1 == gc ? 1.0 : 0.0);
+    }
+    c.sY[col * kLdY + r] = v.x;
+    c.sY[col * kLdY + r + 1] = v.y;
+  }
+  __syncthreads();
+  y_exponents(c);
+}
+
+// Slice rows [k0, k0+16) of the staged right operand into B stage `s`.
+__device__ __forceinline__ void slice_b_chunk(Ctx& c, int s, int k0) {
   const int col = threadIdx.x >> 2, q = threadIdx.x & 3;   // 64 columns x 4 quads of 4 rows
-  const int E = c.sEb[col];
-  const double* y = c.sY + col * (K + 1) + k0 + 4 * q;
-  int d[4][SC::S];
+  const int E = c.sEb[c.yb * kN + col];
+  const double* y = c.sY + col * kLdY + k0 + 4 * q;
+  int d[4][kS];
 #pragma unroll
-  for (int i = 0; i < 4; i++) digits<SC>(fixed_of(y[i], E), d[i]);
+  for (int i = 0; i < 4; i++) digits(fixed_of(y[i], E), d[i]);
   uint8_t* stage = c.sB + s * kBChunkBytes;
   const int off = core_off(col, 4 * q);
 #pragma unroll
-  for (int p = 0; p < SC::S; p++) {
+  for (int p = 0; p < kS; p++) {
     uint2 w;
     w.x = bf16_bits(d[0][p]) | (bf16_bits(d[1][p]) << 16);
     w.y = bf16_bits(d[2][p]) | (bf16_bits(d[3][p]) << 16);
@@ -304,25 +321,22 @@ __device__ __forceinline__ void slice_b_chunk(Ctx& c, int s, int K, int k0) {
   }
 }
 
-// One M-tile (128 rows) of an Ozaki product: the 8 t-group accumulators of
-// X[mt] (prepared slices, K = K chunks [kc0, kc1)) times Y (kN columns, sliced
-// here).  On return (true) the accumulators are final in TMEM.
-template <class SC>
-inline __device__ bool gemm_tile(Ctx& c, const uint8_t* Xprep, int KC, int mt, int kc0, int kc1) {
-  const int K = KC * kKC;
+// The 8 t-group accumulators of X (prepared slices) times the staged right
+// operand.  On return (true) the accumulators are final in TMEM.
+inline __device__ bool gemm(Ctx& c, const uint8_t* Xprep) {
   const uint32_t id = idesc_bf16(kM, kN);
   const uint64_t dA0 = sdesc(smem_u32(c.sA), 128, 256);
   const uint64_t dB0 = sdesc(smem_u32(c.sB), 128, 256);
-  const uint8_t* src = Xprep + (size_t)mt * KC * kAChunkBytes;
   bool ok = true;
-  // prologue: stage 0 <- chunk kc0
+  // prologue: stage 0 <- chunk 0
   if (threadIdx.x == 0) {
+    fence_proxy_async_global();
     mbar_expect_tx(c.bar + 0, kAChunkBytes);
-    tma_load_1d(c.sA, src + (size_t)kc0 * kAChunkBytes, kAChunkBytes, c.bar + 0);
+    tma_load_1d(c.sA, Xprep, kAChunkBytes, c.bar + 0);
   }
-  slice_b_chunk<SC>(c, 0, K, kc0 * kKC);
-  for (int kc = kc0; kc < kc1; kc++) {
-    const int s = (kc - kc0) & 1;
+  slice_b_chunk(c, 0, 0);
+  for (int kc = 0; kc < kChunks; kc++) {
+    const int s = kc & 1;
     fence_proxy_async();
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -331,14 +345,14 @@ inline __device__ bool gemm_tile(Ctx& c, const uint8_t* Xprep, int KC, int mt, i
       if (ok) {
         const uint64_t dA = dA0 + (uint64_t)((s * kAChunkBytes) >> 4);
         const uint64_t dB = dB0 + (uint64_t)((s * kBChunkBytes) >> 4);
-        // pairs (p, q) (0-based) with p + q <= kGroups - 1; t-group ti = p + q;
-        // the first product into each group in chunk kc0 overwrites it
+        // pairs (p, q) with p + q <= kGroups - 1 into t-group p + q; the first
+        // product into each group in chunk 0 overwrites it
 #pragma unroll
-        for (int p = 0; p < SC::S; p++) {
+        for (int p = 0; p < kS; p++) {
 #pragma unroll
-          for (int q = 0; q < SC::S && p + q < kGroups; q++) {
-            const int first_p = (p + q) - (SC::S - 1) > 0 ? (p + q) - (SC::S - 1) : 0;
-            const uint32_t acc = (kc > kc0 || p > first_p) ? 1u : 0u;
+          for (int q = 0; q < kS && p + q < kGroups; q++) {
+            const int first_p = (p + q) - (kS - 1) > 0 ? (p + q) - (kS - 1) : 0;
+            const uint32_t acc = (kc > 0 || p > first_p) ? 1u : 0u;
             mma_bf16(c.tmem + (uint32_t)((p + q) * kN), dA + (uint64_t)((p * kSliceABytes) >> 4),
                      dB + (uint64_t)((q * kSliceBBytes) >> 4), id, acc);
           }
@@ -347,23 +361,22 @@ inline __device__ bool gemm_tile(Ctx& c, const uint8_t* Xprep, int KC, int mt, i
       mma_commit(c.bar + 2 + s);
     }
     c.phase_a[s] ^= 1;
-    if (kc + 1 < kc1) {
+    if (kc + 1 < kChunks) {
       const int s1 = s ^ 1;
-      if (kc + 1 - kc0 >= 2) {   // stage s1 still feeds the MMAs of chunk kc-1
+      if (kc >= 1) {   // stage s1 still feeds the MMAs of chunk kc-1
         if (!mbar_wait(c.bar + 2 + s1, c.phase_m[s1], c.err)) ok = false;
         c.phase_m[s1] ^= 1;
       }
       if (threadIdx.x == 0) {
         mbar_expect_tx(c.bar + s1, kAChunkBytes);
-        tma_load_1d(c.sA + s1 * kAChunkBytes, src + (size_t)(kc + 1) * kAChunkBytes, kAChunkBytes,
+        tma_load_1d(c.sA + s1 * kAChunkBytes, Xprep + (size_t)(kc + 1) * kAChunkBytes, kAChunkBytes,
                     c.bar + s1);
       }
-      slice_b_chunk<SC>(c, s1, K, (kc + 1) * kKC);
+      slice_b_chunk(c, s1, (kc + 1) * kKC);
     }
   }
-  // drain the (up to two) outstanding commits
-  const int n = kc1 - kc0;
-  for (int k = (n >= 2 ? n - 2 : 0); k < n; k++) {
+  // the two outstanding commits
+  for (int k = kChunks - 2; k < kChunks; k++) {
     const int s = k & 1;
     if (!mbar_wait(c.bar + 2 + s, c.phase_m[s], c.err)) ok = false;
     c.phase_m[s] ^= 1;
@@ -373,13 +386,6 @@ inline __device__ bool gemm_tile(Ctx& c, const uint8_t* Xprep, int KC, int mt, i
   if (!ok && threadIdx.x == 0) set_err(c);
   return ok;
 }
-
-// Epilogue modes.
-enum Epi : int {
-  kEpiStoreAdd = 0,   // out = addend (or 0) + R
-  kEpiStoreSub = 1,   // out = R; top -= R (when top != nullptr)
-  kEpiSubInto = 2,    // tgt -= R
-};
 
 // X * 2^(se - 1023) as binary64, rounded to nearest even, built with integer
 // operations from the IEEE 754 encoding (normalise |X|, round to 53 bits,
@@ -408,19 +414,34 @@ __device__ __forceinline__ double scaled_i64(long long X, int se) {
   return __longlong_as_double((long long)(sign | bits));
 }
 
-// Recombine the 8 t-group accumulators of M-tile mt into FP64 and apply the
-// epilogue.  Warp w handles rows 32*(w%4).., columns 32*(w/4)..+31.
-template <class SC>
-inline __device__ void drain(Ctx& c, int mt, const int* Ea, int mode, double* out, int ldo,
-                             const double* addend, int lda, double* top, int ldt) {
+// Epilogue modes (R = the product just computed).
+enum Epi : int {
+  kEpiStore = 0,      // g = R                                   (global)
+  kEpiToY = 1,        // sY = gm + R (gm global, may be null)    -> next right operand
+  kEpiToYSubTop = 2,  // sY = R; gm -= R (gm global, may be null) -> next right operand
+  kEpiSubInto = 3,    // g -= R                                  (global)
+};
+
+// Recombine the 8 t-group accumulators into FP64 and apply the epilogue.
+// Warp w handles rows 32*(w%4).., columns 32*(w/4)..+31.  Ea: row exponents
+// of X (global).
+inline __device__ void drain(Ctx& c, const int* Ea, int mode, double* g, int ldg, double* gm,
+                             int ldm) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int row = mt * kM + 32 * (w & 3) + lane;
+  const int row = 32 * (w & 3) + lane;
   const int cb = 32 * (w >> 2);
   const int ea = __ldcg(Ea + row);
   const uint32_t lane_addr = c.tmem + ((uint32_t)(32 * (w & 3)) << 16);
-  // the memory operand of each mode: addend, top, or the target itself
-  const double* msrc = (mode == kEpiStoreAdd) ? addend : (mode == kEpiStoreSub) ? top : out;
-  const int mld = (mode == kEpiStoreAdd) ? lda : (mode == kEpiStoreSub) ? ldt : ldo;
+  const bool to_y = (mode == kEpiToY || mode == kEpiToYSubTop);
+  const int nb = c.yb ^ 1;   // exponents of the new right operand
+  if (to_y) {
+    if (threadIdx.x < kN) c.sEb[nb * kN + threadIdx.x] = 0;
+    __syncthreads();
+  }
+  // the memory operand of each mode
+  const double* msrc = (mode == kEpiSubInto) ? g : (mode == kEpiStore) ? nullptr : gm;
+  const int mld = (mode == kEpiSubInto) ? ldg : ldm;
+#pragma unroll 1
   for (int pass = 0; pass < 32 / kDC; pass++) {
     const int c0 = cb + kDC * pass;
     // issue the memory loads before the TMEM reads so they overlap
@@ -436,104 +457,122 @@ inline __device__ void drain(Ctx& c, int mt, const int* Ea, int mode, double* ou
       tmem_ld8(lane_addr + (uint32_t)(t * kN + c0), v);
 #pragma unroll
       for (int i = 0; i < kDC; i++) {
-        const long long g = (long long)__float2int_rn(v[i]);
+        const long long q = (long long)__float2int_rn(v[i]);
         if (t < 4)
-          hi[i] = (hi[i] << SC::RHO) + g;
+          hi[i] = (hi[i] << kRho) + q;
         else
-          lo[i] = (lo[i] << SC::RHO) + g;
+          lo[i] = (lo[i] << kRho) + q;
       }
     }
 #pragma unroll
     for (int i = 0; i < kDC; i++) {
       const int col = c0 + i;
-      const long long X =
-          (hi[i] << SC::SHIFT_HI) + ((lo[i] + (1LL << (SC::SHIFT_LO - 1))) >> SC::SHIFT_LO);
-      const int eb = c.sEb[col];
-      const int se = ea + eb - SC::EXP_BIAS;   // biased exponent of the scale of X
-      const double r = (ea > 0 && eb > 0) ? scaled_i64(X, se) : 0.0;
+      const long long X = (hi[i] << kShiftHi) + ((lo[i] + (1LL << (kShiftLo - 1))) >> kShiftLo);
+      const int eb = c.sEb[c.yb * kN + col];
+      const double r = (ea > 0 && eb > 0) ? scaled_i64(X, ea + eb - kExpBias) : 0.0;
       const size_t o = (size_t)col;
-      if (mode == kEpiStoreAdd) {
-        stg_cg(out + row + o * ldo, mem[i] + r);
-      } else if (mode == kEpiStoreSub) {
-        stg_cg(out + row + o * ldo, r);
-        if (top) stg_cg(top + row + o * ldt, mem[i] - r);
+      double y = 0.0;
+      if (mode == kEpiStore) {
+        stg_cg(g + row + o * ldg, r);
+      } else if (mode == kEpiToY) {
+        y = mem[i] + r;
+      } else if (mode == kEpiToYSubTop) {
+        y = r;
+        if (gm) stg_cg(gm + row + o * ldm, mem[i] - r);
       } else {
-        stg_cg(out + row + o * ldo, mem[i] - r);
+        stg_cg(g + row + o * ldg, mem[i] - r);
+      }
+      if (to_y) {
+        c.sY[col * kLdY + row] = y;
+        const unsigned e = __reduce_max_sync(0xffffffffu, (unsigned)biased_exp(y));
+        if (lane == 0) atomicMax(c.sEb + nb * kN + col, (int)e);
       }
     }
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
+  if (to_y) c.yb = nb;
 }
 
-// One full Ozaki product for an NB-row left operand (all M-tiles).
-// tri: 0 dense, 1 X lower triangular (rows r need K <= r), 2 X upper
-// triangular (rows r need K >= r).
-template <class SC>
-inline __device__ bool product(Ctx& c, int NB, const uint8_t* Xprep, const int* Ea, int tri,
-                               const double* Y, int ldy, int mode, double* out, int ldo,
-                               const double* addend, int lda, double* top, int ldt) {
-  const int KC = NB / kKC;
-  stage_y(c, Y, ldy, NB);
-  for (int mt = 0; mt < NB / kM; mt++) {
-    int kc0 = 0, kc1 = KC;
-    if (tri == 1) kc1 = min(KC, (mt + 1) * kM / kKC);
-    if (tri == 2) kc0 = mt * kM / kKC;
-    if (!gemm_tile<SC>(c, Xprep, KC, mt, kc0, kc1)) return false;
-    drain<SC>(c, mt, Ea, mode, out, ldo, addend, lda, top, ldt);
-  }
+// One product: X (prepared, row exponents Ea) times the staged right operand.
+inline __device__ bool product(Ctx& c, const uint8_t* Xprep, const int* Ea, int mode, double* g,
+                               int ldg, double* gm, int ldm) {
+  if (!gemm(c, Xprep)) return false;
+  drain(c, Ea, mode, g, ldg, gm, ldm);
   return true;
 }
 
 // ---------------------------------------------------------------------------
-// Preparation of a panel tile's left operands (once per panel tile)
+// Preparation of a left operand (once per panel tile)
 // ---------------------------------------------------------------------------
-// Slice an NB x NB left operand X into the [mt][kc][slice][core layout]
-// order; X(r, k) = src[r*rs + k*ks]; Ea[r] = max biased exponent of row r.
-template <class SC>
-inline __device__ void prep_operand(const double* src, int rs, int ks, int NB, uint8_t* dst, int* Ea,
-                                    int kind_unit_lower) {
-  // row exponents
-  for (int r = threadIdx.x; r < NB; r += kThreads) {
+// Element masks of the panel tile's operands.
+enum Kind : int {
+  kDense = 0,
+  kUnitLower = 1,    // V of a GEQRT tile: zero above the diagonal, one on it
+  kUnitUpper = 2,    // V^T of a GEQRT tile
+};
+
+// Slice the 128 x 128 left operand X(r, k) = acc(r, k) (shared memory) into
+// the [kc][slice][core layout] order at dst (global) and write its row
+// exponents to Ea (global); sE: 128 ints of shared scratch.
+template <class Acc>
+inline __device__ void slice_left(const Acc& acc, uint8_t* dst, int* Ea, int* sE) {
+  if (threadIdx.x < kK) {
+    const int r = threadIdx.x;
     int e = 0;
-    for (int k = 0; k < NB; k++) {
-      double x = ldg_cg(src + (size_t)r * rs + (size_t)k * ks);
-      if (kind_unit_lower == 1) x = (r > k) ? x : (r == k ? 1.0 : 0.0);        // V (unit lower)
-      if (kind_unit_lower == 2) x = (k > r) ? x : (k == r ? 1.0 : 0.0);        // V^T of unit lower V
-      if (kind_unit_lower == 3) x = (k <= r) ? x : 0.0;                          // T^T (lower)
-      e = max(e, biased_exp(x));
-    }
+#pragma unroll 8
+    for (int k = 0; k < kK; k++) e = max(e, biased_exp(acc(r, k)));
+    sE[r] = e;
     Ea[r] = e;
   }
   __syncthreads();
-  const int KC = NB / kKC;
-  // one thread per (row, k-quad)
-  const int quads = NB * NB / 4;
-  for (int qd = threadIdx.x; qd < quads; qd += kThreads) {
-    const int r = qd % NB;
-    const int k4 = (qd / NB) * 4;
-    const int E = Ea[r];
-    int d[4][SC::S];
+  constexpr int kQuads = kK * kK / 4;
+  for (int qd = threadIdx.x; qd < kQuads; qd += kThreads) {
+    const int r = qd % kK;
+    const int k4 = (qd / kK) * 4;
+    const int E = sE[r];
+    int d[4][kS];
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-      const int k = k4 + i;
-      double x = ldg_cg(src + (size_t)r * rs + (size_t)k * ks);
-      if (kind_unit_lower == 1) x = (r > k) ? x : (r == k ? 1.0 : 0.0);
-      if (kind_unit_lower == 2) x = (k > r) ? x : (k == r ? 1.0 : 0.0);
-      if (kind_unit_lower == 3) x = (k <= r) ? x : 0.0;
-      digits<SC>(fixed_of(x, E), d[i]);
-    }
-    const int mt = r / kM, kc = k4 / kKC;
-    uint8_t* blk = dst + ((size_t)mt * KC + kc) * kAChunkBytes;
-    const int off = core_off(r % kM, k4 % kKC);
+    for (int i = 0; i < 4; i++) digits(fixed_of(acc(r, k4 + i), E), d[i]);
+    uint8_t* blk = dst + (size_t)(k4 / kKC) * kAChunkBytes;
+    const int off = core_off(r, k4 % kKC);
 #pragma unroll
-    for (int p = 0; p < SC::S; p++) {
+    for (int p = 0; p < kS; p++) {
       uint2 w;
       w.x = bf16_bits(d[0][p]) | (bf16_bits(d[1][p]) << 16);
       w.y = bf16_bits(d[2][p]) | (bf16_bits(d[3][p]) << 16);
       *reinterpret_cast<uint2*>(blk + p * kSliceABytes + off) = w;
     }
+  }
+  fence_proxy_async_global();
+  __syncthreads();
+}
+
+// Accessor of a 128 x 128 column-major matrix S staged in shared memory with
+// leading dimension kLdY: X = S or X = S^T, with an element mask.
+struct StagedAcc {
+  const double* s;
+  int rs, ks;   // X(r, k) = s[r * rs + k * ks]
+  int kind;
+  __device__ __forceinline__ double operator()(int r, int k) const {
+    const double x = s[r * rs + k * ks];
+    if (kind == kUnitLower) return (r > k) ? x : (r == k ? 1.0 : 0.0);
+    if (kind == kUnitUpper) return (k > r) ? x : (k == r ? 1.0 : 0.0);
+    return x;
+  }
+};
+
+// Stage a 128 x 128 column-major tile (global, ld kK) in shared memory, ld kLdY.
+__device__ __forceinline__ void stage_tile(double* s, const double* src) {
+  constexpr int kIter = kK * kK / 2 / kThreads;   // 32 pairs per thread
+#pragma unroll 4
+  for (int it = 0; it < kIter; it++) {
+    const int e = threadIdx.x + it * kThreads;
+    const int col = e / (kK / 2), r = 2 * (e % (kK / 2));
+    const double2 v = __ldcg(reinterpret_cast<const double2*>(src + (size_t)col * kK + r));
+    s[col * kLdY + r] = v.x;
+    s[col * kLdY + r + 1] = v.y;
   }
   __syncthreads();
 }

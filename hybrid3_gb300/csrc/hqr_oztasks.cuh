@@ -1,97 +1,123 @@
-// hqr_oztasks.cuh -- tile tasks of the split-precision path.
+// hqr_oztasks.cuh -- tile tasks of the split-precision path (NB = 128).
 //
-//   OZPREP(i,k): full NB x NB upper T of panel tile (k,i) (LAPACK dlarft,
-//     forward, columnwise, from V and TAU -- the rebuild Hybrid_make_Q does
-//     with IB = NB, Hybrid_make_Q.c:124-130,159-163) and the sliced left
-//     operands V^T, T^T and V of that tile.
+//   OZPREP(i,k): the sliced left operands V^T, T^T and V of panel tile (k,i),
+//     with the full NB x NB upper T of the tile (LAPACK dlarft, forward,
+//     columnwise, from V and TAU -- the rebuild Hybrid_make_Q does with
+//     IB = NB, Hybrid_make_Q.c:124-130,159-163).  G = V^T V runs on the tensor
+//     cores (two products); the T recurrence runs in shared memory.
 //   OZAPPLY: one 64-column block of a LARFB (CORE_dormqr, V unit lower) or
-//     SSRFB (CORE_dtsmqr, V dense) as three Ozaki products on the tensor
-//     cores:  W = C_top + V^T C_bot;  W2 = T^T W;  C_top -= W2;  C_bot -= V W2.
+//     SSRFB (CORE_dtsmqr, V dense) as three products:
+//       W = C_top + V^T C_bot;  W2 = T^T W;  C_top -= W2;  C_bot -= V W2,
+//     with W and W2 kept in shared memory between the products.
 #pragma once
 #include "hqr_ozaki.cuh"
 
 namespace hqr {
 
-// dlarft 'F','C' with k = NB: T (global, NB x NB, ld NB) from V (global) and
-// TAU.  unit: V is the unit-lower part of a GEQRT tile, else a dense TS V
-// (whose top part is the identity).  g: NB doubles of shared memory.
-inline __device__ void build_full_t(const double* V, const double* tau, double* T, bool unit, int NB,
-                                    double* g) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int c = 0; c < NB; c++) {
-    const double* vc = V + (size_t)c * NB;
-    for (int a = warp; a < c; a += kWarps) {
-      const double* va = V + (size_t)a * NB;
-      double s = 0.0;
-      for (int r = (unit ? c + 1 : 0) + lane; r < NB; r += 32) s = fma(ldg_cg(va + r), ldg_cg(vc + r), s);
-      s = warp_sum(s);
-      if (lane == 0) g[a] = unit ? s + ldg_cg(va + c) : s;
-    }
-    __syncthreads();
-    const double tc = ldg_cg(tau + c);
-    for (int a = threadIdx.x; a < NB; a += kThreads) {
-      double v;
-      if (a < c) {
-        double s = 0.0;
-        for (int b = a; b < c; b++) s = fma(ldg_cg(T + a + (size_t)b * NB), g[b], s);
-        v = (tc == 0.0) ? 0.0 : -tc * s;
-      } else {
-        v = (a == c) ? tc : 0.0;
+// Offsets of a panel tile's three prepared operands and their row exponents.
+constexpr size_t kOzVT = 0, kOzTT = 1, kOzV = 2;
+
+// X(r, k) = T^T(r, k) = T(k, r), T upper triangular, packed by columns in
+// shared memory: T(a, b) (a <= b) at b (b + 1) / 2 + a.
+struct PackedTTAcc {
+  const double* t;
+  __device__ __forceinline__ double operator()(int r, int k) const {
+    return (k <= r) ? t[r * (r + 1) / 2 + k] : 0.0;
+  }
+};
+
+// T recurrence (dlarft 'F','C', k = NB = 128) in shared memory:
+//   T(c, c) = tau_c;  T(0:c, c) = -tau_c T(0:c, 0:c) G(0:c, c)  (zero when tau_c = 0)
+// sG: strictly upper part of G = V^T V, packed: G(b, c) (b < c) at c (c - 1) / 2 + b.
+// sT: the result, packed upper (see PackedTTAcc).  Two threads per row.
+inline __device__ void t_recurrence(const double* sG, double* sT, const double* tau) {
+  const int a = threadIdx.x >> 1, h = threadIdx.x & 1;
+  for (int c = 0; c < oz::kK; c++) {
+    const double tc = __ldcg(tau + c);
+    double s0 = 0.0, s1 = 0.0;
+    if (a < c) {
+      const int mid = a + (c - a + 1) / 2;
+      const int b0 = h ? mid : a, b1 = h ? c : mid;
+      const double* g = sG + c * (c - 1) / 2;
+      int b = b0;
+      for (; b + 1 < b1; b += 2) {
+        s0 = fma(sT[b * (b + 1) / 2 + a], g[b], s0);
+        s1 = fma(sT[(b + 1) * (b + 2) / 2 + a], g[b + 1], s1);
       }
-      stg_cg(T + a + (size_t)c * NB, v);
+      if (b < b1) s0 = fma(sT[b * (b + 1) / 2 + a], g[b], s0);
     }
+    double s = s0 + s1;
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    if (h == 0 && a <= c) sT[c * (c + 1) / 2 + a] = (a == c) ? tc : (tc == 0.0 ? 0.0 : -tc * s);
     __syncthreads();
   }
 }
 
-// Slice-store layout of a panel tile: [V^T | T^T | V], each oz::operand_bytes(NB).
-template <class SC>
-__device__ void prep_operands(const double* V, const double* T, bool unit, int NB, uint8_t* slices,
-                              int* exps) {
-  const size_t ob = oz::operand_bytes(NB);
-  oz::prep_operand<SC>(V, NB, 1, NB, slices, exps, unit ? 2 : 0);                 // V^T
-  oz::prep_operand<SC>(T, NB, 1, NB, slices + ob, exps + NB, 3);                  // T^T
-  oz::prep_operand<SC>(V, 1, NB, NB, slices + 2 * ob, exps + 2 * NB, unit ? 1 : 0);  // V
-}
-inline __device__ void task_ozprep(const double* V, const double* tau, double* T, bool unit, int NB,
-                                   uint8_t* slices, int* exps, double* smem) {
-  build_full_t(V, tau, T, unit, NB, smem);
-  if (NB <= 128)
-    prep_operands<oz::Scheme8x7>(V, T, unit, NB, slices, exps);
-  else
-    prep_operands<oz::Scheme7x8>(V, T, unit, NB, slices, exps);
+// OZPREP of panel tile V (global, NB x NB; unit: the V of a GEQRT tile, else
+// the dense V of a TSQRT tile) with TAU tau.  G: NB x NB global scratch.
+// slices / exps: this tile's prepared operands and row exponents.  sm: the
+// CTA's dynamic shared memory (oz::kSmemBytes).  False on a device time-out.
+inline __device__ bool task_ozprep(const double* V, const double* tau, double* G, bool unit,
+                                   uint8_t* slices, int* exps, uint8_t* sm, uint32_t tmem,
+                                   unsigned* err) {
+  using namespace oz;
+  constexpr size_t ob = operand_bytes();
+  // 1. V^T and V from a shared-memory copy of the tile
+  {
+    double* sV = reinterpret_cast<double*>(sm);
+    int* sE = reinterpret_cast<int*>(sm + kLdY * kK * 8);
+    stage_tile(sV, V);
+    slice_left(StagedAcc{sV, kLdY, 1, unit ? kUnitUpper : kDense}, slices + kOzVT * ob,
+               exps + kOzVT * kK, sE);
+    slice_left(StagedAcc{sV, 1, kLdY, unit ? kUnitLower : kDense}, slices + kOzV * ob,
+               exps + kOzV * kK, sE);
+  }
+  // 2. G = V^T V on the tensor cores, by 64-column blocks, into G (global)
+  {
+    Ctx c;
+    ctx_init(c, sm, tmem, err);
+    for (int cb = 0; cb < kK / kN; cb++) {
+      stage_y(c, V + (size_t)cb * kN * kK, kK, unit ? cb * kN : -1);
+      if (!product(c, slices + kOzVT * ob, exps + kOzVT * kK, kEpiStore, G + (size_t)cb * kN * kK, kK,
+                   nullptr, 0))
+        return false;
+    }
+    ctx_release(c);
+  }
+  __threadfence_block();
+  // 3. T in shared memory
+  double* sG = reinterpret_cast<double*>(sm);
+  double* sT = sG + kK * (kK - 1) / 2;
+  int* sE = reinterpret_cast<int*>(sT + kK * (kK + 1) / 2);
+  constexpr int kPacked = kK * (kK - 1) / 2;
+#pragma unroll 4
+  for (int idx = threadIdx.x; idx < kPacked; idx += kThreads) {
+    // column c of packed index idx: c (c - 1) / 2 <= idx < (c + 1) c / 2
+    int c = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)idx)) * 0.5f);
+    while (c * (c - 1) / 2 > idx) c--;
+    while ((c + 1) * c / 2 <= idx) c++;
+    sG[idx] = __ldcg(G + (idx - c * (c - 1) / 2) + (size_t)c * kK);
+  }
+  __syncthreads();
+  t_recurrence(sG, sT, tau);
+  // 4. T^T
+  slice_left(PackedTTAcc{sT}, slices + kOzTT * ob, exps + kOzTT * kK, sE);
+  return true;
 }
 
 // One 64-column block of the update.  Ctop: A1 block (SSRFB) or nullptr
-// (LARFB); Cbot: A2 block (SSRFB) or the C block (LARFB); ld NB.  W, W2:
-// per-CTA scratch of NB x 64 doubles (ld NB).  Returns false on a device
-// time-out (error word already set).
-template <class SC>
-__device__ bool ozapply_products(oz::Ctx& c, int NB, const uint8_t* slices, const int* exps, bool unit,
-                                 double* Ctop, double* Cbot, double* W, double* W2) {
-  const size_t ob = oz::operand_bytes(NB);
-  if (!oz::product<SC>(c, NB, slices, exps, unit ? 2 : 0, Cbot, NB, oz::kEpiStoreAdd, W, NB, Ctop,
-                       NB, nullptr, 0))
+// (LARFB); Cbot: A2 block (SSRFB) or the C block (LARFB); ld NB.  Returns
+// false on a device time-out (error word already set).
+inline __device__ bool task_ozapply(oz::Ctx& c, const uint8_t* slices, const int* exps, double* Ctop,
+                                    double* Cbot) {
+  using namespace oz;
+  constexpr size_t ob = operand_bytes();
+  stage_y(c, Cbot, kK, -1);
+  if (!product(c, slices + kOzVT * ob, exps + kOzVT * kK, kEpiToY, nullptr, 0, Ctop, kK)) return false;
+  if (!product(c, slices + kOzTT * ob, exps + kOzTT * kK, kEpiToYSubTop, nullptr, 0, Ctop, kK))
     return false;
-  if (!oz::product<SC>(c, NB, slices + ob, exps + NB, 1, W, NB, oz::kEpiStoreSub, W2, NB, nullptr,
-                       0, Ctop, NB))
-    return false;
-  return oz::product<SC>(c, NB, slices + 2 * ob, exps + 2 * NB, unit ? 1 : 0, W2, NB,
-                         oz::kEpiSubInto, Cbot, NB, nullptr, 0, nullptr, 0);
-}
-inline __device__ bool task_ozapply(oz::Ctx& c, int NB, const uint8_t* slices, const int* exps,
-                                    bool unit, double* Ctop, double* Cbot, double* W, double* W2) {
-  const bool ok = (NB <= 128)
-                      ? ozapply_products<oz::Scheme8x7>(c, NB, slices, exps, unit, Ctop, Cbot, W, W2)
-                      : ozapply_products<oz::Scheme7x8>(c, NB, slices, exps, unit, Ctop, Cbot, W, W2);
-  if (!ok) return false;
-  // every copy and MMA has completed: release the barriers, whose shared
-  // memory the next task may use for other data
-  __syncthreads();
-  if (threadIdx.x == 0)
-    for (int i = 0; i < 4; i++)
-      asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(oz::smem_u32(c.bar + i)) : "memory");
-  __syncthreads();
+  if (!product(c, slices + kOzV * ob, exps + kOzV * kK, kEpiSubInto, Cbot, kK, nullptr, 0)) return false;
+  ctx_release(c);
   return true;
 }
 

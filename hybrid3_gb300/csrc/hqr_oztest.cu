@@ -1,5 +1,5 @@
 // hqr_oztest.cu -- the split-precision product engine on its own: C = X Y for
-// an NB x NB left operand X and an NB x 64 right operand Y (column-major
+// a 128 x 128 left operand X and a 128 x 64 right operand Y (column-major
 // FP64), through exactly the slicing, tcgen05 products and recombination the
 // update tasks use.  A diagnostic / unit-test entry point.
 #include "hqr_ozaki.cuh"
@@ -7,30 +7,24 @@
 
 namespace hqr {
 
-__global__ void __launch_bounds__(kThreads, 1) k_ozaki_product(int NB, const double* X, const double* Y,
-                                                             double* C, uint8_t* prep, int* exps,
-                                                             unsigned* err) {
+__global__ void __launch_bounds__(kThreads, 1) k_ozaki_product(const double* X, const double* Y, double* C,
+                                                             uint8_t* prep, int* exps, unsigned* err) {
   extern __shared__ __align__(1024) uint8_t sm[];
   __shared__ uint32_t s_tmem;
   if ((threadIdx.x >> 5) == 0) oz::tmem_alloc(&s_tmem, 512);
   oz::tc_fence_before();
   __syncthreads();
   oz::tc_fence_after();
-  // X(r, k) = X[r + k*NB]: row stride 1, column stride NB
-  if (NB <= 128)
-    oz::prep_operand<oz::Scheme8x7>(X, 1, NB, NB, prep, exps, 0);
-  else
-    oz::prep_operand<oz::Scheme7x8>(X, 1, NB, NB, prep, exps, 0);
-  __threadfence();
-  __syncthreads();
+  {
+    double* sX = reinterpret_cast<double*>(sm);
+    int* sE = reinterpret_cast<int*>(sm + oz::kLdY * oz::kK * 8);
+    oz::stage_tile(sX, X);
+    oz::slice_left(oz::StagedAcc{sX, 1, oz::kLdY, oz::kDense}, prep, exps, sE);
+  }
   oz::Ctx c;
   oz::ctx_init(c, sm, s_tmem, err);
-  if (NB <= 128)
-    oz::product<oz::Scheme8x7>(c, NB, prep, exps, 0, Y, NB, oz::kEpiStoreAdd, C, NB, nullptr, 0,
-                               nullptr, 0);
-  else
-    oz::product<oz::Scheme7x8>(c, NB, prep, exps, 0, Y, NB, oz::kEpiStoreAdd, C, NB, nullptr, 0,
-                               nullptr, 0);
+  oz::stage_y(c, Y, oz::kK, -1);
+  if (oz::product(c, prep, exps, oz::kEpiStore, C, oz::kK, nullptr, 0)) oz::ctx_release(c);
   oz::tc_fence_before();
   __syncthreads();
   oz::tc_fence_after();
@@ -40,12 +34,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozaki_product(int NB, const dou
 }  // namespace hqr
 
 extern "C" int hqr_ozaki_product(int NB, const double* dX, const double* dY, double* dC, void* stream) {
-  if (!dX || !dY || !dC || NB % hqr::oz::kM != 0 || NB > 256) return HQR_ERR_INVALID;
+  if (!dX || !dY || !dC) return HQR_ERR_INVALID;
+  if (NB != hqr::oz::kK) return HQR_ERR_UNSUPPORTED;
   cudaStream_t s = (cudaStream_t)stream;
   uint8_t* prep = nullptr;
   int* exps = nullptr;
   unsigned* err = nullptr;
-  if (cudaMalloc(&prep, hqr::oz::operand_bytes(NB)) != cudaSuccess ||
+  if (cudaMalloc(&prep, hqr::oz::operand_bytes()) != cudaSuccess ||
       cudaMalloc(&exps, NB * sizeof(int)) != cudaSuccess || cudaMalloc(&err, sizeof(unsigned)) != cudaSuccess) {
     cudaFree(prep);
     cudaFree(exps);
@@ -54,7 +49,7 @@ extern "C" int hqr_ozaki_product(int NB, const double* dX, const double* dY, dou
   cudaMemsetAsync(err, 0, sizeof(unsigned), s);
   cudaFuncSetAttribute(hqr::k_ozaki_product, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        hqr::oz::kSmemBytes);
-  hqr::k_ozaki_product<<<1, hqr::kThreads, hqr::oz::kSmemBytes, s>>>(NB, dX, dY, dC, prep, exps, err);
+  hqr::k_ozaki_product<<<1, hqr::kThreads, hqr::oz::kSmemBytes, s>>>(dX, dY, dC, prep, exps, err);
   unsigned herr = 0;
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s);

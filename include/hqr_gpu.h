@@ -32,7 +32,8 @@ extern "C" {
 
 /* Arithmetic of the trailing updates (panels are always FP64). */
 #define HQR_PREC_FP64 0    /* FP64 on CUDA cores */
-#define HQR_PREC_OZAKI 1   /* split-precision slices on the tensor cores, FP64 recombination */
+#define HQR_PREC_OZAKI 1   /* split-precision slices on the tensor cores, FP64 recombination;
+                              NB = 128 only (HQR_ERR_UNSUPPORTED otherwise) */
 
 /* Error behaviour of the drop-in (Hybrid_*, tile_*) entry points. */
 #define HQR_ERRORS_ABORT 0   /* print to stderr and exit(1) (the reference's MPI_Abort) */
@@ -120,7 +121,7 @@ int hqr_tiles_to_colmajor(long M, long N, int NB, const double *dT, double *dCM,
 int hqr_colmajor_to_tiles(long M, long N, int NB, const double *dCM, double *dT, void *stream);
 /* The split-precision product engine on its own (diagnostics / tests):
  * dC = dX dY for dX NB x NB and dY NB x 64, column-major device arrays,
- * NB in {128, 256}; same slicing, tensor-core products and recombination as
+ * NB = 128; same slicing, tensor-core products and recombination as
  * the HQR_PREC_OZAKI updates.  Synchronous. */
 int hqr_ozaki_product(int NB, const double *dX, const double *dY, double *dC, void *stream);
 /* Measured FP64 FMA issue rate of this GPU in TFLOP/s (a ~10 ms probe of

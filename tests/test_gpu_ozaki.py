@@ -45,8 +45,8 @@ def factor(torch, H, A, M, N, NB, IB, prec):
     return plan, dA, dTAU
 
 
-SHAPES = [(256, 256, 128, 32), (512, 512, 128, 32), (512, 256, 128, 32), (512, 512, 256, 32),
-          (768, 512, 256, 64), (1024, 1024, 128, 32)]
+SHAPES = [(256, 256, 128, 32), (512, 512, 128, 32), (512, 256, 128, 32), (768, 512, 128, 64),
+          (384, 640, 128, 16), (1024, 1024, 128, 32)]
 
 
 @pytest.mark.parametrize("M,N,NB,IB", SHAPES)
@@ -68,7 +68,7 @@ def test_split_factorization_matches_oracle(env, M, N, NB, IB):
     plan.close()
 
 
-@pytest.mark.parametrize("M,N,NB,IB", [(512, 512, 128, 32), (512, 512, 256, 32), (768, 512, 256, 32)])
+@pytest.mark.parametrize("M,N,NB,IB", [(512, 512, 128, 32), (1024, 1024, 128, 64), (768, 512, 128, 32)])
 def test_split_make_q_and_ormqr(env, M, N, NB, IB):
     torch, H = env
     A2d = O.uniform_matrix(M, N, 900 + M)
@@ -104,11 +104,11 @@ def quality(A2d, q_tiles, r_tiles, M, N, NB):
             np.linalg.norm(Qt @ Qt.T - np.eye(M)))
 
 
-@pytest.mark.parametrize("NB", [128, 256])
-def test_split_product_is_as_accurate_as_fp64(env, NB):
+def test_split_product_is_as_accurate_as_fp64(env):
     """The product engine alone (hqr_ozaki_product): exact on integers, and no
     worse than an FP64 matrix product against a quad-precision reference."""
     torch, H = env
+    NB = 128
     rng = np.random.default_rng(NB)
 
     def run(X, Y):
@@ -160,8 +160,10 @@ def test_split_through_drop_in_entry_points(env):
     assert orth <= 4 * ref_orth
 
 
-def test_split_rejects_unsupported_tile_order(env):
+@pytest.mark.parametrize("NB", [64, 256])
+def test_split_rejects_unsupported_tile_order(env, NB):
     torch, H = env
     h = ctypes.c_void_p()
-    assert H.lib().hqr_plan_create(ctypes.byref(h), 192, 192, 64, 16, H.HQR_PREC_OZAKI) == \
+    assert H.lib().hqr_plan_create(ctypes.byref(h), 4 * NB, 4 * NB, NB, 16, H.HQR_PREC_OZAKI) == \
         H.HQR_ERR_UNSUPPORTED
+    assert H.lib().hqr_ozaki_product(NB, 1, 1, 1, None) == H.HQR_ERR_UNSUPPORTED
