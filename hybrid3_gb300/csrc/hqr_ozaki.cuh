@@ -48,7 +48,7 @@ constexpr int kGroups = 8;         // t-group accumulators: t = p + q in [0, 7]
 constexpr int kShiftHi = 14;       // X = (hi << kShiftHi) + (lo >> kShiftLo)
 constexpr int kShiftLo = 18;
 constexpr int kExpBias = 1073;     // biased exponent of the scale of X = Ea + Eb - kExpBias
-constexpr int kDC = 8;             // accumulator columns recombined per epilogue pass
+constexpr int kDC = 8;             // accumulator columns recombined per epilogue pass (tmem_ld_groups)
 constexpr int kLdY = kK + 1;       // leading dimension of the staged right operand
 constexpr int kSliceABytes = kM * kKC * 2;              // 4 KiB
 constexpr int kSliceBBytes = kN * kKC * 2;              // 2 KiB
@@ -60,12 +60,21 @@ constexpr long long kWaitIters = 1LL << 26;             // bounded mbarrier wait
 __host__ __device__ constexpr size_t operand_bytes() { return (size_t)kK * kK * kS * 2; }
 __host__ __device__ constexpr size_t panel_slice_bytes() { return 3 * operand_bytes(); }
 
+// Pipeline depth: A chunks (bulk TMA) and sliced B chunks in flight.
+constexpr int kAStages = 3;
+constexpr int kBStages = 4;
+constexpr int kSlicerWarps = kWarps - 1;   // warp 0 issues the copies and the MMAs
+// Barriers: a_full[kAStages] (TMA bytes), b_full[kBStages] (one arrival per
+// slicer warp), done[kBStages] (tcgen05.commit of one chunk's MMAs).
+constexpr int kBarAFull = 0, kBarBFull = kAStages, kBarDone = kAStages + kBStages;
+constexpr int kNumBars = kAStages + 2 * kBStages;
 // Shared-memory map of the engine.
-constexpr int kOffB = 2 * kAChunkBytes;
-constexpr int kOffBar = kOffB + 2 * kBChunkBytes;
-constexpr int kOffEb = kOffBar + 64;
+constexpr int kOffB = kAStages * kAChunkBytes;
+constexpr int kOffBar = kOffB + kBStages * kBChunkBytes;
+constexpr int kOffEb = kOffBar + 128;
 constexpr int kOffY = kOffEb + 2 * kN * 4;
 constexpr int kSmemBytes = kOffY + kLdY * kN * 8;
+static_assert(kNumBars * 8 <= 128, "barrier area");
 static_assert(kOffY % 16 == 0, "staged operand alignment");
 
 // ---------------------------------------------------------------------------
@@ -172,6 +181,25 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
 #pragma unroll
   for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
 }
+// Columns c..c+7 of all 8 t-group accumulators (group t at column t * kN + c)
+// of this thread's TMEM lane: eight loads, one wait.  The outputs are
+// early-clobber: a load must not overwrite the address of a later one.
+__device__ __forceinline__ void tmem_ld_groups(uint32_t taddr, uint32_t (&r)[8][8]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%64];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%65];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16,%17,%18,%19,%20,%21,%22,%23}, [%66];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%24,%25,%26,%27,%28,%29,%30,%31}, [%67];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%32,%33,%34,%35,%36,%37,%38,%39}, [%68];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%40,%41,%42,%43,%44,%45,%46,%47}, [%69];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%48,%49,%50,%51,%52,%53,%54,%55}, [%70];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%56,%57,%58,%59,%60,%61,%62,%63}, [%71];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=&r"(r[0][0]), "=&r"(r[0][1]), "=&r"(r[0][2]), "=&r"(r[0][3]), "=&r"(r[0][4]), "=&r"(r[0][5]), "=&r"(r[0][6]), "=&r"(r[0][7]), "=&r"(r[1][0]), "=&r"(r[1][1]), "=&r"(r[1][2]), "=&r"(r[1][3]), "=&r"(r[1][4]), "=&r"(r[1][5]), "=&r"(r[1][6]), "=&r"(r[1][7]), "=&r"(r[2][0]), "=&r"(r[2][1]), "=&r"(r[2][2]), "=&r"(r[2][3]), "=&r"(r[2][4]), "=&r"(r[2][5]), "=&r"(r[2][6]), "=&r"(r[2][7]), "=&r"(r[3][0]), "=&r"(r[3][1]), "=&r"(r[3][2]), "=&r"(r[3][3]), "=&r"(r[3][4]), "=&r"(r[3][5]), "=&r"(r[3][6]), "=&r"(r[3][7]), "=&r"(r[4][0]), "=&r"(r[4][1]), "=&r"(r[4][2]), "=&r"(r[4][3]), "=&r"(r[4][4]), "=&r"(r[4][5]), "=&r"(r[4][6]), "=&r"(r[4][7]), "=&r"(r[5][0]), "=&r"(r[5][1]), "=&r"(r[5][2]), "=&r"(r[5][3]), "=&r"(r[5][4]), "=&r"(r[5][5]), "=&r"(r[5][6]), "=&r"(r[5][7]), "=&r"(r[6][0]), "=&r"(r[6][1]), "=&r"(r[6][2]), "=&r"(r[6][3]), "=&r"(r[6][4]), "=&r"(r[6][5]), "=&r"(r[6][6]), "=&r"(r[6][7]), "=&r"(r[7][0]), "=&r"(r[7][1]), "=&r"(r[7][2]), "=&r"(r[7][3]), "=&r"(r[7][4]), "=&r"(r[7][5]), "=&r"(r[7][6]), "=&r"(r[7][7])
+      : "r"(taddr), "r"(taddr + 1 * kN), "r"(taddr + 2 * kN), "r"(taddr + 3 * kN), "r"(taddr + 4 * kN),
+        "r"(taddr + 5 * kN), "r"(taddr + 6 * kN), "r"(taddr + 7 * kN)
+      : "memory");
+}
 
 // ---------------------------------------------------------------------------
 // Slicing
@@ -179,36 +207,43 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* v) {
 __device__ __forceinline__ int biased_exp(double x) {
   return (int)((__double_as_longlong(x) >> 52) & 0x7ff);
 }
-// F = x * 2^(1077 - E) rounded to the nearest integer (|F| <= 2^55 when x's
-// exponent <= E); subnormals and zeros give 0.  Rounding (not truncation)
-// keeps the representation error of elements below the row / column maximum
-// unbiased, so it does not accumulate coherently over successive updates.
+// F = x * 2^(1077 - E) rounded to the nearest integer, halves away from zero
+// (|F| < 2^55 when x's exponent e <= E); subnormals and zeros give 0.
+// Rounding (not truncation) keeps the representation error of elements below
+// the row / column maximum unbiased, so it does not accumulate coherently over
+// successive updates.
 __device__ __forceinline__ long long fixed_of(double x, int E) {
   const long long b = __double_as_longlong(x);
   const int e = (int)((b >> 52) & 0x7ff);
-  if (e == 0) return 0;
-  const long long m = (b & 0xFFFFFFFFFFFFFLL) | (1LL << 52);
-  const int sh = e - E + 2;
-  long long F;
-  if (sh >= 0)
-    F = m << sh;
-  else
-    F = (sh > -60) ? ((m + (1LL << (-sh - 1))) >> (-sh)) : 0;
-  return (b < 0) ? -F : F;
+  const int k = E - e;   // >= 0: E is the maximum exponent of the row / column
+  if (e == 0 || k > 56) return 0;
+  const unsigned long long t = ((unsigned long long)(b & 0xFFFFFFFFFFFFFLL) | (1ULL << 52)) << 2;
+  const unsigned long long F = (k == 0) ? t : (((t >> (k - 1)) + 1ULL) >> 1);
+  return (b < 0) ? -(long long)F : (long long)F;
 }
-// Digits d_0..d_6 of F (signed, round to nearest): F = sum d_p 2^(8 (6 - p)).
+// Balanced base-256 digits d_0..d_6 of F (|F| < 2^55): F = sum d_p 2^(8 (6 - p)),
+// d_1..d_6 in [-128, 127], d_0 in [-128, 128].  Taken from the bytes of F's
+// two's complement, least significant first, with a carry of one whenever a
+// byte (plus the incoming carry) is 128 or more.
 __device__ __forceinline__ void digits(long long F, int* d) {
+  const unsigned lo = (unsigned)F;
+  const int hi = (int)(F >> 32);
+  int c = 0;
 #pragma unroll
-  for (int p = 0; p < kS - 1; p++) {
-    const int u = kRho * (kS - 1 - p);
-    const long long dp = (F + (1LL << (u - 1))) >> u;
-    d[p] = (int)dp;
-    F -= dp << u;
+  for (int j = 0; j < kS - 1; j++) {
+    const unsigned u = (j < 4) ? ((lo >> (8 * j)) & 0xFFu) : (((unsigned)hi >> (8 * (j - 4))) & 0xFFu);
+    const int v = (int)u + c + 128;
+    d[kS - 1 - j] = (v & 255) - 128;
+    c = v >> 8;
   }
-  d[kS - 1] = (int)F;
+  d[0] = (hi >> 16) + c;   // bits 48..63 of F, sign-extended, plus the carry
 }
-__device__ __forceinline__ uint32_t bf16_bits(int d) {
-  return __float_as_uint((float)d) >> 16;    // exact: |d| <= 128 has <= 8 significant bits
+__device__ __forceinline__ uint32_t f32_bits(int d) {
+  return __float_as_uint((float)d);   // exact: |d| <= 128 has <= 8 significant bits
+}
+// Two BF16 digits in one word: the upper halves of their (exact) FP32 images.
+__device__ __forceinline__ uint32_t bf16x2(int d0, int d1) {
+  return __byte_perm(f32_bits(d0), f32_bits(d1), 0x7632);
 }
 // Byte offset of element (row, kk) (kk < 16) inside one K-major slice block:
 // core matrices [row/8][kk/8][8][16 bytes].
@@ -220,14 +255,14 @@ __device__ __forceinline__ int core_off(int row, int kk) {
 // Per-CTA state of the engine (shared memory + TMEM)
 // ---------------------------------------------------------------------------
 struct Ctx {
-  uint8_t* sA;          // 2 stages x kAChunkBytes
-  uint8_t* sB;          // 2 stages x kBChunkBytes
-  uint64_t* bar;        // [0,1] A full, [2,3] MMA done
+  uint8_t* sA;          // kAStages x kAChunkBytes
+  uint8_t* sB;          // kBStages x kBChunkBytes
+  uint64_t* bar;        // kNumBars mbarriers (kBarAFull, kBarBFull, kBarDone)
   int* sEb;             // 2 x kN column exponents of the right operand
   double* sY;           // the right operand: kK x kN doubles, ld kLdY
   uint32_t tmem;        // base of the 512 TMEM columns
-  uint32_t phase_a[2];  // phase parity per stage (kept identical in every thread)
-  uint32_t phase_m[2];
+  int n;                // K chunks consumed so far in this task (same in every thread)
+  int na;               // K chunks whose A copy has been issued (thread 0 only)
   int yb;               // which half of sEb describes sY
   unsigned* err;        // scheduler error word
 };
@@ -240,14 +275,13 @@ __device__ __forceinline__ void ctx_init(Ctx& c, uint8_t* base, uint32_t tmem, u
   c.sY = reinterpret_cast<double*>(base + kOffY);
   c.tmem = tmem;
   c.err = err;
+  c.n = 0;
+  c.na = 0;
   c.yb = 0;
   if (threadIdx.x == 0) {
-    for (int i = 0; i < 4; i++) mbar_init(c.bar + i, 1);
+    for (int i = 0; i < kNumBars; i++)
+      mbar_init(c.bar + i, (i >= kBarBFull && i < kBarDone) ? kSlicerWarps : 1);
     mbar_fence_init();
-  }
-  for (int i = 0; i < 2; i++) {
-    c.phase_a[i] = 0;
-    c.phase_m[i] = 0;
   }
   __syncthreads();
 }
@@ -256,7 +290,7 @@ __device__ __forceinline__ void ctx_init(Ctx& c, uint8_t* base, uint32_t tmem, u
 __device__ __forceinline__ void ctx_release(Ctx& c) {
   __syncthreads();
   if (threadIdx.x == 0)
-    for (int i = 0; i < 4; i++)
+    for (int i = 0; i < kNumBars; i++)
       asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(c.bar + i)) : "memory");
   __syncthreads();
 }
@@ -268,13 +302,15 @@ __device__ __forceinline__ void set_err(const Ctx& c) {
 // Column exponents (max biased exponent) of the staged right operand into
 // sEb[c.yb].
 __device__ __forceinline__ void y_exponents(Ctx& c) {
-  const int col = threadIdx.x >> 2, part = threadIdx.x & 3;   // 4 threads per column
+  constexpr int kTPC = kThreads / kN;   // threads per column
+  static_assert(kTPC >= 1 && kTPC <= 32 && (kTPC & (kTPC - 1)) == 0, "column split");
+  const int col = threadIdx.x / kTPC, part = threadIdx.x % kTPC;
   int e = 0;
   const double* y = c.sY + col * kLdY;
-#pragma unroll 8
-  for (int r = part; r < kK; r += 4) e = max(e, biased_exp(y[r]));
-  e = max(e, __shfl_xor_sync(0xffffffffu, e, 1));
-  e = max(e, __shfl_xor_sync(0xffffffffu, e, 2));
+#pragma unroll 4
+  for (int r = part; r < kK; r += kTPC) e = max(e, biased_exp(y[r]));
+#pragma unroll
+  for (int o = 1; o < kTPC; o <<= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
   if (part == 0) c.sEb[c.yb * kN + col] = e;
   __syncthreads();
 }
@@ -284,7 +320,7 @@ __device__ __forceinline__ void y_exponents(Ctx& c) {
 // unit_col of a unit-lower V (zero above the diagonal, one on it).
 __device__ __forceinline__ void stage_y(Ctx& c, const double* Y, int ldy, int unit_col) {
   static_assert(kK * kN / 2 % kThreads == 0, "staging loop");
-  constexpr int kIter = kK * kN / 2 / kThreads;   // 16 pairs per thread
+  constexpr int kIter = kK * kN / 2 / kThreads;   // pairs per thread
 #pragma unroll 4
   for (int it = 0; it < kIter; it++) {
     const int e = threadIdx.x + it * kThreads;
@@ -302,49 +338,74 @@ __device__ __forceinline__ void stage_y(Ctx& c, const double* Y, int ldy, int un
   y_exponents(c);
 }
 
-// Slice rows [k0, k0+16) of the staged right operand into B stage `s`.
-__device__ __forceinline__ void slice_b_chunk(Ctx& c, int s, int k0) {
-  const int col = threadIdx.x >> 2, q = threadIdx.x & 3;   // 64 columns x 4 quads of 4 rows
+// Slice quad g (column g / 4 of 64, rows k0 + 4 (g % 4) .. +3) of the staged
+// right operand into B stage `s`.
+__device__ __forceinline__ void slice_b_quad(Ctx& c, uint8_t* stage, int g, int k0) {
+  const int col = g >> 2, q = g & 3;
   const int E = c.sEb[c.yb * kN + col];
   const double* y = c.sY + col * kLdY + k0 + 4 * q;
   int d[4][kS];
 #pragma unroll
   for (int i = 0; i < 4; i++) digits(fixed_of(y[i], E), d[i]);
-  uint8_t* stage = c.sB + s * kBChunkBytes;
   const int off = core_off(col, 4 * q);
 #pragma unroll
   for (int p = 0; p < kS; p++) {
     uint2 w;
-    w.x = bf16_bits(d[0][p]) | (bf16_bits(d[1][p]) << 16);
-    w.y = bf16_bits(d[2][p]) | (bf16_bits(d[3][p]) << 16);
+    w.x = bf16x2(d[0][p], d[1][p]);
+    w.y = bf16x2(d[2][p], d[3][p]);
     *reinterpret_cast<uint2*>(stage + p * kSliceBBytes + off) = w;
   }
 }
 
-// The 8 t-group accumulators of X (prepared slices) times the staged right
-// operand.  On return (true) the accumulators are final in TMEM.
-inline __device__ bool gemm(Ctx& c, const uint8_t* Xprep) {
-  const uint32_t id = idesc_bf16(kM, kN);
-  const uint64_t dA0 = sdesc(smem_u32(c.sA), 128, 256);
-  const uint64_t dB0 = sdesc(smem_u32(c.sB), 128, 256);
-  bool ok = true;
-  // prologue: stage 0 <- chunk 0
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+// Wait for the completion of task chunk n on barrier array `base` of `stages`.
+__device__ __forceinline__ bool wait_chunk(const Ctx& c, int base, int stages, int n) {
+  return mbar_wait(c.bar + base + n % stages, (uint32_t)((n / stages) & 1), c.err);
+}
+__device__ __forceinline__ void issue_a(Ctx& c, const uint8_t* X, int chunk, int n) {
+  uint64_t* b = c.bar + kBarAFull + n % kAStages;
+  mbar_expect_tx(b, kAChunkBytes);
+  tma_load_1d(c.sA + (n % kAStages) * kAChunkBytes, X + (size_t)chunk * kAChunkBytes, kAChunkBytes, b);
+}
+
+// Issue the bulk copies of the first chunks of the next product's left
+// operand X (thread 0), e.g. before the right operand is staged.
+__device__ __forceinline__ void prefetch(Ctx& c, const uint8_t* X) {
   if (threadIdx.x == 0) {
     fence_proxy_async_global();
-    mbar_expect_tx(c.bar + 0, kAChunkBytes);
-    tma_load_1d(c.sA, Xprep, kAChunkBytes, c.bar + 0);
+    for (; c.na < c.n + kAStages; c.na++) issue_a(c, X, c.na - c.n, c.na);
   }
-  slice_b_chunk(c, 0, 0);
-  for (int kc = 0; kc < kChunks; kc++) {
-    const int s = kc & 1;
-    fence_proxy_async();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      if (!mbar_wait(c.bar + s, c.phase_a[s], c.err)) ok = false;
-      tc_fence_after();
-      if (ok) {
-        const uint64_t dA = dA0 + (uint64_t)((s * kAChunkBytes) >> 4);
-        const uint64_t dB = dB0 + (uint64_t)((s * kBChunkBytes) >> 4);
+}
+
+// The 8 t-group accumulators of X (prepared slices) times the staged right
+// operand; Xnext (or nullptr): the left operand of the next product, whose
+// first chunks are fetched as soon as their stages are free.  Warp 0, one
+// thread: bulk copies of A and the MMAs; warps 1..7: slicing of B, up to
+// kBStages chunks ahead of the MMAs.  On return (true) the accumulators are
+// final in TMEM.
+inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
+  const int n0 = c.n;
+  bool ok = true;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) {
+    if (lane == 0) {
+      const uint32_t id = idesc_bf16(kM, kN);
+      const uint64_t dA0 = sdesc(smem_u32(c.sA), 128, 256);
+      const uint64_t dB0 = sdesc(smem_u32(c.sB), 128, 256);
+      fence_proxy_async_global();
+      // chunks of this product not prefetched yet (stages free: every earlier MMA is done)
+      for (; c.na < n0 + kAStages; c.na++) issue_a(c, X, c.na - n0, c.na);
+      for (int j = 0; j < kChunks && ok; j++) {
+        const int n = n0 + j;
+        if (!wait_chunk(c, kBarAFull, kAStages, n) || !wait_chunk(c, kBarBFull, kBStages, n)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint64_t dA = dA0 + (uint64_t)(((n % kAStages) * kAChunkBytes) >> 4);
+        const uint64_t dB = dB0 + (uint64_t)(((n % kBStages) * kBChunkBytes) >> 4);
         // pairs (p, q) with p + q <= kGroups - 1 into t-group p + q; the first
         // product into each group in chunk 0 overwrites it
 #pragma unroll
@@ -352,36 +413,57 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* Xprep) {
 #pragma unroll
           for (int q = 0; q < kS && p + q < kGroups; q++) {
             const int first_p = (p + q) - (kS - 1) > 0 ? (p + q) - (kS - 1) : 0;
-            const uint32_t acc = (kc > 0 || p > first_p) ? 1u : 0u;
+            const uint32_t acc = (j > 0 || p > first_p) ? 1u : 0u;
             mma_bf16(c.tmem + (uint32_t)((p + q) * kN), dA + (uint64_t)((p * kSliceABytes) >> 4),
                      dB + (uint64_t)((q * kSliceBBytes) >> 4), id, acc);
           }
         }
+        mma_commit(c.bar + kBarDone + n % kBStages);
+        // refill the A stage of chunk n - 1 with chunk n + 2 once its MMAs are done
+        if (j >= 1 && j + 2 < kChunks) {
+          if (!wait_chunk(c, kBarDone, kBStages, n - 1)) {
+            ok = false;
+            break;
+          }
+          issue_a(c, X, j + 2, n + 2);
+          c.na = n + 3;
+        }
       }
-      mma_commit(c.bar + 2 + s);
+      // prefetch the next product's first chunks into the stages of the last three
+      if (ok && Xnext) {
+        for (int j = 0; j < kAStages; j++) {
+          if (!wait_chunk(c, kBarDone, kBStages, n0 + kChunks - kAStages + j)) {
+            ok = false;
+            break;
+          }
+          issue_a(c, Xnext, j, n0 + kChunks + j);
+        }
+        if (ok) c.na = n0 + kChunks + kAStages;
+      }
     }
-    c.phase_a[s] ^= 1;
-    if (kc + 1 < kChunks) {
-      const int s1 = s ^ 1;
-      if (kc >= 1) {   // stage s1 still feeds the MMAs of chunk kc-1
-        if (!mbar_wait(c.bar + 2 + s1, c.phase_m[s1], c.err)) ok = false;
-        c.phase_m[s1] ^= 1;
+    __syncwarp();
+  } else {
+    // slicer thread ts owns quads ts, ts + 224, ... of the product's 8 x 256
+    const int ts = threadIdx.x - 32;
+    constexpr int kStride = kSlicerWarps * 32;
+    int g = ts;
+    for (int j = 0; j < kChunks && ok; j++) {
+      const int n = n0 + j;
+      if (n >= kBStages && !wait_chunk(c, kBarDone, kBStages, n - kBStages)) {
+        ok = false;
+        break;
       }
-      if (threadIdx.x == 0) {
-        mbar_expect_tx(c.bar + s1, kAChunkBytes);
-        tma_load_1d(c.sA + s1 * kAChunkBytes, Xprep + (size_t)(kc + 1) * kAChunkBytes, kAChunkBytes,
-                    c.bar + s1);
-      }
-      slice_b_chunk(c, s1, (kc + 1) * kKC);
+      uint8_t* stage = c.sB + (n % kBStages) * kBChunkBytes;
+      for (; g < (j + 1) * 256; g += kStride) slice_b_quad(c, stage, g & 255, j * kKC);
+      fence_proxy_async();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(c.bar + kBarBFull + n % kBStages);
     }
   }
-  // the two outstanding commits
-  for (int k = kChunks - 2; k < kChunks; k++) {
-    const int s = k & 1;
-    if (!mbar_wait(c.bar + 2 + s, c.phase_m[s], c.err)) ok = false;
-    c.phase_m[s] ^= 1;
-  }
+  // every thread: the last chunk's MMAs (and with them all earlier ones) are done
+  if (ok && !wait_chunk(c, kBarDone, kBStages, n0 + kChunks - 1)) ok = false;
   tc_fence_after();
+  c.n = n0 + kChunks;
   ok = __syncthreads_and(ok) != 0;   // uniform across the CTA
   if (!ok && threadIdx.x == 0) set_err(c);
   return ok;
@@ -423,13 +505,15 @@ enum Epi : int {
 };
 
 // Recombine the 8 t-group accumulators into FP64 and apply the epilogue.
-// Warp w handles rows 32*(w%4).., columns 32*(w/4)..+31.  Ea: row exponents
-// of X (global).
+// Warp w handles TMEM lanes (rows) 32*(w%4).. and kColsPerWarp columns from
+// kColsPerWarp*(w/4).  Ea: row exponents of X (global).
 inline __device__ void drain(Ctx& c, const int* Ea, int mode, double* g, int ldg, double* gm,
                              int ldm) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  constexpr int kColsPerWarp = kN / (kWarps / 4);
+  static_assert(kColsPerWarp % kDC == 0, "epilogue passes");
   const int row = 32 * (w & 3) + lane;
-  const int cb = 32 * (w >> 2);
+  const int cb = kColsPerWarp * (w >> 2);
   const int ea = __ldcg(Ea + row);
   const uint32_t lane_addr = c.tmem + ((uint32_t)(32 * (w & 3)) << 16);
   const bool to_y = (mode == kEpiToY || mode == kEpiToYSubTop);
@@ -442,7 +526,7 @@ inline __device__ void drain(Ctx& c, const int* Ea, int mode, double* g, int ldg
   const double* msrc = (mode == kEpiSubInto) ? g : (mode == kEpiStore) ? nullptr : gm;
   const int mld = (mode == kEpiSubInto) ? ldg : ldm;
 #pragma unroll 1
-  for (int pass = 0; pass < 32 / kDC; pass++) {
+  for (int pass = 0; pass < kColsPerWarp / kDC; pass++) {
     const int c0 = cb + kDC * pass;
     // issue the memory loads before the TMEM reads so they overlap
     double mem[kDC];
@@ -451,13 +535,13 @@ inline __device__ void drain(Ctx& c, const int* Ea, int mode, double* g, int ldg
     long long hi[kDC], lo[kDC];
 #pragma unroll
     for (int i = 0; i < kDC; i++) hi[i] = lo[i] = 0;
+    uint32_t acc[kGroups][kDC];
+    tmem_ld_groups(lane_addr + (uint32_t)c0, acc);
 #pragma unroll
     for (int t = 0; t < kGroups; t++) {
-      float v[kDC];
-      tmem_ld8(lane_addr + (uint32_t)(t * kN + c0), v);
 #pragma unroll
       for (int i = 0; i < kDC; i++) {
-        const long long q = (long long)__float2int_rn(v[i]);
+        const long long q = (long long)__float2int_rn(__uint_as_float(acc[t][i]));
         if (t < 4)
           hi[i] = (hi[i] << kRho) + q;
         else
@@ -495,10 +579,11 @@ inline __device__ void drain(Ctx& c, const int* Ea, int mode, double* g, int ldg
   if (to_y) c.yb = nb;
 }
 
-// One product: X (prepared, row exponents Ea) times the staged right operand.
-inline __device__ bool product(Ctx& c, const uint8_t* Xprep, const int* Ea, int mode, double* g,
-                               int ldg, double* gm, int ldm) {
-  if (!gemm(c, Xprep)) return false;
+// One product: X (prepared, row exponents Ea) times the staged right operand;
+// Xnext: the next product's left operand (prefetched) or nullptr.
+inline __device__ bool product(Ctx& c, const uint8_t* Xprep, const uint8_t* Xnext, const int* Ea,
+                               int mode, double* g, int ldg, double* gm, int ldm) {
+  if (!gemm(c, Xprep, Xnext)) return false;
   drain(c, Ea, mode, g, ldg, gm, ldm);
   return true;
 }
@@ -540,8 +625,8 @@ inline __device__ void slice_left(const Acc& acc, uint8_t* dst, int* Ea, int* sE
 #pragma unroll
     for (int p = 0; p < kS; p++) {
       uint2 w;
-      w.x = bf16_bits(d[0][p]) | (bf16_bits(d[1][p]) << 16);
-      w.y = bf16_bits(d[2][p]) | (bf16_bits(d[3][p]) << 16);
+      w.x = bf16x2(d[0][p], d[1][p]);
+      w.y = bf16x2(d[2][p], d[3][p]);
       *reinterpret_cast<uint2*>(blk + p * kSliceABytes + off) = w;
     }
   }
@@ -565,7 +650,7 @@ struct StagedAcc {
 
 // Stage a 128 x 128 column-major tile (global, ld kK) in shared memory, ld kLdY.
 __device__ __forceinline__ void stage_tile(double* s, const double* src) {
-  constexpr int kIter = kK * kK / 2 / kThreads;   // 32 pairs per thread
+  constexpr int kIter = kK * kK / 2 / kThreads;   // pairs per thread
 #pragma unroll 4
   for (int it = 0; it < kIter; it++) {
     const int e = threadIdx.x + it * kThreads;

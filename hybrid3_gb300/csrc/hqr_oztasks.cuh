@@ -29,15 +29,18 @@ struct PackedTTAcc {
 // T recurrence (dlarft 'F','C', k = NB = 128) in shared memory:
 //   T(c, c) = tau_c;  T(0:c, c) = -tau_c T(0:c, 0:c) G(0:c, c)  (zero when tau_c = 0)
 // sG: strictly upper part of G = V^T V, packed: G(b, c) (b < c) at c (c - 1) / 2 + b.
-// sT: the result, packed upper (see PackedTTAcc).  Two threads per row.
+// sT: the result, packed upper (see PackedTTAcc).  kTPR adjacent threads per
+// row split the sum over b.
 inline __device__ void t_recurrence(const double* sG, double* sT, const double* tau) {
-  const int a = threadIdx.x >> 1, h = threadIdx.x & 1;
+  constexpr int kTPR = kThreads / oz::kK;
+  static_assert(kTPR >= 1 && kTPR <= 32 && (kTPR & (kTPR - 1)) == 0, "row split");
+  const int a = threadIdx.x / kTPR, h = threadIdx.x % kTPR;
   for (int c = 0; c < oz::kK; c++) {
     const double tc = __ldcg(tau + c);
     double s0 = 0.0, s1 = 0.0;
     if (a < c) {
-      const int mid = a + (c - a + 1) / 2;
-      const int b0 = h ? mid : a, b1 = h ? c : mid;
+      const int len = c - a;
+      const int b0 = a + (len * h) / kTPR, b1 = a + (len * (h + 1)) / kTPR;
       const double* g = sG + c * (c - 1) / 2;
       int b = b0;
       for (; b + 1 < b1; b += 2) {
@@ -47,7 +50,8 @@ inline __device__ void t_recurrence(const double* sG, double* sT, const double* 
       if (b < b1) s0 = fma(sT[b * (b + 1) / 2 + a], g[b], s0);
     }
     double s = s0 + s1;
-    s += __shfl_xor_sync(0xffffffffu, s, 1);
+#pragma unroll
+    for (int o = 1; o < kTPR; o <<= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if (h == 0 && a <= c) sT[c * (c + 1) / 2 + a] = (a == c) ? tc : (tc == 0.0 ? 0.0 : -tc * s);
     __syncthreads();
   }
@@ -77,9 +81,10 @@ inline __device__ bool task_ozprep(const double* V, const double* tau, double* G
     Ctx c;
     ctx_init(c, sm, tmem, err);
     for (int cb = 0; cb < kK / kN; cb++) {
+      prefetch(c, slices + kOzVT * ob);
       stage_y(c, V + (size_t)cb * kN * kK, kK, unit ? cb * kN : -1);
-      if (!product(c, slices + kOzVT * ob, exps + kOzVT * kK, kEpiStore, G + (size_t)cb * kN * kK, kK,
-                   nullptr, 0))
+      if (!product(c, slices + kOzVT * ob, (cb + 1 < kK / kN) ? slices + kOzVT * ob : nullptr,
+                   exps + kOzVT * kK, kEpiStore, G + (size_t)cb * kN * kK, kK, nullptr, 0))
         return false;
     }
     ctx_release(c);
@@ -112,11 +117,16 @@ inline __device__ bool task_ozapply(oz::Ctx& c, const uint8_t* slices, const int
                                     double* Cbot) {
   using namespace oz;
   constexpr size_t ob = operand_bytes();
+  prefetch(c, slices + kOzVT * ob);
   stage_y(c, Cbot, kK, -1);
-  if (!product(c, slices + kOzVT * ob, exps + kOzVT * kK, kEpiToY, nullptr, 0, Ctop, kK)) return false;
-  if (!product(c, slices + kOzTT * ob, exps + kOzTT * kK, kEpiToYSubTop, nullptr, 0, Ctop, kK))
+  if (!product(c, slices + kOzVT * ob, slices + kOzTT * ob, exps + kOzVT * kK, kEpiToY, nullptr, 0, Ctop,
+               kK))
     return false;
-  if (!product(c, slices + kOzV * ob, exps + kOzV * kK, kEpiSubInto, Cbot, kK, nullptr, 0)) return false;
+  if (!product(c, slices + kOzTT * ob, slices + kOzV * ob, exps + kOzTT * kK, kEpiToYSubTop, nullptr, 0,
+               Ctop, kK))
+    return false;
+  if (!product(c, slices + kOzV * ob, nullptr, exps + kOzV * kK, kEpiSubInto, Cbot, kK, nullptr, 0))
+    return false;
   ctx_release(c);
   return true;
 }

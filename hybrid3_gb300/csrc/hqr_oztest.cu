@@ -23,8 +23,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozaki_product(const double* X, 
   }
   oz::Ctx c;
   oz::ctx_init(c, sm, s_tmem, err);
+  oz::prefetch(c, prep);
   oz::stage_y(c, Y, oz::kK, -1);
-  if (oz::product(c, prep, exps, oz::kEpiStore, C, oz::kK, nullptr, 0)) oz::ctx_release(c);
+  if (oz::product(c, prep, nullptr, exps, oz::kEpiStore, C, oz::kK, nullptr, 0)) oz::ctx_release(c);
   oz::tc_fence_before();
   __syncthreads();
   oz::tc_fence_after();

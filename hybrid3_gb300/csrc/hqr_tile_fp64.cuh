@@ -24,6 +24,10 @@ namespace hqr {
 
 constexpr int kMaxW = 32;      // inner block width
 constexpr int kRC = 128;       // V row chunk staged per pass
+constexpr int kRedSlots = 32;  // block-reduction scratch: kWarps partials, then 4 broadcasts
+constexpr int kBcast = kWarps; // first broadcast slot
+constexpr int kSplitItems = 256;   // at most this many (output, split) items in W = V^T C
+static_assert(kWarps + 4 <= kRedSlots, "reduction scratch");
 
 // Shape of the tile kernels for one (NB, IB) configuration.
 struct TileShape {
@@ -56,8 +60,8 @@ struct SmemPlan {
     p.off_g = o; o += w * w;               // Gram scratch of the T-block build
     p.off_w = o; o += w * CB;
     p.off_w2 = o; o += w * CB;
-    p.off_part = o; o += 2048;             // split-K partials (<= 256 items x 8)
-    p.off_red = o; o += 16;                // block reductions / broadcasts
+    p.off_part = o; o += 8 * kSplitItems;  // split-K partials (<= kSplitItems items x 8)
+    p.off_red = o; o += kRedSlots;         // block reductions (kWarps) + broadcasts (4)
     p.off_tau = o; o += kMaxW;
     p.total = o;
     return p;
@@ -125,14 +129,14 @@ __device__ void block_larfg(double* alpha, double* x, int n, double* tau_out, do
       scal = 1.0 / (a - beta);
       for (int j = 0; j < knt; j++) beta *= safmin;
     }
-    red[8] = tau;
-    red[9] = scal;
-    red[10] = (double)knt;
-    red[11] = beta;
+    red[kBcast + 0] = tau;
+    red[kBcast + 1] = scal;
+    red[kBcast + 2] = (double)knt;
+    red[kBcast + 3] = beta;
   }
   __syncthreads();
-  const double tau = red[8], scal = red[9];
-  const int knt = (int)red[10];
+  const double tau = red[kBcast + 0], scal = red[kBcast + 1];
+  const int knt = (int)red[kBcast + 2];
   if (tau != 0.0) {
     const double rsafmn = 1.0 / (DBL_MIN / (DBL_EPSILON * 0.5));
     for (int r = threadIdx.x; r < n; r += kThreads) {
@@ -142,7 +146,7 @@ __device__ void block_larfg(double* alpha, double* x, int n, double* tau_out, do
     }
   }
   if (threadIdx.x == 0) {
-    *alpha = red[11];
+    *alpha = red[kBcast + 3];
     *tau_out = tau;
   }
   __syncthreads();
@@ -266,7 +270,7 @@ __device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off
   // ---- W = Vt^T Ct + Vb^T Cb -------------------------------------------
   const int G8 = ncol >> 3;
   const int outs = w * G8;                       // items per split
-  int S = kThreads / (outs > 0 ? outs : 1);
+  int S = kSplitItems / (outs > 0 ? outs : 1);
   if (S < 1) S = 1;
   const int item = tid;
   const int a = item % w;
