@@ -75,6 +75,8 @@ SIGNATURES = {
     "mat_make": (None, [_ST, _dp, _U, _I]),
     "mat_remv": (None, [_ST, _dp, _U, _I]),
     "mat_dprint": (None, [_ST, _dp, _dp]),
+    "mat_print": (None, [_ST, _vp, _dp, ctypes.c_char_p]),
+    "mat_print_tile": (None, [_vp, _dp, ctypes.c_char_p, _I, _I]),
     # include/TileSch.h
     "TilSch_init": (None, [ctypes.POINTER(TilSchList), _L]),
     "TilSch_pop": (_I, [ctypes.POINTER(TilSchList), ctypes.POINTER(TilSch)]),
@@ -83,6 +85,7 @@ SIGNATURES = {
     "TilSch_fully": (_I, [ctypes.POINTER(TilSchList)]),
     "TilSch_depend": (_I, [ctypes.POINTER(TilSchList), TilSch, _U]),
     "TilSch_delete": (_I, [ctypes.POINTER(TilSchList), TilSch]),
+    "TilSch_end": (None, [ctypes.POINTER(TilSchList)]),
     # include/hqr_gpu.h
     "hqr_status_string": (ctypes.c_char_p, [_I]),
     "hqr_set_error_mode": (None, [_I]),
@@ -111,6 +114,23 @@ SIGNATURES = {
     "hqr_zero_reflectors": (_I, [_L, _L, _I, _vp, _vp]),
     "hqr_fp64_peak_tflops": (_D, [_vp]),
     "hqr_ozaki_product": (_I, [_I, _vp, _vp, _vp, _vp]),
+    # include/tile_kernel.h (pointer arguments: host or device addresses)
+    "tile_init": (_vp, [ctypes.c_char, _I, _I]),
+    "tile_dgeqrt": (None, [_I, _I, _I, _vp, _I, _vp, _vp, _vp, _I, _vp]),
+    "tile_dtsqrt": (None, [_I, _I, _I, _vp, _I, _vp, _I, _vp, _vp, _I, _vp]),
+    "tile_dlarfb": (None, [_I, _I, _vp, _I, _vp, _vp, _I, _vp]),
+    "tile_dssrfb": (None, [_I, _I, _vp, _vp, _I, _vp, _vp, _I, _vp]),
+    "tile_sub_dgeqr2": (None, [_I, _I, _vp, _I, _vp, _vp, _vp]),
+    "tile_sub_dlarft": (None, [_I, _I, _vp, _I, _vp, _vp, _I, _vp]),
+    "tile_sub_dlarfb": (None, [_I, _I, _I, _vp, _I, _vp, _I, _vp, _I, _vp]),
+    "tile_sub_dssrfb": (None, [_I, _I, _I, _I, _vp, _I, _vp, _I, _vp, _I, _vp, _I, _vp]),
+    "tile_dlarft": (None, [_I, _I, _I, _vp, _I, _vp, _vp, _I, _vp]),
+    "tile_dssrfb_head": (None, [_I, _I, _vp, _vp, _I, _vp, _vp, _I, _vp]),
+    "tile_dssrfb_tail": (None, [_I, _I, _vp, _I, _vp, _vp]),
+    "tile_return_dlarfb": (None, [_I, _I, _vp, _I, _vp, _vp, _I, _vp]),
+    "tile_return_dssrfb": (None, [_I, _I, _vp, _vp, _I, _vp, _vp, _I, _vp]),
+    "tile_return_dlarft": (None, [_I, _I, _vp, _I, _vp, _vp, _I, _vp]),
+    "tile_sub_dtsqr2": (None, [_I, _I, _vp, _I, _vp, _I, _vp, _vp]),
 }
 
 _lib = None

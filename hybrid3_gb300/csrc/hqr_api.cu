@@ -118,6 +118,8 @@ int d2h(double* h, const double* d, size_t n, cudaStream_t s) {
 
 }  // namespace
 
+int hqr::report_error(const char* fn, int rc) { return report(fn, rc); }
+
 int hqr::record_cuda_error(cudaError_t e, const char* where) {
   snprintf(g_cuda_msg, sizeof(g_cuda_msg), "%s: %s (%d)", where, cudaGetErrorString(e), (int)e);
   return HQR_ERR_CUDA;

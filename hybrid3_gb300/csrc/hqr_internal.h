@@ -24,6 +24,9 @@ int make_geometry(long M, long N, int NB, int IB, Geometry* g);
 // Remember the text of a failed CUDA call (reported by hqr_last_cuda_error)
 // and return HQR_ERR_CUDA.
 int record_cuda_error(cudaError_t e, const char* where);
+// Report a drop-in entry point's status the way the error mode says (print
+// and exit, or print and remember for hqr_last_error); returns rc.
+int report_error(const char* fn, int rc);
 
 // Scheduler workspace (dependency counters, queues, control words, stats).
 struct DagWorkspace {
