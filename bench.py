@@ -197,9 +197,43 @@ def split_products(NB: int) -> int:
     return 34 if NB <= 128 else 36
 
 
+def graded_tiles(H, torch, L, n: int, NBs, kappa: float, seed: int):
+    """A = U diag(sigma) V^T in the tile layouts of each NB in NBs, on the
+    device: U, V Haar (QR of Gaussians with columns signed by diag(R),
+    Mezzadri 2007), sigma_i = kappa^(-i/(n-1)).  Input generation only
+    (torch, outside the timed path)."""
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+
+    def haar():
+        Z = torch.randn(n, n, dtype=torch.float64, device="cuda", generator=gen)
+        Q, R = torch.linalg.qr(Z)
+        Q *= torch.sign(torch.diagonal(R))
+        del Z, R
+        return Q
+
+    U = haar()
+    U *= kappa ** (-torch.arange(n, dtype=torch.float64, device="cuda") / (n - 1))
+    V = haar()
+    A = U @ V.T
+    del U, V
+    cm = A.T.contiguous()          # column-major storage of A
+    del A
+    out = {}
+    for NB in NBs:
+        tiles = torch.empty(n * n, dtype=torch.float64, device="cuda")
+        H.check(L.hqr_colmajor_to_tiles(n, n, NB, cm.data_ptr(), tiles.data_ptr(), None), "to tiles")
+        out[NB] = tiles
+    torch.cuda.synchronize()
+    del cm
+    torch.cuda.empty_cache()
+    return out
+
+
 def measure(H, torch, L, args, precision: str, n: int, NB: int, IB: int, steps: int, warmup: int,
-            dist, world: int, clocks_too: bool, check: bool):
-    """Time `steps` device-resident steps (factorization + make_Q)."""
+            dist, world: int, clocks_too: bool, check: bool, init=None):
+    """Time `steps` device-resident steps (factorization + make_Q).  init: the
+    input in tile layout (device), else the seeded uniform matrix."""
     M = N = n
     ntau = (M // NB) * (N // NB) * NB
     prec = H.HQR_PREC_OZAKI if precision == "split" else H.HQR_PREC_FP64
@@ -210,7 +244,10 @@ def measure(H, torch, L, args, precision: str, n: int, NB: int, IB: int, steps: 
     dA = torch.empty_like(dA0)
     dQ = torch.empty_like(dA0)
     dTAU = torch.zeros(ntau, dtype=f64, device="cuda")
-    H.check(L.hqr_fill_uniform(M, N, NB, 20151130, dA0.data_ptr(), s), "fill")
+    if init is None:
+        H.check(L.hqr_fill_uniform(M, N, NB, 20151130, dA0.data_ptr(), s), "fill")
+    else:
+        dA0.copy_(init)
     plan = H.Plan(M, N, NB, IB, prec)
     ev = lambda: torch.cuda.Event(enable_timing=True)
 
@@ -348,6 +385,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--kappa", type=float, default=None,
+                    help="graded input A = U diag(sigma) V^T with condition number kappa "
+                         "(accuracy configuration); default: uniform[-1,1)")
     args = ap.parse_args()
     if args.nb is None:
         args.nb = 128 if args.precision == "split" else 256
@@ -375,14 +415,21 @@ def main():
     n, NB, IB = args.n, args.nb, args.ib
 
     peak_fp64 = L.hqr_fp64_peak_tflops(None)
+    init = init64 = None
+    if args.kappa is not None:
+        compare_too = args.precision == "split" and not args.no_compare
+        t = graded_tiles(H, torch, L, n, sorted({NB, args.fp64_nb} if compare_too else {NB}),
+                         args.kappa, 1000 + rank)
+        init = t[NB]
+        init64 = t.get(args.fp64_nb)
     main_run = measure(H, torch, L, args, args.precision, n, NB, IB, args.steps, args.warmup, dist,
-                       world, True, not args.no_check)
+                       world, True, not args.no_check, init)
     value = main_run["flops"] / main_run["elapsed"] / 1e12
 
     compare = None
     if args.precision == "split" and not args.no_compare:
         fp = measure(H, torch, L, args, "fp64", n, args.fp64_nb, IB, 1, 1, dist, world, False,
-                     not args.no_check)
+                     not args.no_check, init64)
         fv = fp["flops"] / fp["elapsed"] / 1e12
         compare = {"value": round(fv, 6), "unit": "TFLOP/s", "NB": args.fp64_nb, "IB": IB,
                    "steps": 1, "warmup": 1, "ms_per_step": round(1e3 * fp["elapsed"], 3),
@@ -431,8 +478,9 @@ def main():
         "ms_per_step": round(1e3 * main_run["elapsed"] / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"tiled QR + Q generation (make_Q), n={n} square, NB={NB}, IB={IB}, "
-                               "uniform[-1,1) seed 20151130",
+        "config": {"workload": f"tiled QR + Q generation (make_Q), n={n} square, NB={NB}, IB={IB}, " +
+                               ("uniform[-1,1) seed 20151130" if args.kappa is None else
+                                f"graded A = U diag(sigma) V^T, U, V Haar, kappa={args.kappa:g}"),
                    "n": n, "NB": NB, "IB": IB,
                    "precision": ("split (Ozaki BF16 slices on tcgen05, FP64 panels)"
                                  if args.precision == "split" else "fp64 (plain)"),

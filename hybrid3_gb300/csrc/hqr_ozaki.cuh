@@ -221,29 +221,25 @@ __device__ __forceinline__ long long fixed_of(double x, int E) {
   const unsigned long long F = (k == 0) ? t : (((t >> (k - 1)) + 1ULL) >> 1);
   return (b < 0) ? -(long long)F : (long long)F;
 }
-// Balanced base-256 digits d_0..d_6 of F (|F| < 2^55): F = sum d_p 2^(8 (6 - p)),
-// d_1..d_6 in [-128, 127], d_0 in [-128, 128].  Taken from the bytes of F's
-// two's complement, least significant first, with a carry of one whenever a
-// byte (plus the incoming carry) is 128 or more.
-__device__ __forceinline__ void digits(long long F, int* d) {
-  const unsigned lo = (unsigned)F;
-  const int hi = (int)(F >> 32);
-  int c = 0;
+// Balanced base-256 digits d_0..d_6 of F (|F| < 2^55) as exact floats:
+// F = sum d_p 2^(8 (6 - p)), d_1..d_6 in [-128, 127], d_0 in [-128, 128].
+// Adding 128 at each of the six low byte positions, G = F + 0x808080808080,
+// lets the carries do the balancing: byte j of G is d_(6-j) + 128 (j < 6) and
+// G >> 48 is d_0.  The float of byte b - 128 is (2^23 + b) - (2^23 + 128),
+// with 2^23 + b assembled by one byte permute: exact, no conversion unit.
+__device__ __forceinline__ void digits(long long F, float* d) {
+  const unsigned long long G = (unsigned long long)F + 0x0000808080808080ULL;
+  const uint32_t lo = (uint32_t)G, hi = (uint32_t)(G >> 32);
 #pragma unroll
   for (int j = 0; j < kS - 1; j++) {
-    const unsigned u = (j < 4) ? ((lo >> (8 * j)) & 0xFFu) : (((unsigned)hi >> (8 * (j - 4))) & 0xFFu);
-    const int v = (int)u + c + 128;
-    d[kS - 1 - j] = (v & 255) - 128;
-    c = v >> 8;
+    const uint32_t bits = __byte_perm(j < 4 ? lo : hi, 0x4B000000u, 0x7440u | (uint32_t)(j & 3));
+    d[kS - 1 - j] = __uint_as_float(bits) - 8388736.0f;
   }
-  d[0] = (hi >> 16) + c;   // bits 48..63 of F, sign-extended, plus the carry
-}
-__device__ __forceinline__ uint32_t f32_bits(int d) {
-  return __float_as_uint((float)d);   // exact: |d| <= 128 has <= 8 significant bits
+  d[0] = (float)(int)((long long)G >> 48);
 }
 // Two BF16 digits in one word: the upper halves of their (exact) FP32 images.
-__device__ __forceinline__ uint32_t bf16x2(int d0, int d1) {
-  return __byte_perm(f32_bits(d0), f32_bits(d1), 0x7632);
+__device__ __forceinline__ uint32_t bf16x2(float d0, float d1) {
+  return __byte_perm(__float_as_uint(d0), __float_as_uint(d1), 0x7632);
 }
 // Byte offset of element (row, kk) (kk < 16) inside one K-major slice block:
 // core matrices [row/8][kk/8][8][16 bytes].
@@ -344,7 +340,7 @@ __device__ __forceinline__ void slice_b_quad(Ctx& c, uint8_t* stage, int g, int 
   const int col = g >> 2, q = g & 3;
   const int E = c.sEb[c.yb * kN + col];
   const double* y = c.sY + col * kLdY + k0 + 4 * q;
-  int d[4][kS];
+  float d[4][kS];
 #pragma unroll
   for (int i = 0; i < 4; i++) digits(fixed_of(y[i], E), d[i]);
   const int off = core_off(col, 4 * q);
@@ -533,20 +529,20 @@ inline __device__ void drain(Ctx& c, const int* Ea, int mode, double* g, int ldg
 #pragma unroll
     for (int i = 0; i < kDC; i++) mem[i] = msrc ? ldg_cg(msrc + row + (size_t)(c0 + i) * mld) : 0.0;
     long long hi[kDC], lo[kDC];
-#pragma unroll
-    for (int i = 0; i < kDC; i++) hi[i] = lo[i] = 0;
     uint32_t acc[kGroups][kDC];
     tmem_ld_groups(lane_addr + (uint32_t)c0, acc);
+    // Horner in base 2^8 over the groups, paired: |g_t| <= n_t 2^21 (n_t pairs
+    // per group), so g0 2^8 + g1 and g2 2^8 + g3 fit in 32 bits; the low
+    // groups need 64 bits.
 #pragma unroll
-    for (int t = 0; t < kGroups; t++) {
+    for (int i = 0; i < kDC; i++) {
+      int g[kGroups];
 #pragma unroll
-      for (int i = 0; i < kDC; i++) {
-        const long long q = (long long)__float2int_rn(__uint_as_float(acc[t][i]));
-        if (t < 4)
-          hi[i] = (hi[i] << kRho) + q;
-        else
-          lo[i] = (lo[i] << kRho) + q;
-      }
+      for (int t = 0; t < kGroups; t++) g[t] = __float2int_rn(__uint_as_float(acc[t][i]));
+      const int a = g[0] * 256 + g[1], b = g[2] * 256 + g[3];
+      hi[i] = (long long)a * 65536 + b;
+      const long long c = (long long)g[4] * 256 + g[5], d = (long long)g[6] * 256 + g[7];
+      lo[i] = c * 65536 + d;
     }
 #pragma unroll
     for (int i = 0; i < kDC; i++) {
@@ -617,7 +613,7 @@ inline __device__ void slice_left(const Acc& acc, uint8_t* dst, int* Ea, int* sE
     const int r = qd % kK;
     const int k4 = (qd / kK) * 4;
     const int E = sE[r];
-    int d[4][kS];
+    float d[4][kS];
 #pragma unroll
     for (int i = 0; i < 4; i++) digits(fixed_of(acc(r, k4 + i), E), d[i]);
     uint8_t* blk = dst + (size_t)(k4 / kKC) * kAChunkBytes;

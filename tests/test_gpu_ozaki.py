@@ -167,3 +167,43 @@ def test_split_rejects_unsupported_tile_order(env, NB):
     assert H.lib().hqr_plan_create(ctypes.byref(h), 4 * NB, 4 * NB, NB, 16, H.HQR_PREC_OZAKI) == \
         H.HQR_ERR_UNSUPPORTED
     assert H.lib().hqr_ozaki_product(NB, 1, 1, 1, None) == H.HQR_ERR_UNSUPPORTED
+
+
+def graded(n, kappa, seed):
+    """A = U diag(sigma) V^T, U and V Haar (QR of Gaussians, columns signed by
+    diag(R), Mezzadri 2007), sigma_i = kappa^(-i/(n-1))."""
+    rng = np.random.default_rng(seed)
+
+    def haar():
+        Q, R = np.linalg.qr(rng.standard_normal((n, n)))
+        return Q * np.sign(np.diag(R))
+
+    s = kappa ** (-np.arange(n) / (n - 1))
+    return (haar() * s) @ haar().T
+
+
+@pytest.mark.parametrize("kappa", [1e2, 1e8, 1e12])
+def test_split_on_graded_condition_numbers(env, kappa):
+    """Householder QR is backward stable whatever the conditioning: the split
+    path's residual and orthogonality stay within 4x of the FP64 path's on the
+    same matrix, and R, V, TAU match the oracle elementwise."""
+    torch, H = env
+    n, NB, IB = 512, 128, 32
+    A2d = graded(n, kappa, int(np.log10(kappa)))
+    A = O.to_tiles(A2d, NB)
+    out = {}
+    for prec in (H.HQR_PREC_OZAKI, H.HQR_PREC_FP64):
+        plan, dA, dTAU = factor(torch, H, A, n, n, NB, IB, prec)
+        dQ = torch.zeros(n * n, dtype=torch.float64, device="cuda")
+        a = dA.cpu().numpy()
+        H.check(H.lib().hqr_make_q(plan.h, dQ.data_ptr(), dA.data_ptr(), dTAU.data_ptr(), 0, None), "make_q")
+        out[prec] = (a, dTAU.cpu().numpy(), quality(A2d, dQ.cpu().numpy(), dA.cpu().numpy(), n, n, NB))
+        plan.close()
+    ra, rtau = O.tile_qr(A, n, n, NB, IB)
+    a, tau, (res, orth) = out[H.HQR_PREC_OZAKI]
+    t = tol(A2d)
+    assert np.abs(a - ra).max() <= t
+    assert np.abs(tau - rtau).max() <= t
+    res64, orth64 = out[H.HQR_PREC_FP64][2]
+    assert res <= 4 * max(res64, 1e-16)
+    assert orth <= 4 * orth64
