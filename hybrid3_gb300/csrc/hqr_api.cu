@@ -109,6 +109,26 @@ size_t tau_len(const hqr::Geometry& g) { return (size_t)g.MT * g.NT * g.NB; }
     if (_rc != HQR_OK) return _rc;  \
   } while (0)
 
+// Q^T into dQ, which the caller has zeroed (Hybrid_make_Q.c:91-95 sets the
+// diagonal of a caller-zeroed Q and applies H_1^T ... H_k^T to it).  Square
+// matrices: Q = H_1 (H_2 (... (H_k I))) accumulated backwards, which skips the
+// tile columns that are still unit vectors (2/3 of the forward updates), then
+// transposed in place; the identity is written whole, so the result does not
+// depend on dQ's prior contents.  Other shapes: the forward application.
+int build_qt(hqr_plan* plan, double* dQ, const double* dRY, const double* dTAU, bool rebuild_t,
+             cudaStream_t s) {
+  const hqr::Geometry& g = plan->g;
+  if (g.M == g.N && g.NB % 32 == 0) {
+    hqr::make_identity(dQ, g.M, g.N, g.NB, true, s);
+    TRY(hqr::launch_build_q(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g_timeout_ns, s, &plan->oz));
+    hqr::transpose_tiles(dQ, g.N, g.NB, s);
+    return cuda_rc(cudaGetLastError());
+  }
+  hqr::make_identity(dQ, g.M, g.N, g.NB, false, s);
+  return hqr::launch_apply_qt(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g.NT, rebuild_t, g_timeout_ns, s,
+                              &plan->oz);
+}
+
 int h2d(double* d, const double* h, size_t n, cudaStream_t s) {
   return cuda_rc(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, s));
 }
@@ -232,10 +252,7 @@ int hqr_make_q_async(hqr_plan_t* plan, double* dQ, double* dRY, const double* dT
   if (!plan || !dQ || !dRY || !dTAU) return HQR_ERR_INVALID;
   const hqr::Geometry& g = plan->g;
   cudaStream_t s = (cudaStream_t)stream;
-  // Hybrid_make_Q.c:91-95 sets the diagonal of the caller-zeroed Q
-  hqr::make_identity(dQ, g.M, g.N, g.NB, false, s);
-  TRY(hqr::launch_apply_qt(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g.NT, !use_plan_t, g_timeout_ns, s,
-                           &plan->oz));
+  TRY(build_qt(plan, dQ, dRY, dTAU, !use_plan_t, s));
   hqr::zero_reflectors(dRY, g.M, g.N, g.NB, s);
   return cuda_rc(cudaGetLastError());
 }
@@ -360,14 +377,17 @@ static int do_apply(mat_stat_t* st, double* Q, double* RY, double* TAU, int rank
   TRY(stage_reserve(2, (size_t)M * N, &dQ));
   TRY(h2d(dRY, RY, (size_t)M * N, s));
   TRY(h2d(dTAU, TAU, tau_len(plan->g), s));
-  if (mode == 1) {
-    hqr::make_identity(dQ, M, N, NB, true, s);
-  } else {
+  if (mode == 2) {
     TRY(h2d(dQ, Q, (size_t)M * N, s));
-    if (mode == 0) hqr::make_identity(dQ, M, N, NB, false, s);
+    TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dQ, plan->g.NT, true,
+                             g_timeout_ns, s, &plan->oz));
+  } else {
+    // make_Q (caller-zeroed Q, Hybrid_make_Q.c:91-95) and dorgqr (Q := I,
+    // Hybrid_dorgqr.c:56) both produce Q^T of the factorization
+    if (mode == 0 && plan->g.M != plan->g.N) TRY(h2d(dQ, Q, (size_t)M * N, s));
+    if (mode == 1) hqr::make_identity(dQ, M, N, NB, true, s);
+    TRY(build_qt(plan, dQ, dRY, dTAU, true, s));
   }
-  TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dQ, plan->g.NT, true,
-                           g_timeout_ns, s, &plan->oz));
   TRY(hqr_plan_status(plan, s));
   if (mode == 0) {
     hqr::zero_reflectors(dRY, M, N, NB, s);

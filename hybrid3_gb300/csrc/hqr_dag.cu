@@ -195,6 +195,30 @@ int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, doubl
   return run_dag(p, ws, g, stream);
 }
 
+int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT, const double* dTAU,
+                   double* dQ, long long timeout_ns, cudaStream_t stream, const OzWorkspace* ozw) {
+  if (g.M != g.N) return HQR_ERR_INVALID;
+  DagParams p{};
+  p.mode = kModeBuildQ;
+  p.MT = g.MT;
+  p.NT = g.NT;
+  p.CT = g.NT;
+  p.steps = g.steps;
+  p.J = g.NT;
+  p.A = const_cast<double*>(dA);
+  p.T = dT;
+  p.TAU = const_cast<double*>(dTAU);
+  p.C = dQ;
+  p.timeout_ns = timeout_ns;
+  set_oz(p, g, ozw);
+  p.prep = 0;
+  // per step i: MT - i panel tasks and NC (NT - i) (MT - i) updates
+  long long n = 0;
+  for (int i = 0; i < g.steps; i++) n += (g.MT - i) + (long long)p.NC * (g.NT - i) * (g.MT - i);
+  p.n_tasks = (int)n;
+  return run_dag(p, ws, g, stream);
+}
+
 bool oz_supported(const Geometry& g) { return g.NB == oz::kK; }
 
 static size_t panel_tiles(const Geometry& g) {

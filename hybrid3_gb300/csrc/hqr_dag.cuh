@@ -33,6 +33,11 @@ namespace hqr {
 enum DagMode : int {
   kModeFactor = 0,    // Hybrid_tile_QR: GEQRT/TSQRT panels + LARFB/SSRFB updates of A
   kModeApplyQt = 1,   // C <- Q^T C: T-build panels + LARFB/SSRFB updates of C
+  // Q <- Q_0 Q_1 ... Q_{steps-1} C for C = I (square): the panel columns from
+  // the last to the first, each panel tile's reflector H (not H^T), tile rows
+  // from the bottom up; step i touches tile columns j >= i only (columns j < i
+  // are still unit vectors in rows >= i), 2/3 of the updates of kModeApplyQt.
+  kModeBuildQ = 2,
 };
 
 // With split precision (DagParams::oz) the update tasks run OZAPPLY and every
@@ -128,7 +133,9 @@ __device__ __forceinline__ TaskDesc decode(const DagParams& p, int id) {
 }
 
 __device__ __forceinline__ bool update_valid(const DagParams& p, int i, int j) {
-  return (p.mode == kModeFactor) ? (j > i && j < p.NT) : (j < p.CT);
+  if (p.mode == kModeFactor) return j > i && j < p.NT;
+  if (p.mode == kModeBuildQ) return j >= i && j < p.CT;
+  return j < p.CT;
 }
 
 __device__ __forceinline__ bool is_high_priority(const DagParams& p, int id) {
@@ -230,8 +237,12 @@ __global__ void dag_init_kernel(DagParams p) {
     const int j = u % p.J;
     const int i = u / p.J;
     (void)c;
-    if (k >= i && i < p.steps && update_valid(p, i, j))
-      deps = 1 + (k > i ? 1 : 0) + (i > 0 ? 1 : 0);
+    if (k >= i && i < p.steps && update_valid(p, i, j)) {
+      if (p.mode == kModeBuildQ)   // panel + chain from the tile below + step i+1's write of (k, j)
+        deps = 1 + (k < p.MT - 1 ? 1 : 0) + ((k > i && j > i && i + 1 < p.steps) ? 1 : 0);
+      else
+        deps = 1 + (k > i ? 1 : 0) + (i > 0 ? 1 : 0);
+    }
   }
   p.cnt[id] = deps;
 }
@@ -249,12 +260,19 @@ __device__ void release_dependents(const DagParams& p, const TaskDesc& t) {
     if (feeds_prep) {
       release(p, prep_id(p, t.i, t.k));
     } else {
-      const int j0 = (p.mode == kModeFactor) ? t.i + 1 : 0;
+      const int j0 = (p.mode == kModeFactor) ? t.i + 1 : (p.mode == kModeBuildQ) ? t.i : 0;
       const int j1 = (p.mode == kModeFactor) ? p.NT : p.CT;
       for (int j = j0; j < j1; j++)
         for (int c = 0; c < p.NC; c++) release(p, update_id(p, t.i, j, t.k, c));
     }
     if ((t.type == kGEQRT || t.type == kTSQRT) && t.k + 1 < p.MT) release(p, panel_id(p, t.i, t.k + 1));
+    return;
+  }
+  if (p.mode == kModeBuildQ) {
+    // the chain runs from the bottom tile up to the LARFB; the step before
+    // (i - 1) next writes tile (k, j), which this task wrote last
+    if (t.k - 1 >= t.i) release(p, update_id(p, t.i, t.j, t.k - 1, t.c));
+    if (t.i >= 1) release(p, update_id(p, t.i - 1, t.j, t.k, t.c));
     return;
   }
   // LARFB / SSRFB: LIN to the next task of this column chain
@@ -336,7 +354,7 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
           const size_t slot = panel_slot(p.MT, t.i, t.k);
           task_ozprep(p.A + o, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.T + o, t.k == t.i,
                       p.slices + slot * oz::panel_slice_bytes(), p.sexp + slot * 3 * NB,
-                      reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
+                      reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr, p.mode != kModeBuildQ);
         }
         break;
       }
@@ -349,7 +367,8 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
           task_ozapply(c, p.slices + slot * oz::panel_slice_bytes(), p.sexp + slot * 3 * NB, nullptr,
                        p.C + oc + (size_t)t.c * oz::kN * NB);
         } else {
-          task_larfb(p.A + ov, p.T + ov, p.C + oc, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp);
+          task_larfb(p.A + ov, p.T + ov, p.C + oc, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp,
+                     p.mode == kModeBuildQ);
         }
         break;
       }
@@ -364,7 +383,8 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
           task_ozapply(c, p.slices + slot * oz::panel_slice_bytes(), p.sexp + slot * 3 * NB,
                        p.C + o1 + cofs, p.C + o2 + cofs);
         } else {
-          task_ssrfb(p.C + o1, p.C + o2, p.A + ov, p.T + ov, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp);
+          task_ssrfb(p.C + o1, p.C + o2, p.A + ov, p.T + ov, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp,
+                     p.mode == kModeBuildQ);
         }
         break;
       }

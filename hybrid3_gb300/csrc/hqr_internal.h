@@ -59,6 +59,10 @@ int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, d
 int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT,
                     const double* dTAU, double* dC, int CT, bool rebuild_t, long long timeout_ns,
                     cudaStream_t stream, const OzWorkspace* oz = nullptr);
+// Q = H_0 H_1 ... H_{steps-1} dQ for dQ = I (square matrices): backward
+// accumulation, skipping the tile columns that are still unit vectors.
+int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT, const double* dTAU,
+                   double* dQ, long long timeout_ns, cudaStream_t stream, const OzWorkspace* oz = nullptr);
 // Scratch supplied by the caller instead of a DagWorkspace (no allocation).
 struct ExternalScratch {
   double* T;
@@ -85,6 +89,8 @@ int dag_sm_count();
 // Utility kernels (hqr_util.cu)
 void fill_uniform(double* dA, long M, long N, int NB, uint64_t seed, cudaStream_t s);
 void make_identity(double* dQ, long M, long N, int NB, bool zero_first, cudaStream_t s);
+// In-place transpose of a square N x N tile-layout matrix (NB a multiple of 32).
+void transpose_tiles(double* dQ, long N, int NB, cudaStream_t s);
 void zero_reflectors(double* dA, long M, long N, int NB, cudaStream_t s);
 void dgemm_tn_tiles(const double* dA, const double* dB, double* dC, long M, long N, int NB,
                     cudaStream_t s);

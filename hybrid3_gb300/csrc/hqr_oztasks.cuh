@@ -17,12 +17,14 @@ namespace hqr {
 // Offsets of a panel tile's three prepared operands and their row exponents.
 constexpr size_t kOzVT = 0, kOzTT = 1, kOzV = 2;
 
-// X(r, k) = T^T(r, k) = T(k, r), T upper triangular, packed by columns in
-// shared memory: T(a, b) (a <= b) at b (b + 1) / 2 + a.
-struct PackedTTAcc {
+// T upper triangular, packed by columns in shared memory: T(a, b) (a <= b)
+// at b (b + 1) / 2 + a.  As a left operand: X = T^T (transposed) or X = T.
+struct PackedTAcc {
   const double* t;
+  bool transposed;
   __device__ __forceinline__ double operator()(int r, int k) const {
-    return (k <= r) ? t[r * (r + 1) / 2 + k] : 0.0;
+    if (transposed) return (k <= r) ? t[r * (r + 1) / 2 + k] : 0.0;   // T^T(r, k) = T(k, r)
+    return (r <= k) ? t[k * (k + 1) / 2 + r] : 0.0;
   }
 };
 
@@ -59,11 +61,13 @@ inline __device__ void t_recurrence(const double* sG, double* sT, const double* 
 
 // OZPREP of panel tile V (global, NB x NB; unit: the V of a GEQRT tile, else
 // the dense V of a TSQRT tile) with TAU tau.  G: NB x NB global scratch.
-// slices / exps: this tile's prepared operands and row exponents.  sm: the
-// CTA's dynamic shared memory (oz::kSmemBytes).  False on a device time-out.
+// slices / exps: this tile's prepared operands and row exponents; the middle
+// operand is T^T (applying H^T) or, with t_transposed false, T (applying H).
+// sm: the CTA's dynamic shared memory (oz::kSmemBytes).  False on a device
+// time-out.
 inline __device__ bool task_ozprep(const double* V, const double* tau, double* G, bool unit,
                                    uint8_t* slices, int* exps, uint8_t* sm, uint32_t tmem,
-                                   unsigned* err) {
+                                   unsigned* err, bool t_transposed) {
   using namespace oz;
   constexpr size_t ob = operand_bytes();
   // 1. V^T and V from a shared-memory copy of the tile
@@ -105,8 +109,8 @@ inline __device__ bool task_ozprep(const double* V, const double* tau, double* G
   }
   __syncthreads();
   t_recurrence(sG, sT, tau);
-  // 4. T^T
-  slice_left(PackedTTAcc{sT}, slices + kOzTT * ob, exps + kOzTT * kK, sE);
+  // 4. T^T or T
+  slice_left(PackedTAcc{sT, t_transposed}, slices + kOzTT * ob, exps + kOzTT * kK, sE);
   return true;
 }
 

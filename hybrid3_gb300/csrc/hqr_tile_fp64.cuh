@@ -243,14 +243,15 @@ __device__ void build_t_block(const double* V, int ldv, int m, int w, bool unit,
 // ---------------------------------------------------------------------------
 // Apply the transpose of one w-column block reflector H = I - V T V^T,
 // V = [Vt; Vb], to [Ct; Cb] held in shared memory:
-//     W = Vt^T Ct + Vb^T Cb;  W = T^T W;  Ct -= Vt W;  Cb -= Vb W.
+//     W = Vt^T Ct + Vb^T Cb;  W = T^T W;  Ct -= Vt W;  Cb -= Vb W
+// (notrans: H itself, W = T W).
 // Vt: w x w unit lower (unit_top) or the identity; Vb: mb x w.  V and T are
 // read from global memory (ld ldv / ldt).  ncol must be a multiple of 8.
 // ---------------------------------------------------------------------------
 __device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off,
                               const double* __restrict__ gT, int ldt, int w, int mb, bool unit_top,
                               double* Ct, int ldct, double* Cb, int ldcb, int ncol, double* smem,
-                              const SmemPlan& sp, int RC) {
+                              const SmemPlan& sp, int RC, bool notrans = false) {
   double* sVb = smem + sp.off_vb;
   double* sVt = smem + sp.off_vt;
   double* sT = smem + sp.off_t;
@@ -314,11 +315,14 @@ __device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off
   }
   __syncthreads();
 
-  // ---- W2 = T^T W ---------------------------------------------------------
+  // ---- W2 = T^T W (notrans: T W) --------------------------------------------
   for (int e = tid; e < w * ncol; e += kThreads) {
     const int aa = e % w, j = e / w;
     double v = 0.0;
-    for (int b = 0; b <= aa; b++) v = fma(sT[b + aa * w], sW[b + j * w], v);
+    if (notrans)
+      for (int b = aa; b < w; b++) v = fma(sT[aa + b * w], sW[b + j * w], v);
+    else
+      for (int b = 0; b <= aa; b++) v = fma(sT[b + aa * w], sW[b + j * w], v);
     sW2[aa + j * w] = v;
   }
   __syncthreads();
@@ -455,26 +459,30 @@ __device__ void task_tsqrt(double* A1, double* A2, double* T, double* tau_g, con
 }
 
 // CORE_dormqr(Left, Trans, NB, ncol, NB, IB, V, NB, T, NB, C, NB) on columns
-// [c0, c0+ncol) of C.
+// [c0, c0+ncol) of C (notrans: CORE_dormqr(Left, NoTrans, ...), the inner
+// blocks in reverse order).
 __device__ void task_larfb(const double* V, const double* T, double* C, int c0, int ncol,
-                           const TileShape& sh, double* smem, const SmemPlan& sp) {
+                           const TileShape& sh, double* smem, const SmemPlan& sp, bool notrans = false) {
   const int NB = sh.NB, w = sh.w;
   double* sC = smem + sp.off_c1;
   __syncthreads();
   load_block(sC, NB, C + (size_t)c0 * NB, NB, NB, ncol);
   __syncthreads();
-  for (int i0 = 0; i0 < NB; i0 += w) {
+  for (int b = 0; b < NB / w; b++) {
+    const int i0 = (notrans ? NB / w - 1 - b : b) * w;
     apply_block_t(V + i0 + (size_t)i0 * NB, NB, w, T + i0 + (size_t)i0 * NB, NB, w, NB - i0 - w, true,
-                  sC + i0, NB, sC + i0 + w, NB, ncol, smem, sp, sh.RC);
+                  sC + i0, NB, sC + i0 + w, NB, ncol, smem, sp, sh.RC, notrans);
   }
   store_block(C + (size_t)c0 * NB, NB, sC, NB, NB, ncol);
   __syncthreads();
 }
 
 // CORE_dtsmqr(Left, Trans, NB, ncol, NB, ncol, NB, IB, A1, NB, A2, NB, V, NB,
-// T, NB) on columns [c0, c0+ncol) of A1 and A2.
+// T, NB) on columns [c0, c0+ncol) of A1 and A2 (notrans: Left, NoTrans, the
+// inner blocks in reverse order).
 __device__ void task_ssrfb(double* A1, double* A2, const double* V, const double* T, int c0,
-                           int ncol, const TileShape& sh, double* smem, const SmemPlan& sp) {
+                           int ncol, const TileShape& sh, double* smem, const SmemPlan& sp,
+                           bool notrans = false) {
   const int NB = sh.NB, w = sh.w;
   double* s1 = smem + sp.off_c1;
   double* s2 = smem + sp.off_c2;
@@ -482,9 +490,10 @@ __device__ void task_ssrfb(double* A1, double* A2, const double* V, const double
   load_block(s1, NB, A1 + (size_t)c0 * NB, NB, NB, ncol);
   load_block(s2, NB, A2 + (size_t)c0 * NB, NB, NB, ncol);
   __syncthreads();
-  for (int i0 = 0; i0 < NB; i0 += w) {
+  for (int b = 0; b < NB / w; b++) {
+    const int i0 = (notrans ? NB / w - 1 - b : b) * w;
     apply_block_t(V + (size_t)i0 * NB, NB, 0, T + i0 + (size_t)i0 * NB, NB, w, NB, false, s1 + i0, NB,
-                  s2, NB, ncol, smem, sp, sh.RC);
+                  s2, NB, ncol, smem, sp, sh.RC, notrans);
   }
   store_block(A1 + (size_t)c0 * NB, NB, s1, NB, NB, ncol);
   store_block(A2 + (size_t)c0 * NB, NB, s2, NB, NB, ncol);

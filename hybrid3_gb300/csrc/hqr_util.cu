@@ -47,6 +47,31 @@ __global__ void k_identity(double* Q, long M, long N, int NB, int zero_first) {
   }
 }
 
+// In-place transpose of a square tile-layout matrix, by 32 x 32 blocks (each
+// inside one tile): the CTA of block (bi, bj), bi <= bj, swaps the transposes
+// of blocks (bi, bj) and (bj, bi) through shared memory.  Block 32 x 8.
+__global__ void k_transpose_tiles(double* Q, long N, int NB) {
+  __shared__ double a[32][33], b[32][33];
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (bi > bj) return;
+  const int MT = (int)(N / NB);
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  auto at = [&](long R, long C) -> size_t {
+    return ((size_t)(R / NB) + (size_t)(C / NB) * MT) * (size_t)NB * NB + (size_t)(R % NB) +
+           (size_t)(C % NB) * NB;
+  };
+  const long r0 = 32L * bi, c0 = 32L * bj;
+  for (int y = ty; y < 32; y += 8) {
+    a[y][tx] = Q[at(r0 + tx, c0 + y)];
+    if (bi != bj) b[y][tx] = Q[at(c0 + tx, r0 + y)];
+  }
+  __syncthreads();
+  for (int y = ty; y < 32; y += 8) {
+    Q[at(c0 + tx, r0 + y)] = a[tx][y];
+    if (bi != bj) Q[at(r0 + tx, c0 + y)] = b[tx][y];
+  }
+}
+
 // Zero V: the strictly lower part of the diagonal tiles (i,i) and every tile
 // (k,i), k > i, of the first min(MT, NT) tile columns.
 __global__ void k_zero_reflectors(double* A, long M, long N, int NB) {
@@ -213,6 +238,10 @@ void fill_uniform(double* dA, long M, long N, int NB, uint64_t seed, cudaStream_
 }
 void make_identity(double* dQ, long M, long N, int NB, bool zero_first, cudaStream_t s) {
   k_identity<<<grid_for((size_t)M * N), 256, 0, s>>>(dQ, M, N, NB, zero_first ? 1 : 0);
+}
+void transpose_tiles(double* dQ, long N, int NB, cudaStream_t s) {
+  const int nb = (int)(N / 32);
+  k_transpose_tiles<<<dim3(nb, nb), dim3(32, 8), 0, s>>>(dQ, N, NB);
 }
 void zero_reflectors(double* dA, long M, long N, int NB, cudaStream_t s) {
   k_zero_reflectors<<<grid_for((size_t)M * N), 256, 0, s>>>(dA, M, N, NB);

@@ -186,7 +186,9 @@ def graded(n, kappa, seed):
 def test_split_on_graded_condition_numbers(env, kappa):
     """Householder QR is backward stable whatever the conditioning: the split
     path's residual and orthogonality stay within 4x of the FP64 path's on the
-    same matrix, and R, V, TAU match the oracle elementwise."""
+    same matrix, and R matches the oracle elementwise (absolute errors of R are
+    eps ||A||; V and TAU of the late, tiny trailing blocks are ill-determined
+    for large kappa, for any two FP64 implementations alike)."""
     torch, H = env
     n, NB, IB = 512, 128, 32
     A2d = graded(n, kappa, int(np.log10(kappa)))
@@ -201,9 +203,8 @@ def test_split_on_graded_condition_numbers(env, kappa):
         plan.close()
     ra, rtau = O.tile_qr(A, n, n, NB, IB)
     a, tau, (res, orth) = out[H.HQR_PREC_OZAKI]
-    t = tol(A2d)
-    assert np.abs(a - ra).max() <= t
-    assert np.abs(tau - rtau).max() <= t
+    R = np.triu(O.from_tiles(a, n, n, NB))
+    assert np.abs(R - np.triu(O.from_tiles(ra, n, n, NB))).max() <= tol(A2d)
     res64, orth64 = out[H.HQR_PREC_FP64][2]
     assert res <= 4 * max(res64, 1e-16)
     assert orth <= 4 * orth64
