@@ -192,9 +192,10 @@ def measured_peaks():
         return {}
 
 
-# slice products per emulated product (digit scheme by tile order)
+# slice products per emulated product: 8 digits per element, the 36 digit
+# pairs with p + q <= 7 (NB = 128, the only tile order of the split path)
 def split_products(NB: int) -> int:
-    return 34 if NB <= 128 else 36
+    return 36
 
 
 def graded_tiles(H, torch, L, n: int, NBs, kappa: float, seed: int):

@@ -9,21 +9,27 @@
 // Algorithms 59, 2012):
 //
 //   * every row of X (and every column of Y) is scaled by the power of two of
-//     its largest element and written as a fixed-point integer F, |F| <= 2^55;
-//   * F is split into kS = 7 signed digits of kRho = 8 bits, |d| <= 128,
-//     F = sum_p d_p 2^(8 (6 - p)); every digit is an exact BF16 value;
-//   * the slice products X_p Y_q with p + q <= 7 (0-based; 34 of the 49) are
+//     its largest element and written as a fixed-point integer F, |F| < 2^62,
+//     so an element 2^-9 of its row maximum still keeps 53 bits;
+//   * F is split into kS = 8 signed digits of kRho = 8 bits, |d_0| <= 64,
+//     |d_p| <= 128, F = sum_p d_p 2^(8 (7 - p)); every digit is an exact BF16
+//     value;
+//   * the slice products X_p Y_q with p + q <= 7 (0-based; 36 of the 64) are
 //     exact on the tensor cores: |d_x d_y| <= 2^14, a K = 128 sum stays below
-//     2^21, and the <= 7 products sharing t = p + q (weight 2^(-8t)) are
-//     accumulated in one FP32 TMEM accumulator, < 7 * 2^21 < 2^24;
+//     2^21, and the <= 8 products sharing t = p + q (weight 2^(-8t)) are
+//     accumulated in one FP32 TMEM accumulator, < 7 * 2^21 < 2^24 (the two
+//     products with the top digit are at most 2^13);
 //   * the 8 t-group accumulators (8 x 64 TMEM columns = the whole TMEM) are
-//     recombined exactly in 64-bit integers (two Horner chains in base 2^8)
-//     and turned into FP64 by integer operations on the IEEE 754 encoding.
-//     The dropped products weigh < 2^-64 of rowmax(X) * colmax(Y) * K.
+//     recombined exactly in 64-bit integers (two Horner chains in base 2^8,
+//     V = hi 2^32 + lo, up to 76 bits), shifted right only as far as V's bit
+//     length requires to fit 61 bits, and turned into FP64 by integer
+//     operations on the IEEE 754 encoding: the result is V rounded once (to
+//     within 2^-61).  The dropped products weigh < 2^-58 of
+//     rowmax(X) * colmax(Y) * K.
 //
 // The left operands are sliced once per panel tile into HBM, already in the
-// tcgen05 K-major core-matrix layout, so each 16-deep K chunk of all 7 slices
-// arrives with one 28 KiB bulk TMA copy.  The right operand lives in shared
+// tcgen05 K-major core-matrix layout, so each 16-deep K chunk of all 8 slices
+// arrives with one 32 KiB bulk TMA copy.  The right operand lives in shared
 // memory (staged from HBM for the first product of an update, written there
 // by the previous product's epilogue otherwise) and is sliced chunk by chunk
 // into a double-buffered stage while the MMAs of the previous chunk run.
@@ -43,17 +49,15 @@ constexpr int kM = 128;            // rows per MMA (one TMEM lane per row)
 constexpr int kKC = 16;            // K per BF16 MMA
 constexpr int kChunks = kK / kKC;  // 8 K chunks per product
 constexpr int kRho = 8;            // bits per digit
-constexpr int kS = 7;              // digits (slices) per element
+constexpr int kS = 8;              // digits (slices) per element
 constexpr int kGroups = 8;         // t-group accumulators: t = p + q in [0, 7]
-constexpr int kShiftHi = 14;       // X = (hi << kShiftHi) + (lo >> kShiftLo)
-constexpr int kShiftLo = 18;
-constexpr int kExpBias = 1073;     // biased exponent of the scale of X = Ea + Eb - kExpBias
+constexpr int kExpBias = 1089;     // biased exponent of the scale of V = hi 2^32 + lo: Ea + Eb - kExpBias
 constexpr int kDC = 8;             // accumulator columns recombined per epilogue pass (tmem_ld_groups)
 constexpr int kLdY = kK + 1;       // leading dimension of the staged right operand
 constexpr int kSliceABytes = kM * kKC * 2;              // 4 KiB
 constexpr int kSliceBBytes = kN * kKC * 2;              // 2 KiB
-constexpr int kAChunkBytes = kS * kSliceABytes;         // 28 KiB: all slices of one K chunk
-constexpr int kBChunkBytes = kS * kSliceBBytes;         // 14 KiB
+constexpr int kAChunkBytes = kS * kSliceABytes;         // 32 KiB: all slices of one K chunk
+constexpr int kBChunkBytes = kS * kSliceBBytes;         // 16 KiB
 constexpr long long kWaitIters = 1LL << 26;             // bounded mbarrier waits
 
 // Bytes of one prepared left operand and of the three of a panel tile.
@@ -207,8 +211,8 @@ __device__ __forceinline__ void tmem_ld_groups(uint32_t taddr, uint32_t (&r)[8][
 __device__ __forceinline__ int biased_exp(double x) {
   return (int)((__double_as_longlong(x) >> 52) & 0x7ff);
 }
-// F = x * 2^(1077 - E) rounded to the nearest integer, halves away from zero
-// (|F| < 2^55 when x's exponent e <= E); subnormals and zeros give 0.
+// F = x * 2^(1084 - E) rounded to the nearest integer, halves away from zero
+// (|F| < 2^62 when x's exponent e <= E); subnormals and zeros give 0.
 // Rounding (not truncation) keeps the representation error of elements below
 // the row / column maximum unbiased, so it does not accumulate coherently over
 // successive updates.
@@ -216,26 +220,27 @@ __device__ __forceinline__ long long fixed_of(double x, int E) {
   const long long b = __double_as_longlong(x);
   const int e = (int)((b >> 52) & 0x7ff);
   const int k = E - e;   // >= 0: E is the maximum exponent of the row / column
-  if (e == 0 || k > 56) return 0;
-  const unsigned long long t = ((unsigned long long)(b & 0xFFFFFFFFFFFFFLL) | (1ULL << 52)) << 2;
+  if (e == 0 || k > 63) return 0;
+  const unsigned long long t = ((unsigned long long)(b & 0xFFFFFFFFFFFFFLL) | (1ULL << 52)) << 9;
   const unsigned long long F = (k == 0) ? t : (((t >> (k - 1)) + 1ULL) >> 1);
   return (b < 0) ? -(long long)F : (long long)F;
 }
-// Balanced base-256 digits d_0..d_6 of F (|F| < 2^55) as exact floats:
-// F = sum d_p 2^(8 (6 - p)), d_1..d_6 in [-128, 127], d_0 in [-128, 128].
-// Adding 128 at each of the six low byte positions, G = F + 0x808080808080,
-// lets the carries do the balancing: byte j of G is d_(6-j) + 128 (j < 6) and
-// G >> 48 is d_0.  The float of byte b - 128 is (2^23 + b) - (2^23 + 128),
-// with 2^23 + b assembled by one byte permute: exact, no conversion unit.
+// Balanced base-256 digits d_0..d_7 of F (|F| < 2^62) as exact floats:
+// F = sum d_p 2^(8 (7 - p)), d_1..d_7 in [-128, 127], d_0 in [-64, 64].
+// Adding 128 at each of the seven low byte positions, G = F + 0x80808080808080
+// (no overflow: |G| < 2^63), lets the carries do the balancing: byte j of G is
+// d_(7-j) + 128 (j < 7) and G >> 56 is d_0.  The float of byte b - 128 is
+// (2^23 + b) - (2^23 + 128), with 2^23 + b assembled by one byte permute:
+// exact, no conversion unit.
 __device__ __forceinline__ void digits(long long F, float* d) {
-  const unsigned long long G = (unsigned long long)F + 0x0000808080808080ULL;
-  const uint32_t lo = (uint32_t)G, hi = (uint32_t)(G >> 32);
+  const long long G = F + 0x0080808080808080LL;
+  const uint32_t lo = (uint32_t)G, hi = (uint32_t)((unsigned long long)G >> 32);
 #pragma unroll
   for (int j = 0; j < kS - 1; j++) {
     const uint32_t bits = __byte_perm(j < 4 ? lo : hi, 0x4B000000u, 0x7440u | (uint32_t)(j & 3));
     d[kS - 1 - j] = __uint_as_float(bits) - 8388736.0f;
   }
-  d[0] = (float)(int)((long long)G >> 48);
+  d[0] = (float)(int)(G >> 56);
 }
 // Two BF16 digits in one word: the upper halves of their (exact) FP32 images.
 __device__ __forceinline__ uint32_t bf16x2(float d0, float d1) {
@@ -531,9 +536,9 @@ inline __device__ void drain(Ctx& c, const int* Ea, int mode, double* g, int ldg
     long long hi[kDC], lo[kDC];
     uint32_t acc[kGroups][kDC];
     tmem_ld_groups(lane_addr + (uint32_t)c0, acc);
-    // Horner in base 2^8 over the groups, paired: |g_t| <= n_t 2^21 (n_t pairs
-    // per group), so g0 2^8 + g1 and g2 2^8 + g3 fit in 32 bits; the low
-    // groups need 64 bits.
+    // Horner in base 2^8 over the groups, paired: |g_t| <= 2^21 (t + 1) (the
+    // two pairs with the top digit at half that), so g0 2^8 + g1 and
+    // g2 2^8 + g3 fit in 32 bits; the low groups need 64 bits.
 #pragma unroll
     for (int i = 0; i < kDC; i++) {
       int g[kGroups];
@@ -547,9 +552,14 @@ inline __device__ void drain(Ctx& c, const int* Ea, int mode, double* g, int ldg
 #pragma unroll
     for (int i = 0; i < kDC; i++) {
       const int col = c0 + i;
-      const long long X = (hi[i] << kShiftHi) + ((lo[i] + (1LL << (kShiftLo - 1))) >> kShiftLo);
+      // V = hi 2^32 + lo, |hi| < 2^44, |lo| < 2^48: exact when hi has at most
+      // 29 bits, else shifted right by its excess (lo rounded), |X| < 2^61 + 2^48
+      const long long h = hi[i];
+      const int bl = 64 - __clzll(h < 0 ? -h : h);
+      const int sh = bl > 29 ? bl - 29 : 0;
+      const long long X = (long long)((unsigned long long)h << (32 - sh)) + ((lo[i] + ((1LL << sh) >> 1)) >> sh);
       const int eb = c.sEb[c.yb * kN + col];
-      const double r = (ea > 0 && eb > 0) ? scaled_i64(X, ea + eb - kExpBias) : 0.0;
+      const double r = (ea > 0 && eb > 0) ? scaled_i64(X, ea + eb - kExpBias + sh) : 0.0;
       const size_t o = (size_t)col;
       double y = 0.0;
       if (mode == kEpiStore) {
