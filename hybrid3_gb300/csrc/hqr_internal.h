@@ -50,6 +50,8 @@ struct OzWorkspace {
 size_t oz_slice_bytes(const Geometry& g);
 size_t oz_exp_bytes(const Geometry& g);
 bool oz_supported(const Geometry& g);
+// Inner block width of the FP64 panels for the split path (see hqr_dag.cu).
+int narrow_panels(Geometry* g);
 
 // Enqueue a factorization DAG on `stream` (no synchronisation).
 int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, double* dTAU,

@@ -470,31 +470,26 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
   return ok;
 }
 
-// X * 2^(se - 1023) as binary64, rounded to nearest even, built with integer
-// operations from the IEEE 754 encoding (normalise |X|, round to 53 bits,
-// add the exponent).  The FP64 units of this part are scarce; the epilogue
-// keeps them for the one addition per element.  Falls back to FP64
-// arithmetic when the result is not a normal number.
+// X * 2^(se - 1023) as binary64, rounded to nearest even, built branch-free
+// with integer operations from the IEEE 754 encoding (normalise |X|, round to
+// 53 bits, add the exponent).  The FP64 units of this part are scarce; the
+// epilogue keeps them for the one addition per element.  Range: results below
+// 2^-1022 flush to zero, results of 2^1024 and above saturate to +-inf (a
+// rounding carry out of the largest exponent lands on the inf encoding).
 __device__ __forceinline__ double scaled_i64(long long X, int se) {
-  if (X == 0) return 0.0;
-  const unsigned long long sign = (X < 0) ? (1ULL << 63) : 0ULL;
-  unsigned long long u = (X < 0) ? 0ULL - (unsigned long long)X : (unsigned long long)X;
-  const int lz = __clzll((long long)u);
-  u <<= lz;                                              // leading one at bit 63
-  unsigned long long m = u >> 11;                        // 53 significant bits
-  const unsigned rem = (unsigned)u & 0x7FFu;
-  m += (rem > 0x400u || (rem == 0x400u && (m & 1ULL))) ? 1ULL : 0ULL;
-  const int e = se + 63 - lz;                            // biased exponent before a carry
+  const unsigned long long sign = (unsigned long long)X & (1ULL << 63);
+  const unsigned long long u0 = X < 0 ? 0ULL - (unsigned long long)X : (unsigned long long)X;
+  const int lz = __clzll((long long)u0);                       // 64 when X == 0
+  const unsigned long long u = u0 << (lz & 63);                // leading one at bit 63
+  const unsigned long long m = u >> 11;                        // 53 significant bits
+  const unsigned long long rb = (u >> 10) & 1ULL, sticky = (u & 0x3FFULL) != 0ULL;
+  const unsigned long long mr = m + (rb & (sticky | (m & 1ULL)));
+  const int e = se + 63 - lz;                                  // biased exponent before a carry
   // m carries its leading one into the exponent field (and a rounding carry
   // to 2^53 bumps the exponent once more, with a zero fraction)
-  const unsigned long long bits = ((unsigned long long)(e - 1) << 52) + m;
-  const int ef = (int)(bits >> 52);
-  if (e < 1 || ef > 2046) {
-    const double scale = (se > 0 && se < 2047) ? __longlong_as_double((long long)se << 52)
-                                               : ldexp(1.0, se - 1023);
-    return (double)X * scale;
-  }
-  return __longlong_as_double((long long)(sign | bits));
+  const unsigned long long bits = ((unsigned long long)(e - 1) << 52) + mr;
+  const unsigned long long res = (e < 1 || X == 0) ? 0ULL : (e > 2046 ? 0x7FF0000000000000ULL : bits);
+  return __longlong_as_double((long long)(sign | res));
 }
 
 // Epilogue modes (R = the product just computed).

@@ -94,10 +94,12 @@ __device__ void block_larfg(double* alpha, double* x, int n, double* tau_out, do
   }
   ss = block_sum(ss, red);
   double xnorm;
+  bool plain = false;   // ||x||^2 and alpha^2 in range: beta from the squared norms directly
   if (ss == 0.0) {
     xnorm = 0.0;
   } else if (ss >= 1e-290 && ss <= 1e290) {
     xnorm = sqrt(ss);
+    plain = true;
   } else {  // scaled norm, as LAPACK dnrm2 does, for tiny or huge columns
     double amax = 0.0;
     for (int r = threadIdx.x; r < n; r += kThreads) amax = fmax(amax, fabs(x[r]));
@@ -114,7 +116,14 @@ __device__ void block_larfg(double* alpha, double* x, int n, double* tau_out, do
   if (threadIdx.x == 0) {
     double a = *alpha, tau = 0.0, beta = a, scal = 1.0;
     int knt = 0;
-    if (xnorm != 0.0) {
+    const double aa = fabs(a);
+    if (xnorm != 0.0 && plain && aa < 1e140 && (aa > 1e-140 || a == 0.0)) {
+      // dlapy2(alpha, ||x||) as sqrt(alpha^2 + ||x||^2): no overflow or
+      // underflow in this range, one square root instead of two
+      beta = -copysign(sqrt(fma(a, a, ss)), a);
+      tau = (beta - a) / beta;
+      scal = 1.0 / (a - beta);
+    } else if (xnorm != 0.0) {
       const double safmin = DBL_MIN / (DBL_EPSILON * 0.5);
       const double rsafmn = 1.0 / safmin;
       double xn = xnorm;
