@@ -41,7 +41,7 @@ class MatStat(ctypes.Structure):
 
 
 class HqrStats(ctypes.Structure):
-    _fields_ = [("count", ctypes.c_ulonglong * 6), ("cycles", ctypes.c_ulonglong * 6)]
+    _fields_ = [("count", ctypes.c_ulonglong * 7), ("cycles", ctypes.c_ulonglong * 7)]
 
 
 class TilSch(ctypes.Structure):

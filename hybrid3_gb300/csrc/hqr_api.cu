@@ -239,9 +239,9 @@ int hqr_geqrf(hqr_plan_t* plan, double* dA, double* dTAU, void* stream) {
 
 int hqr_plan_stats(hqr_plan_t* plan, hqr_stats_t* out, void* stream) {
   if (!plan || !out || !plan->ws.stats) return HQR_ERR_INVALID;
-  unsigned long long v[12];
+  unsigned long long v[14];
   TRY(hqr::dag_stats(&plan->ws, v, (cudaStream_t)stream));
-  for (int t = 0; t < 6; t++) {
+  for (int t = 0; t < 7; t++) {
     out->count[t] = v[2 * t];
     out->cycles[t] = v[2 * t + 1];
   }

@@ -60,7 +60,7 @@ int dag_workspace_reserve(DagWorkspace* ws, size_t n_ids) {
   if (cudaMalloc(&ws->qhi, n_ids * sizeof(int)) != cudaSuccess) return HQR_ERR_NOMEM;
   if (cudaMalloc(&ws->qlo, n_ids * sizeof(int)) != cudaSuccess) return HQR_ERR_NOMEM;
   if (cudaMalloc(&ws->ctl, kCtlWords * sizeof(unsigned)) != cudaSuccess) return HQR_ERR_NOMEM;
-  if (cudaMalloc(&ws->stats, 2 * kNumTypes * sizeof(unsigned long long)) != cudaSuccess)
+  if (cudaMalloc(&ws->stats, 2 * kNumStats * sizeof(unsigned long long)) != cudaSuccess)
     return HQR_ERR_NOMEM;
   if (cudaMemset(ws->ctl, 0, kCtlWords * sizeof(unsigned)) != cudaSuccess) return HQR_ERR_CUDA;
   ws->cap_ids = n_ids;
@@ -125,7 +125,7 @@ static int run_dag(DagParams& p, DagWorkspace* ws, const Geometry& g, cudaStream
   // error word is kept (cleared by dag_status) so a failure is never lost.
   cudaError_t e0 = cudaMemsetAsync(ws->ctl, 0, kErr * sizeof(unsigned), stream);
   if (e0 == cudaSuccess)
-    e0 = cudaMemsetAsync(ws->stats, 0, 2 * kNumTypes * sizeof(unsigned long long), stream);
+    e0 = cudaMemsetAsync(ws->stats, 0, 2 * kNumStats * sizeof(unsigned long long), stream);
   if (e0 != cudaSuccess) return record_cuda_error(e0, "DAG workspace reset");
   const int blocks = (p.n_ids + 255) / 256;
   dag_init_kernel<<<blocks, 256, 0, stream>>>(p);
@@ -246,7 +246,7 @@ size_t factor_task_ids(const Geometry& g) {
 int launch_factor_external(const Geometry& g, const ExternalScratch& x, double* dA, double* dTAU,
                            long long timeout_ns, cudaStream_t stream) {
   static_assert(kExternalCtlBytes == kCtlWords * sizeof(unsigned), "control words");
-  static_assert(kExternalStatsBytes == 2 * kNumTypes * sizeof(unsigned long long), "stats");
+  static_assert(kExternalStatsBytes == 2 * kNumStats * sizeof(unsigned long long), "stats");
   DagParams p{};
   p.mode = kModeFactor;
   p.MT = g.MT;
@@ -317,9 +317,9 @@ int dag_status(DagWorkspace* ws, cudaStream_t stream) {
   return HQR_OK;
 }
 
-int dag_stats(DagWorkspace* ws, unsigned long long out[12], cudaStream_t stream) {
+int dag_stats(DagWorkspace* ws, unsigned long long out[14], cudaStream_t stream) {
   if (cudaStreamSynchronize(stream) != cudaSuccess) return HQR_ERR_CUDA;
-  if (cudaMemcpy(out, ws->stats, 12 * sizeof(unsigned long long), cudaMemcpyDeviceToHost) !=
+  if (cudaMemcpy(out, ws->stats, 14 * sizeof(unsigned long long), cudaMemcpyDeviceToHost) !=
       cudaSuccess)
     return HQR_ERR_CUDA;
   return HQR_OK;

@@ -46,6 +46,9 @@ enum DagMode : int {
 enum TaskType : int {
   kGEQRT = 0, kTSQRT = 1, kLARFB = 2, kSSRFB = 3, kTBUILD = 4, kOZPREP = 5, kNumTypes = 6
 };
+// Statistics slots: one per task type, then the scheduler's own time (thread
+// 0 of each CTA: popping the next task and releasing the dependents).
+constexpr int kStatSched = kNumTypes, kNumStats = kNumTypes + 1;
 
 // Control words of the scheduler (one cache line each is not needed: the
 // counters are touched once per task).
@@ -156,9 +159,17 @@ __device__ __forceinline__ void push_ready(const DagParams& p, int id) {
   }
 }
 
-__device__ __forceinline__ void release(const DagParams& p, int id) {
-  __threadfence();
-  if (atomicSub(p.cnt + id, 1) == 1) push_ready(p, id);
+// One input of task `id` is available (the releasing task's writes were fenced
+// before).  A task that becomes ready is queued, or, when `keep` is given and
+// still empty and the task is not on the high-priority queue, handed back to
+// the caller to run next (a continuation: no queue round trip).
+__device__ __forceinline__ void release(const DagParams& p, int id, int* keep = nullptr) {
+  if (atomicSub(p.cnt + id, 1) == 1) {
+    if (keep && *keep < 0 && !is_high_priority(p, id))
+      *keep = id;
+    else
+      push_ready(p, id);
+  }
 }
 
 // Wait (bounded) until slot of queue q has been written; returns the id or -1.
@@ -254,7 +265,8 @@ __global__ void dag_seed_kernel(DagParams p) {
 }
 
 // --- releases after a task ---------------------------------------------------------
-__device__ void release_dependents(const DagParams& p, const TaskDesc& t) {
+// keep: receives at most one ready low-priority dependent to run next.
+__device__ void release_dependents(const DagParams& p, const TaskDesc& t, int* keep) {
   if (t.type == kGEQRT || t.type == kTSQRT || t.type == kTBUILD || t.type == kOZPREP) {
     const bool feeds_prep = (t.type == kGEQRT || t.type == kTSQRT) && p.prep;
     if (feeds_prep) {
@@ -271,18 +283,18 @@ __device__ void release_dependents(const DagParams& p, const TaskDesc& t) {
   if (p.mode == kModeBuildQ) {
     // the chain runs from the bottom tile up to the LARFB; the step before
     // (i - 1) next writes tile (k, j), which this task wrote last
-    if (t.k - 1 >= t.i) release(p, update_id(p, t.i, t.j, t.k - 1, t.c));
-    if (t.i >= 1) release(p, update_id(p, t.i - 1, t.j, t.k, t.c));
+    if (t.k - 1 >= t.i) release(p, update_id(p, t.i, t.j, t.k - 1, t.c), keep);
+    if (t.i >= 1) release(p, update_id(p, t.i - 1, t.j, t.k, t.c), keep);
     return;
   }
   // LARFB / SSRFB: LIN to the next task of this column chain
-  if (t.k + 1 < p.MT) release(p, update_id(p, t.i, t.j, t.k + 1, t.c));
+  if (t.k + 1 < p.MT) release(p, update_id(p, t.i, t.j, t.k + 1, t.c), keep);
   // MEM to the next step (only SSRFB: LARFB's tile row is final)
   if (t.type == kSSRFB && t.i + 1 < p.steps) {
     if (p.mode == kModeFactor && t.j == t.i + 1)
       release(p, panel_id(p, t.i + 1, t.k));
     else
-      release(p, update_id(p, t.i + 1, t.j, t.k, t.c));
+      release(p, update_id(p, t.i + 1, t.j, t.k, t.c), keep);
   }
 }
 
@@ -315,8 +327,8 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
   __shared__ uint32_t s_tmem;
   const int NB = p.sh.NB;
   const size_t tsz = (size_t)NB * NB;
-  unsigned long long local_cnt[kNumTypes] = {0, 0, 0, 0, 0, 0};
-  unsigned long long local_cyc[kNumTypes] = {0, 0, 0, 0, 0, 0};
+  unsigned long long local_cnt[kNumStats] = {0, 0, 0, 0, 0, 0, 0};
+  unsigned long long local_cyc[kNumStats] = {0, 0, 0, 0, 0, 0, 0};
   if (OZ) {
     // the whole TMEM of this SM (one CTA per SM): 8 t-group accumulators x 64 columns
     if ((threadIdx.x >> 5) == 0) oz::tmem_alloc(&s_tmem, 512);
@@ -324,14 +336,29 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
     __syncthreads();
     oz::tc_fence_after();
   }
+  int next = -1;   // thread 0: a continuation kept from the last release
   for (;;) {
-    if (threadIdx.x == 0) s_id = pop_task(p);
+    const long long cp = clock64();
+    if (threadIdx.x == 0) {
+      // A kept continuation runs next unless a high-priority task is waiting:
+      // then it goes to the queue like any other ready task.
+      volatile unsigned* ctl = p.ctl;
+      if (next >= 0 && ctl[kErr] == 0u && ctl[kHiHead] >= ctl[kHiTail]) {
+        __threadfence();   // acquire: the other producers' tile writes are visible
+        s_id = next;
+      } else {
+        if (next >= 0) push_ready(p, next);
+        s_id = pop_task(p);
+      }
+      next = -1;
+    }
     __syncthreads();
     const int id = s_id;
     __syncthreads();
     if (id < 0) break;
     const TaskDesc t = decode(p, id);
     const long long c0 = clock64();
+    if (threadIdx.x == 0) local_cyc[kStatSched] += (unsigned long long)(c0 - cp);
     switch (t.type) {
       case kGEQRT: {
         const size_t o = tile_off(t.i, t.i, p.MT, NB);
@@ -396,14 +423,17 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
     __syncthreads();
     if (threadIdx.x == 0) {
       local_cnt[t.type]++;
-      local_cyc[t.type] += (unsigned long long)(clock64() - c0);
-      release_dependents(p, t);
+      const long long c1 = clock64();
+      local_cyc[t.type] += (unsigned long long)(c1 - c0);
+      release_dependents(p, t, &next);
       __threadfence();
       atomicAdd(p.ctl + kDone, 1u);
+      local_cnt[kStatSched]++;
+      local_cyc[kStatSched] += (unsigned long long)(clock64() - c1);
     }
   }
   if (threadIdx.x == 0 && p.stats) {
-    for (int ty = 0; ty < kNumTypes; ty++) {
+    for (int ty = 0; ty < kNumStats; ty++) {
       if (local_cnt[ty]) {
         atomicAdd(p.stats + 2 * ty, local_cnt[ty]);
         atomicAdd(p.stats + 2 * ty + 1, local_cyc[ty]);

@@ -75,7 +75,7 @@ struct ExternalScratch {
   unsigned long long* stats;     // 10 counters, zeroed by the caller
 };
 constexpr int kExternalCtlBytes = 8 * 4;
-constexpr int kExternalStatsBytes = 12 * 8;
+constexpr int kExternalStatsBytes = 14 * 8;
 // Number of task ids of the factorization DAG (size of cnt / qhi / qlo).
 size_t factor_task_ids(const Geometry& g);
 // Enqueue the factorization DAG on caller-supplied scratch.
@@ -85,7 +85,7 @@ int launch_factor_external(const Geometry& g, const ExternalScratch& x, double* 
 int external_status(const ExternalScratch& x, cudaStream_t stream);
 // Read and clear the scheduler's error word (synchronises `stream`).
 int dag_status(DagWorkspace* ws, cudaStream_t stream);
-int dag_stats(DagWorkspace* ws, unsigned long long out[12], cudaStream_t stream);
+int dag_stats(DagWorkspace* ws, unsigned long long out[14], cudaStream_t stream);
 int dag_sm_count();
 
 // Utility kernels (hqr_util.cu)

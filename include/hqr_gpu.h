@@ -43,10 +43,12 @@ typedef struct hqr_plan hqr_plan_t;
 
 /* Per-task-type execution counters of the last DAG run (device clock cycles
  * summed over CTAs).  Index: 0 GEQRT, 1 TSQRT, 2 LARFB, 3 SSRFB, 4 T-build,
- * 5 split-precision panel preparation (full T + operand slices). */
+ * 5 split-precision panel preparation (full T + operand slices), 6 the
+ * scheduler itself (thread 0 of each CTA popping tasks and releasing their
+ * dependents; count = tasks). */
 typedef struct {
-    unsigned long long count[6];
-    unsigned long long cycles[6];
+    unsigned long long count[7];
+    unsigned long long cycles[7];
 } hqr_stats_t;
 
 const char *hqr_status_string(int status);
