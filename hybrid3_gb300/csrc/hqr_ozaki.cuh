@@ -21,11 +21,10 @@
 //     products with the top digit are at most 2^13);
 //   * the 8 t-group accumulators (8 x 64 TMEM columns = the whole TMEM) are
 //     recombined exactly in 64-bit integers (two Horner chains in base 2^8,
-//     V = hi 2^32 + lo, up to 76 bits), shifted right only as far as V's bit
-//     length requires to fit 61 bits, and turned into FP64 by integer
-//     operations on the IEEE 754 encoding: the result is V rounded once (to
-//     within 2^-61).  The dropped products weigh < 2^-58 of
-//     rowmax(X) * colmax(Y) * K.
+//     V = hi 2^32 + lo, up to 77 bits), shifted right only as far as V's bit
+//     length requires to fit 63 bits, rounding to odd, and converted to FP64
+//     with integer operations: the result is V correctly rounded, once.  The
+//     dropped products weigh < 2^-58 of rowmax(X) * colmax(Y) * K.
 //
 // The left operands are sliced once per panel tile into HBM, already in the
 // tcgen05 K-major core-matrix layout, so each 16-deep K chunk of all 8 slices
@@ -53,7 +52,8 @@ constexpr int kS = 8;              // digits (slices) per element
 constexpr int kGroups = 8;         // t-group accumulators: t = p + q in [0, 7]
 constexpr int kExpBias = 1089;     // biased exponent of the scale of V = hi 2^32 + lo: Ea + Eb - kExpBias
 constexpr int kDC = 8;             // accumulator columns recombined per epilogue pass (tmem_ld_groups)
-constexpr int kLdY = kK + 1;       // leading dimension of the staged right operand
+constexpr int kLdY = kK + 2;       // leading dimension of the staged right operand (16-byte columns)
+constexpr int kLdT = kK + 1;       // leading dimension of a staged 128 x 128 tile
 constexpr int kSliceABytes = kM * kKC * 2;              // 4 KiB
 constexpr int kSliceBBytes = kN * kKC * 2;              // 2 KiB
 constexpr int kAChunkBytes = kS * kSliceABytes;         // 32 KiB: all slices of one K chunk
@@ -332,8 +332,7 @@ __device__ __forceinline__ void stage_y(Ctx& c, const double* Y, int ldy, int un
       v.x = (r > gc) ? v.x : (r == gc ? 1.0 : 0.0);
       v.y = (r + 1 > gc) ? v.y : (r + 1 == gc ? 1.0 : 0.0);
     }
-    c.sY[col * kLdY + r] = v.x;
-    c.sY[col * kLdY + r + 1] = v.y;
+    *reinterpret_cast<double2*>(c.sY + col * kLdY + r) = v;
   }
   __syncthreads();
   y_exponents(c);
@@ -344,10 +343,14 @@ __device__ __forceinline__ void stage_y(Ctx& c, const double* Y, int ldy, int un
 __device__ __forceinline__ void slice_b_quad(Ctx& c, uint8_t* stage, int g, int k0) {
   const int col = g >> 2, q = g & 3;
   const int E = c.sEb[c.yb * kN + col];
-  const double* y = c.sY + col * kLdY + k0 + 4 * q;
+  // two 16-byte loads: conflict-free (a quarter warp covers all 8 16-byte bank groups)
+  const double2* y = reinterpret_cast<const double2*>(c.sY + col * kLdY + k0 + 4 * q);
+  const double2 y01 = y[0], y23 = y[1];
   float d[4][kS];
-#pragma unroll
-  for (int i = 0; i < 4; i++) digits(fixed_of(y[i], E), d[i]);
+  digits(fixed_of(y01.x, E), d[0]);
+  digits(fixed_of(y01.y, E), d[1]);
+  digits(fixed_of(y23.x, E), d[2]);
+  digits(fixed_of(y23.y, E), d[3]);
   const int off = core_off(col, 4 * q);
 #pragma unroll
   for (int p = 0; p < kS; p++) {
@@ -470,26 +473,60 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
   return ok;
 }
 
-// X * 2^(se - 1023) as binary64, rounded to nearest even, built branch-free
-// with integer operations from the IEEE 754 encoding (normalise |X|, round to
-// 53 bits, add the exponent).  The FP64 units of this part are scarce; the
-// epilogue keeps them for the one addition per element.  Range: results below
-// 2^-1022 flush to zero, results of 2^1024 and above saturate to +-inf (a
-// rounding carry out of the largest exponent lands on the inf encoding).
-__device__ __forceinline__ double scaled_i64(long long X, int se) {
-  const unsigned long long sign = (unsigned long long)X & (1ULL << 63);
-  const unsigned long long u0 = X < 0 ? 0ULL - (unsigned long long)X : (unsigned long long)X;
-  const int lz = __clzll((long long)u0);                       // 64 when X == 0
-  const unsigned long long u = u0 << (lz & 63);                // leading one at bit 63
-  const unsigned long long m = u >> 11;                        // 53 significant bits
-  const unsigned long long rb = (u >> 10) & 1ULL, sticky = (u & 0x3FFULL) != 0ULL;
-  const unsigned long long mr = m + (rb & (sticky | (m & 1ULL)));
-  const int e = se + 63 - lz;                                  // biased exponent before a carry
-  // m carries its leading one into the exponent field (and a rounding carry
-  // to 2^53 bumps the exponent once more, with a zero fraction)
-  const unsigned long long bits = ((unsigned long long)(e - 1) << 52) + mr;
-  const unsigned long long res = (e < 1 || X == 0) ? 0ULL : (e > 2046 ? 0x7FF0000000000000ULL : bits);
-  return __longlong_as_double((long long)(sign | res));
+// One output of a product from the words of its 8 t-group accumulators
+// (column i of acc: FP32 images of exact integers g_t, |g_t| <= t 2^21, g_0 <=
+// 2^19): V = sum_t g_t 2^(8 (7 - t)), |V| < 2^77, and the result V 2^k as
+// binary64, rounded once to nearest even.  Results below 2^-1022 flush to
+// zero, results of 2^1024 and above saturate to +-inf; valid == false gives 0.
+//  * g_0..g_2 (|g| <= 2^22) come from the FP32 adder: the encoding of
+//    g + 1.5 2^23 is g plus a constant (removed once, in the sum); the others
+//    from the conversion unit.
+//  * V = hi 2^32 + lo (64-bit Horner chains over t < 4 and t >= 4), then
+//    V = vh 2^32 + vl with vl the low 32 bits of lo.
+//  * X = V / 2^s rounded to odd (truncated, last bit set when a discarded bit
+//    is), s the smallest shift that leaves |X| <= 2^62: when s > 0, X keeps 62
+//    significant bits, so rounding X to 53 bits is the correct rounding of V
+//    (rounding to odd at >= 55 bits makes the second rounding innocuous).
+//  * |X| normalised, rounded to 53 bits and placed in the IEEE 754 encoding
+//    with integer operations: on this part the FP64 pipe (which also converts
+//    integers to binary64) is scarce, and the epilogue keeps it for the one
+//    addition per element.
+constexpr float kMagic = 12582912.0f;                                 // 1.5 2^23
+constexpr long long kMagicSum = 0x4B400000LL * (16777216LL + 65536LL + 256LL);
+__device__ __forceinline__ double recombine(const uint32_t (&acc)[kGroups][kDC], int i, int k,
+                                            bool valid) {
+  const long long b0 = __float_as_int(__uint_as_float(acc[0][i]) + kMagic);
+  const long long b1 = __float_as_int(__uint_as_float(acc[1][i]) + kMagic);
+  const long long b2 = __float_as_int(__uint_as_float(acc[2][i]) + kMagic);
+  const long long g3 = __float2int_rn(__uint_as_float(acc[3][i]));
+  const long long g4 = __float2int_rn(__uint_as_float(acc[4][i]));
+  const long long g5 = __float2int_rn(__uint_as_float(acc[5][i]));
+  const long long g6 = __float2int_rn(__uint_as_float(acc[6][i]));
+  const long long g7 = __float2int_rn(__uint_as_float(acc[7][i]));
+  const long long hi = b0 * 16777216LL + b1 * 65536LL + b2 * 256LL + (g3 - kMagicSum);
+  const long long lo = g4 * 16777216LL + g5 * 65536LL + g6 * 256LL + g7;
+  const long long vh = hi + (lo >> 32);                  // |vh| < 2^45
+  const uint32_t vl = (uint32_t)lo;
+  // s = bit length of |vh| (one's complement for negatives) beyond 30 bits, in [0, 15]
+  const uint32_t top = (uint32_t)((unsigned long long)(vh ^ (vh >> 63)) >> 30);
+  const int s = 32 - __clz((int)top);
+  const uint32_t sticky = (uint32_t)((unsigned long long)vl << (32 - s)) != 0u ? 1u : 0u;
+  const long long X =
+      (long long)(((unsigned long long)vh << (32 - s)) | (unsigned long long)((vl >> s) | sticky));
+  const unsigned long long sg = (unsigned long long)(X >> 63);
+  const unsigned long long ax = ((unsigned long long)X ^ sg) - sg;   // |X| <= 2^62
+  const int lz = __clzll((long long)ax);                 // 64 when X == 0
+  const unsigned long long u = ax << (lz & 63);          // leading one at bit 63
+  const unsigned long long m = u >> 11;                  // 53 significant bits
+  const uint32_t low = (uint32_t)u & 0x7FFu;             // round half to even on the 11 dropped bits
+  const unsigned long long mr = m + (((low + ((uint32_t)m & 1u)) > 0x400u) ? 1ULL : 0ULL);
+  const int e = k + s + 1023 + 63 - lz;                  // biased exponent before a rounding carry
+  // m carries its leading one into the exponent field (a rounding carry to
+  // 2^53 bumps the exponent once more, with a zero fraction)
+  const unsigned long long bits = mr + ((unsigned long long)(e - 1) << 52);
+  const unsigned long long res =
+      (!valid || ax == 0ULL || e < 1) ? 0ULL : (e > 2046 ? 0x7FF0000000000000ULL : bits);
+  return __longlong_as_double((long long)(res | (sg & 0x8000000000000000ULL)));
 }
 
 // Epilogue modes (R = the product just computed).
@@ -528,33 +565,13 @@ inline __device__ void drain(Ctx& c, const int* Ea, int mode, double* g, int ldg
     double mem[kDC];
 #pragma unroll
     for (int i = 0; i < kDC; i++) mem[i] = msrc ? ldg_cg(msrc + row + (size_t)(c0 + i) * mld) : 0.0;
-    long long hi[kDC], lo[kDC];
     uint32_t acc[kGroups][kDC];
     tmem_ld_groups(lane_addr + (uint32_t)c0, acc);
-    // Horner in base 2^8 over the groups, paired: |g_t| <= 2^21 (t + 1) (the
-    // two pairs with the top digit at half that), so g0 2^8 + g1 and
-    // g2 2^8 + g3 fit in 32 bits; the low groups need 64 bits.
-#pragma unroll
-    for (int i = 0; i < kDC; i++) {
-      int g[kGroups];
-#pragma unroll
-      for (int t = 0; t < kGroups; t++) g[t] = __float2int_rn(__uint_as_float(acc[t][i]));
-      const int a = g[0] * 256 + g[1], b = g[2] * 256 + g[3];
-      hi[i] = (long long)a * 65536 + b;
-      const long long c = (long long)g[4] * 256 + g[5], d = (long long)g[6] * 256 + g[7];
-      lo[i] = c * 65536 + d;
-    }
 #pragma unroll
     for (int i = 0; i < kDC; i++) {
       const int col = c0 + i;
-      // V = hi 2^32 + lo, |hi| < 2^44, |lo| < 2^48: exact when hi has at most
-      // 29 bits, else shifted right by its excess (lo rounded), |X| < 2^61 + 2^48
-      const long long h = hi[i];
-      const int bl = 64 - __clzll(h < 0 ? -h : h);
-      const int sh = bl > 29 ? bl - 29 : 0;
-      const long long X = (long long)((unsigned long long)h << (32 - sh)) + ((lo[i] + ((1LL << sh) >> 1)) >> sh);
       const int eb = c.sEb[c.yb * kN + col];
-      const double r = (ea > 0 && eb > 0) ? scaled_i64(X, ea + eb - kExpBias + sh) : 0.0;
+      const double r = recombine(acc, i, ea + eb - (kExpBias + 1023), ea > 0 && eb > 0);
       const size_t o = (size_t)col;
       double y = 0.0;
       if (mode == kEpiStore) {
@@ -636,7 +653,7 @@ inline __device__ void slice_left(const Acc& acc, uint8_t* dst, int* Ea, int* sE
 }
 
 // Accessor of a 128 x 128 column-major matrix S staged in shared memory with
-// leading dimension kLdY: X = S or X = S^T, with an element mask.
+// leading dimension kLdT: X = S or X = S^T, with an element mask.
 struct StagedAcc {
   const double* s;
   int rs, ks;   // X(r, k) = s[r * rs + k * ks]
@@ -649,7 +666,7 @@ struct StagedAcc {
   }
 };
 
-// Stage a 128 x 128 column-major tile (global, ld kK) in shared memory, ld kLdY.
+// Stage a 128 x 128 column-major tile (global, ld kK) in shared memory, ld kLdT.
 __device__ __forceinline__ void stage_tile(double* s, const double* src) {
   constexpr int kIter = kK * kK / 2 / kThreads;   // pairs per thread
 #pragma unroll 4
@@ -657,8 +674,8 @@ __device__ __forceinline__ void stage_tile(double* s, const double* src) {
     const int e = threadIdx.x + it * kThreads;
     const int col = e / (kK / 2), r = 2 * (e % (kK / 2));
     const double2 v = __ldcg(reinterpret_cast<const double2*>(src + (size_t)col * kK + r));
-    s[col * kLdY + r] = v.x;
-    s[col * kLdY + r + 1] = v.y;
+    s[col * kLdT + r] = v.x;
+    s[col * kLdT + r + 1] = v.y;
   }
   __syncthreads();
 }

@@ -73,11 +73,11 @@ inline __device__ bool task_ozprep(const double* V, const double* tau, double* G
   // 1. V^T and V from a shared-memory copy of the tile
   {
     double* sV = reinterpret_cast<double*>(sm);
-    int* sE = reinterpret_cast<int*>(sm + kLdY * kK * 8);
+    int* sE = reinterpret_cast<int*>(sm + kLdT * kK * 8);
     stage_tile(sV, V);
-    slice_left(StagedAcc{sV, kLdY, 1, unit ? kUnitUpper : kDense}, slices + kOzVT * ob,
+    slice_left(StagedAcc{sV, kLdT, 1, unit ? kUnitUpper : kDense}, slices + kOzVT * ob,
                exps + kOzVT * kK, sE);
-    slice_left(StagedAcc{sV, 1, kLdY, unit ? kUnitLower : kDense}, slices + kOzV * ob,
+    slice_left(StagedAcc{sV, 1, kLdT, unit ? kUnitLower : kDense}, slices + kOzV * ob,
                exps + kOzV * kK, sE);
   }
   // 2. G = V^T V on the tensor cores, by 64-column blocks, into G (global)

@@ -17,9 +17,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_ozaki_product(const double* X, 
   oz::tc_fence_after();
   {
     double* sX = reinterpret_cast<double*>(sm);
-    int* sE = reinterpret_cast<int*>(sm + oz::kLdY * oz::kK * 8);
+    int* sE = reinterpret_cast<int*>(sm + oz::kLdT * oz::kK * 8);
     oz::stage_tile(sX, X);
-    oz::slice_left(oz::StagedAcc{sX, 1, oz::kLdY, oz::kDense}, prep, exps, sE);
+    oz::slice_left(oz::StagedAcc{sX, 1, oz::kLdT, oz::kDense}, prep, exps, sE);
   }
   oz::Ctx c;
   oz::ctx_init(c, sm, s_tmem, err);
