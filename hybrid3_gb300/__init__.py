@@ -105,6 +105,7 @@ SIGNATURES = {
     "hqr_make_q": (_I, [_vp, _vp, _vp, _vp, _I, _vp]),
     "hqr_make_q_async": (_I, [_vp, _vp, _vp, _vp, _I, _vp]),
     "hqr_ormqr_t": (_I, [_vp, _vp, _vp, _vp, _I, _I, _vp]),
+    "hqr_lstsq": (_I, [_vp, _vp, _vp, _I, _I, _vp, _I, _I, _vp, _vp]),
     "hqr_dgemm_tn": (_I, [_L, _I, _vp, _vp, _vp, _vp]),
     "hqr_make_identity": (_I, [_L, _L, _I, _vp, _vp]),
     "hqr_fill_uniform": (_I, [_L, _L, _I, ctypes.c_uint64, _vp, _vp]),
@@ -186,6 +187,14 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+    def lstsq(self, dA, dB, nrhs, dX, refine_steps=1, ldb=None, ldx=None, stream=None):
+        """hqr_lstsq on device addresses (tile-layout A of this plan's shape,
+        column-major B and X); returns ||b - A x||_2 per right-hand side."""
+        res = (ctypes.c_double * nrhs)()
+        check(lib().hqr_lstsq(self.h, dA, dB, ldb or self.M, nrhs, dX, ldx or self.N, refine_steps,
+                              res, stream), "hqr_lstsq")
+        return list(res)
 
     def stats(self, stream=None):
         s = HqrStats()

@@ -5,6 +5,7 @@
 // in tile layout, void return, abort on error -- Hybrid_tile_QR.c:992-999 and
 // friends call MPI_Abort): each call stages its operands in device buffers
 // owned by the library, runs the tile DAG on the GPU and copies results back.
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -270,6 +271,66 @@ int hqr_ormqr_t(hqr_plan_t* plan, const double* dRY, const double* dTAU, double*
   TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, !use_plan_t,
                            g_timeout_ns, (cudaStream_t)stream, &plan->oz));
   return hqr_plan_status(plan, stream);
+}
+
+namespace {
+// Device workspace of one least-squares call, freed on every return path.
+struct LstsqWork {
+  double* Af = nullptr;   // the factored copy of A
+  double* tau = nullptr;
+  double* C = nullptr;    // right-hand sides / residuals in tile layout
+  double* R = nullptr;    // residual, column-major M x nrhs
+  double* nrm = nullptr;
+  ~LstsqWork() {
+    cudaFree(Af);
+    cudaFree(tau);
+    cudaFree(C);
+    cudaFree(R);
+    cudaFree(nrm);
+  }
+};
+int dmalloc(double** p, size_t n) {
+  return cudaMalloc(p, n * sizeof(double)) == cudaSuccess ? HQR_OK : HQR_ERR_NOMEM;
+}
+}  // namespace
+
+int hqr_lstsq(hqr_plan_t* plan, const double* dA, const double* dB, int ldb, int nrhs, double* dX,
+              int ldx, int refine_steps, double* resid, void* stream) {
+  if (!plan || !dA || !dB || !dX || nrhs <= 0 || refine_steps < 0) return HQR_ERR_INVALID;
+  const hqr::Geometry& g = plan->g;
+  if (g.M < g.N || ldb < g.M || ldx < g.N) return HQR_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int CT = (nrhs + g.NB - 1) / g.NB;
+  LstsqWork w;
+  TRY(dmalloc(&w.Af, (size_t)g.M * g.N));
+  TRY(dmalloc(&w.tau, tau_len(g)));
+  TRY(dmalloc(&w.C, (size_t)g.M * CT * g.NB));
+  TRY(dmalloc(&w.R, (size_t)g.M * nrhs));
+  TRY(dmalloc(&w.nrm, (size_t)nrhs));
+  TRY(cuda_rc(cudaMemcpyAsync(w.Af, dA, (size_t)g.M * g.N * sizeof(double), cudaMemcpyDeviceToDevice, s)));
+  TRY(hqr_geqrf(plan, w.Af, w.tau, stream));
+  for (int it = 0; it <= refine_steps; it++) {
+    if (it == 0) {
+      hqr::pack_rhs(dB, ldb, nrhs, w.C, g.M, g.NB, CT, s);
+    } else {
+      TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, w.R, g.M, nrhs, s));
+      hqr::pack_rhs(w.R, g.M, nrhs, w.C, g.M, g.NB, CT, s);
+    }
+    TRY(cuda_rc(cudaGetLastError()));
+    TRY(hqr_ormqr_t(plan, w.Af, w.tau, w.C, CT, 1, stream));
+    TRY(hqr::trsm_tiles(w.Af, g.M, g.N, g.NB, w.C, nrhs, s));
+    hqr::update_x(w.C, g.M, g.NB, g.N, nrhs, dX, ldx, it > 0, s);
+    TRY(cuda_rc(cudaGetLastError()));
+  }
+  if (resid) {
+    TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, w.R, g.M, nrhs, s));
+    hqr::col_norm2(w.R, g.M, g.M, nrhs, w.nrm, s);
+    TRY(cuda_rc(cudaMemcpyAsync(resid, w.nrm, (size_t)nrhs * sizeof(double), cudaMemcpyDeviceToHost, s)));
+  }
+  TRY(cuda_rc(cudaStreamSynchronize(s)));
+  if (resid)
+    for (int q = 0; q < nrhs; q++) resid[q] = sqrt(resid[q]);
+  return HQR_OK;
 }
 
 int hqr_dgemm_tn(long N, int NB, const double* dA, const double* dB, double* dC, void* stream) {

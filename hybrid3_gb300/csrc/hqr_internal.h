@@ -28,6 +28,18 @@ int record_cuda_error(cudaError_t e, const char* where);
 // and exit, or print and remember for hqr_last_error); returns rc.
 int report_error(const char* fn, int rc);
 
+// Least-squares helpers (hqr_lstsq.cu).  Right-hand sides: column-major
+// M x nrhs; C: tile layout with MT = M / NB tile rows and CT tile columns.
+void pack_rhs(const double* dB, long ldb, int nrhs, double* dC, long M, int NB, int CT, cudaStream_t s);
+void update_x(const double* dC, long M, int NB, long N, int nrhs, double* dX, long ldx, bool accumulate,
+              cudaStream_t s);
+int residual(const double* dA, long M, long N, int NB, const double* dX, long ldx, const double* dB,
+             long ldb, double* dR, long ldr, int nrhs, cudaStream_t s);
+void col_norm2(const double* dR, long M, long ldr, int nrhs, double* dOut, cudaStream_t s);
+// Back substitution R Y = C(1:N, :) in place (R: upper triangle of the
+// factored A's first N / NB tile rows).
+int trsm_tiles(const double* dRA, long M, long N, int NB, double* dC, int nrhs, cudaStream_t s);
+
 // Scheduler workspace (dependency counters, queues, control words, stats).
 struct DagWorkspace {
   int* cnt = nullptr;

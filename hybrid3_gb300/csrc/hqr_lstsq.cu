@@ -1,0 +1,238 @@
+// hqr_lstsq.cu -- device kernels of the least-squares solve (hqr_lstsq): the
+// right-hand sides in and out of the tile layout, the FP64 residual
+// r = b - A x on the original A, and the blocked back substitution with the R
+// of a tile QR.
+//
+// The reference has no solve (its driver stops at Q and R, main.c:145-258);
+// this is the first extension its callers need: x = R^-1 (Q^T b)(1:n), then
+// FP64 iterative refinement x += R^-1 (Q^T (b - A x))(1:n).
+#include "hqr_internal.h"
+
+namespace hqr {
+namespace {
+
+constexpr int kRhsChunk = 16;   // right-hand sides per thread pass
+constexpr int kRBlock = 32;     // columns of R staged per pass of the diagonal solve
+
+// C (tile layout of an M x CT*NB matrix, MT tile rows) <- B (column-major
+// M x nrhs, ld ldb), zero beyond column nrhs.
+__global__ void k_pack_rhs(const double* __restrict__ B, long ldb, int nrhs, double* __restrict__ C,
+                           long M, int MT, int NB, int CT) {
+  const long n = M * (long)CT * NB;
+  const long tile_elems = (long)NB * NB;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const long tile = e / tile_elems;
+    const int within = (int)(e - tile * tile_elems);
+    const long row = (tile % MT) * NB + within % NB;
+    const long col = (tile / MT) * NB + within / NB;
+    C[e] = col < nrhs ? B[row + col * ldb] : 0.0;
+  }
+}
+
+// X (column-major N x nrhs, ld ldx) <- Y or X + Y, Y = the first N rows of C
+// (tile layout, MT tile rows).
+__global__ void k_update_x(const double* __restrict__ C, int MT, int NB, long N, int nrhs,
+                           double* __restrict__ X, long ldx, int accumulate) {
+  const long n = N * (long)nrhs;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const long row = e % N, col = e / N;
+    const long off = ((row / NB) + (col / NB) * (long)MT) * NB * NB + (col % NB) * NB + row % NB;
+    const double y = C[off];
+    X[row + col * ldx] = accumulate ? X[row + col * ldx] + y : y;
+  }
+}
+
+// R = B - A X in FP64.  A: tile layout M x N; X: column-major N x nrhs;
+// B, R: column-major M x nrhs.  Block (ti, q0 / kRhsChunk): tile row ti,
+// right-hand sides q0..q0+15; thread r = row r of the tile row (NB threads).
+__global__ void k_residual(const double* __restrict__ A, long M, long N, int NB,
+                           const double* __restrict__ X, long ldx, const double* __restrict__ B,
+                           long ldb, double* __restrict__ R, long ldr, int nrhs) {
+  extern __shared__ double sx[];   // NB x kRhsChunk slice of X
+  const int MT = (int)(M / NB), NT = (int)(N / NB);
+  const int ti = blockIdx.x, q0 = blockIdx.y * kRhsChunk;
+  const int r = threadIdx.x;
+  double acc[kRhsChunk];
+#pragma unroll
+  for (int q = 0; q < kRhsChunk; q++) acc[q] = 0.0;
+  for (int tj = 0; tj < NT; tj++) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < NB * kRhsChunk; e += blockDim.x) {
+      const int k = e % NB, q = e / NB;
+      sx[e] = (q0 + q < nrhs) ? X[(long)tj * NB + k + (long)(q0 + q) * ldx] : 0.0;
+    }
+    __syncthreads();
+    const double* At = A + ((long)ti + (long)tj * MT) * NB * NB;
+#pragma unroll 4
+    for (int k = 0; k < NB; k++) {
+      const double a = __ldcs(At + r + (long)k * NB);
+#pragma unroll
+      for (int q = 0; q < kRhsChunk; q++) acc[q] = fma(a, sx[k + q * NB], acc[q]);
+    }
+  }
+  const long row = (long)ti * NB + r;
+#pragma unroll
+  for (int q = 0; q < kRhsChunk; q++)
+    if (q0 + q < nrhs) R[row + (long)(q0 + q) * ldr] = B[row + (long)(q0 + q) * ldb] - acc[q];
+}
+
+// ||R(:, q)||_2^2 of each column (column-major M x nrhs, ld ldr): one block per
+// column, fixed summation order.
+__global__ void k_col_norm2(const double* __restrict__ R, long M, long ldr, double* __restrict__ out) {
+  __shared__ double red[32];
+  const double* c = R + (long)blockIdx.x * ldr;
+  double s = 0.0;
+  for (long i = threadIdx.x; i < M; i += blockDim.x) s = fma(c[i], c[i], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+    out[blockIdx.x] = t;
+  }
+}
+
+// One step of the back substitution R Y = C over the first NT tile rows of C
+// (tile layout, MT tile rows; tile column blockIdx.y holds ncol(y) valid
+// columns).  For i < NT, block k < i first updates C_k -= R_ki Y_i (Y_i =
+// tile row i of C, solved by the step before); then block k = i - 1 solves
+// R_kk Y_k = C_k in place.  i = NT: only the diagonal solve of tile row NT-1.
+// RA: the factored A, R in the upper triangle of its tiles (k <= i).
+// Thread r owns row r of the tile (NB threads).
+__global__ void k_trsm_step(const double* __restrict__ RA, int MT, int NB, double* __restrict__ C,
+                            int i, int NT, int nrhs) {
+  extern __shared__ double sm[];   // NB x kRhsChunk right operand / NB x kRBlock R columns + 2 x kRhsChunk
+  const int k = (i < NT) ? (int)blockIdx.x : NT - 1;
+  const int tj = blockIdx.y;
+  const int ncol = min(NB, nrhs - tj * NB);
+  const int r = threadIdx.x;
+  const long tile = (long)NB * NB;
+  double* Ck = C + ((long)k + (long)tj * MT) * tile;
+  if (i < NT) {
+    const double* Rki = RA + ((long)k + (long)i * MT) * tile;
+    const double* Yi = C + ((long)i + (long)tj * MT) * tile;
+    for (int c0 = 0; c0 < ncol; c0 += kRhsChunk) {
+      const int nq = min(kRhsChunk, ncol - c0);
+      __syncthreads();
+      for (int e = threadIdx.x; e < NB * kRhsChunk; e += blockDim.x) {
+        const int kk = e % NB, q = e / NB;
+        sm[e] = q < nq ? Yi[kk + (long)(c0 + q) * NB] : 0.0;
+      }
+      __syncthreads();
+      double acc[kRhsChunk];
+#pragma unroll
+      for (int q = 0; q < kRhsChunk; q++) acc[q] = 0.0;
+#pragma unroll 4
+      for (int kk = 0; kk < NB; kk++) {
+        const double a = Rki[r + (long)kk * NB];
+#pragma unroll
+        for (int q = 0; q < kRhsChunk; q++) acc[q] = fma(a, sm[kk + q * NB], acc[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < kRhsChunk; q++)
+        if (q < nq) Ck[r + (long)(c0 + q) * NB] -= acc[q];
+    }
+  }
+  if (k != ((i < NT) ? i - 1 : NT - 1) || k < 0) return;
+  // R_kk Y = C_k: rows from the bottom; thread r keeps its row's values in
+  // registers, the solved value of row j is broadcast through a double buffer
+  // (one barrier per row), R's columns are staged kRBlock at a time.
+  __syncthreads();
+  const double* Rkk = RA + ((long)k + (long)k * MT) * tile;
+  double* sR = sm;                          // NB x kRBlock
+  double* sy = sm + (long)NB * kRBlock;     // 2 x kRhsChunk
+  for (int c0 = 0; c0 < ncol; c0 += kRhsChunk) {
+    const int nq = min(kRhsChunk, ncol - c0);
+    double v[kRhsChunk];
+#pragma unroll
+    for (int q = 0; q < kRhsChunk; q++) v[q] = q < nq ? Ck[r + (long)(c0 + q) * NB] : 0.0;
+    int buf = 0;
+    for (int jend = NB; jend > 0; jend -= kRBlock) {
+      const int jb = jend > kRBlock ? jend - kRBlock : 0;
+      __syncthreads();
+      for (int e = threadIdx.x; e < NB * (jend - jb); e += blockDim.x) {
+        const int rr = e % NB, cc = e / NB;
+        sR[e] = Rkk[rr + (long)(jb + cc) * NB];
+      }
+      __syncthreads();
+      for (int j = jend - 1; j >= jb; j--) {
+        if (r == j) {
+          const double d = sR[j + (j - jb) * NB];
+#pragma unroll
+          for (int q = 0; q < kRhsChunk; q++) {
+            v[q] = v[q] / d;
+            sy[buf * kRhsChunk + q] = v[q];
+          }
+        }
+        __syncthreads();
+        if (r < j) {
+          const double rj = sR[r + (j - jb) * NB];
+#pragma unroll
+          for (int q = 0; q < kRhsChunk; q++) v[q] = fma(-rj, sy[buf * kRhsChunk + q], v[q]);
+        }
+        buf ^= 1;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kRhsChunk; q++)
+      if (q < nq) Ck[r + (long)(c0 + q) * NB] = v[q];
+  }
+}
+
+int blocks_for(long n) {
+  long b = (n + 255) / 256;
+  return (int)(b < 1 ? 1 : (b > 4 * 152 ? 4 * 152 : b));
+}
+
+}  // namespace
+
+void pack_rhs(const double* dB, long ldb, int nrhs, double* dC, long M, int NB, int CT, cudaStream_t s) {
+  k_pack_rhs<<<blocks_for(M * (long)CT * NB), 256, 0, s>>>(dB, ldb, nrhs, dC, M, (int)(M / NB), NB, CT);
+}
+
+void update_x(const double* dC, long M, int NB, long N, int nrhs, double* dX, long ldx, bool accumulate,
+              cudaStream_t s) {
+  k_update_x<<<blocks_for(N * (long)nrhs), 256, 0, s>>>(dC, (int)(M / NB), NB, N, nrhs, dX, ldx,
+                                                         accumulate ? 1 : 0);
+}
+
+int residual(const double* dA, long M, long N, int NB, const double* dX, long ldx, const double* dB,
+             long ldb, double* dR, long ldr, int nrhs, cudaStream_t s) {
+  const dim3 grid((unsigned)(M / NB), (unsigned)((nrhs + kRhsChunk - 1) / kRhsChunk));
+  const size_t smem = (size_t)NB * kRhsChunk * sizeof(double);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_residual, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(k_residual)");
+  }
+  k_residual<<<grid, NB, smem, s>>>(dA, M, N, NB, dX, ldx, dB, ldb, dR, ldr, nrhs);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? HQR_OK : record_cuda_error(e, "k_residual launch");
+}
+
+void col_norm2(const double* dR, long M, long ldr, int nrhs, double* dOut, cudaStream_t s) {
+  k_col_norm2<<<nrhs, 256, 0, s>>>(dR, M, ldr, dOut);
+}
+
+size_t trsm_smem_bytes(int NB) {
+  const size_t a = (size_t)NB * kRhsChunk, b = (size_t)NB * kRBlock + 2 * kRhsChunk;
+  return (a > b ? a : b) * sizeof(double);
+}
+
+int trsm_tiles(const double* dRA, long M, long N, int NB, double* dC, int nrhs, cudaStream_t s) {
+  const int MT = (int)(M / NB), NT = (int)(N / NB);
+  const int CT = (nrhs + NB - 1) / NB;
+  const size_t smem = trsm_smem_bytes(NB);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_trsm_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(k_trsm_step)");
+  }
+  for (int i = NT; i >= 1; i--) {
+    const dim3 grid((unsigned)(i < NT ? i : 1), (unsigned)CT);
+    k_trsm_step<<<grid, NB, smem, s>>>(dRA, MT, NB, dC, i, NT, nrhs);
+  }
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? HQR_OK : record_cuda_error(e, "k_trsm_step launch");
+}
+
+}  // namespace hqr

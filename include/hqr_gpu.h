@@ -108,6 +108,20 @@ int hqr_make_q_async(hqr_plan_t *plan, double *dQ, double *dRY, const double *dT
 int hqr_ormqr_t(hqr_plan_t *plan, const double *dRY, const double *dTAU, double *dC, int CT,
                 int use_plan_t, void *stream);
 
+/* No counterpart in the reference (its driver stops at Q and R).  Least
+ * squares min ||A x - b||_2 for a full-rank dA (M >= N, tile layout of this
+ * plan's shape, device, left unmodified) and nrhs right-hand sides dB
+ * (column-major M x nrhs, ld ldb >= M, device): a copy of A is factored on
+ * this plan (its precision), c = Q^T b runs on the device DAG (dormqr), R x =
+ * c(1:N) is solved by blocked back substitution, then refine_steps steps of
+ * FP64 iterative refinement: r = b - A x with the original A in FP64, x +=
+ * R^-1 (Q^T r)(1:N).  dX: column-major N x nrhs (ld ldx >= N, device).
+ * resid (host, nrhs doubles, may be NULL) receives ||b - A x||_2 of the
+ * returned x per right-hand side.  Allocates its workspace (the copy of A,
+ * TAU, the packed right-hand sides); synchronous. */
+int hqr_lstsq(hqr_plan_t *plan, const double *dA, const double *dB, int ldb, int nrhs, double *dX,
+              int ldx, int refine_steps, double *resid, void *stream);
+
 /* Tile-wise C = A^T B of square tiled matrices (Hybrid_dgemm). */
 int hqr_dgemm_tn(long N, int NB, const double *dA, const double *dB, double *dC, void *stream);
 /* Identity in tile layout (Hybrid_make_I). */

@@ -176,6 +176,32 @@ def dgemm_tn(A: np.ndarray, B: np.ndarray, M: int, N: int, NB: int):
     return C
 
 
+def lstsq(A_tiles: np.ndarray, B: np.ndarray, M: int, N: int, NB: int, IB: int,
+          refine_steps: int = 1) -> np.ndarray:
+    """The least-squares solve of hqr_lstsq restated on the CPU: the oracle's
+    tile QR of A, c = Q^T b by its dormqr, back substitution with R, then
+    ``refine_steps`` FP64 refinement steps x += R^-1 (Q^T (b - A x))(1:N).
+    B: (M, nrhs) array; returns x as an (N, nrhs) array."""
+    from scipy.linalg import solve_triangular
+    B = np.asarray(B, dtype=np.float64).reshape(M, -1)
+    nrhs = B.shape[1]
+    CT = (nrhs + NB - 1) // NB
+    A2d = from_tiles(A_tiles, M, N, NB)
+    RY, TAU = tile_qr(A_tiles, M, N, NB, IB)
+    R = np.triu(from_tiles(RY, M, N, NB)[:N, :N])
+
+    def solve(rhs):
+        pad = np.zeros((M, CT * NB))
+        pad[:, :nrhs] = rhs
+        c = from_tiles(dormqr(RY, TAU, to_tiles(pad, NB), M, N, NB, CT), M, CT * NB, NB)
+        return solve_triangular(R, c[:N, :nrhs], lower=False)
+
+    x = solve(B)
+    for _ in range(refine_steps):
+        x = x + solve(B - A2d @ x)
+    return x
+
+
 def mat_make(M: int, N: int, NB: int, seed: int) -> np.ndarray:
     A = np.zeros(M * N)
     lib().orc_mat_fill(M, N, NB, ptr(A), seed, 0)
