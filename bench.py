@@ -370,13 +370,97 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
             "api": "Hybrid_tile_QR + Hybrid_make_Q (pinned host arrays)"}
 
 
+def lstsq_flops(m: int, n: int, nrhs: int, refine: int) -> float:
+    """Algorithmic flops of hqr_lstsq: QR, then per solve Q^T b (4mn - 2n^2 per
+    right-hand side) and back substitution (n^2), per refinement step a
+    residual (2mn)."""
+    per_solve = (4.0 * m * n - 2.0 * n * n + n * n) * nrhs
+    return qr_flops(m, n) + (refine + 1) * per_solve + refine * 2.0 * m * n * nrhs
+
+
+def run_lstsq(H, torch, L, args):
+    """Least squares min ||A x - b|| through hqr_lstsq: A (m x n) = U diag(sigma)
+    V^T with Haar U, V and sigma geometric from 1 to 1/kappa, x_true ~ N(0,1),
+    b = A x_true + 1e-8 N(0,1), nrhs right-hand sides; inputs generated with
+    torch on the device, outside the timed region.  Timed: whole hqr_lstsq
+    calls (copy of A, QR, Q^T b, back substitution, refinement).  Checked
+    against an FP64 least-squares solution of the same problem
+    (torch.linalg.lstsq, check only) and against x_true."""
+    m, n, nrhs, NB, IB = args.m, args.n, args.nrhs, args.nb, args.ib
+    kappa = args.kappa if args.kappa is not None else 1e3
+    prec = H.HQR_PREC_OZAKI if args.precision == "split" else H.HQR_PREC_FP64
+    f64 = torch.float64
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(20151130)
+
+    def haar(r, c):
+        Z = torch.randn(r, c, dtype=f64, device="cuda", generator=gen)
+        Q, R = torch.linalg.qr(Z)
+        Q *= torch.sign(torch.diagonal(R))
+        return Q
+
+    U = haar(m, n)
+    U *= kappa ** (-torch.arange(n, dtype=f64, device="cuda") / (n - 1))
+    A = U @ haar(n, n).T
+    del U
+    x_true = torch.randn(n, nrhs, dtype=f64, device="cuda", generator=gen)
+    b = A @ x_true + 1e-8 * torch.randn(m, nrhs, dtype=f64, device="cuda", generator=gen)
+    cm = A.T.contiguous()                       # column-major storage of A
+    dA = torch.empty(m * n, dtype=f64, device="cuda")
+    H.check(L.hqr_colmajor_to_tiles(m, n, NB, cm.data_ptr(), dA.data_ptr(), None), "to tiles")
+    del cm
+    dB = b.T.contiguous()                       # column-major m x nrhs
+    dX = torch.zeros(nrhs, n, dtype=f64, device="cuda")   # column-major n x nrhs
+    plan = H.Plan(m, n, NB, IB, prec)
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        plan.lstsq(dA.data_ptr(), dB.data_ptr(), nrhs, dX.data_ptr(), refine_steps=args.refine)
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        res = plan.lstsq(dA.data_ptr(), dB.data_ptr(), nrhs, dX.data_ptr(), refine_steps=args.refine)
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    elapsed = e0.elapsed_time(e1) / 1e3 / args.steps
+    plan.close()
+    x = dX.T
+    x_ref = torch.linalg.lstsq(A, b).solution
+    rel = lambda a, r: float(torch.linalg.norm(a - r) / torch.linalg.norm(r))
+    flops = lstsq_flops(m, n, nrhs, args.refine)
+    line = {
+        "metric": "least-squares solve TFLOP/s (QR + Q^T b + back substitution + FP64 refinement)",
+        "value": round(flops / elapsed / 1e12, 6), "unit": "TFLOP/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * elapsed, 3),
+        "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"least squares, A {m}x{n} = U diag(sigma) V^T (Haar U, V, sigma "
+                               f"geometric 1..1/kappa), kappa={kappa:g}, {nrhs} right-hand sides, "
+                               f"b = A x_true + 1e-8 noise",
+                   "m": m, "n": n, "nrhs": nrhs, "kappa": kappa, "NB": NB, "IB": IB,
+                   "refine_steps": args.refine,
+                   "precision": ("split (Ozaki BF16 slices on tcgen05, FP64 panels)"
+                                 if args.precision == "split" else "fp64 (plain)")},
+        "accuracy": {"forward_error_vs_fp64_lstsq": rel(x, x_ref),
+                     "forward_error_vs_x_true": rel(x, x_true),
+                     "fp64_lstsq_error_vs_x_true": rel(x_ref, x_true),
+                     "residual_norm_max": max(res),
+                     "fp64_lstsq_residual_norm_max": float(torch.linalg.norm(b - A @ x_ref, dim=0).max())},
+        "algorithmic_flops": flops,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=16384)
+    ap.add_argument("--n", type=int, default=None, help="order (default 16384; 8192 columns with --lstsq)")
     ap.add_argument("--precision", default="split", choices=["split", "fp64"])
     ap.add_argument("--nb", type=int, default=None, help="tile order (default 128 split, 256 fp64)")
     ap.add_argument("--ib", type=int, default=32)
@@ -389,7 +473,14 @@ def main():
     ap.add_argument("--kappa", type=float, default=None,
                     help="graded input A = U diag(sigma) V^T with condition number kappa "
                          "(accuracy configuration); default: uniform[-1,1)")
+    ap.add_argument("--lstsq", action="store_true",
+                    help="least-squares workload through hqr_lstsq instead of QR + make_Q")
+    ap.add_argument("--m", type=int, default=32768, help="rows of A for --lstsq")
+    ap.add_argument("--nrhs", type=int, default=16, help="right-hand sides for --lstsq")
+    ap.add_argument("--refine", type=int, default=1, help="FP64 refinement steps for --lstsq")
     args = ap.parse_args()
+    if args.n is None:
+        args.n = 8192 if args.lstsq else 16384
     if args.nb is None:
         args.nb = 128 if args.precision == "split" else 256
 
@@ -413,6 +504,10 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     L = H.lib()
     L.hqr_set_error_mode(H.HQR_ERRORS_RETURN)
+    if args.lstsq:
+        if rank == 0:
+            run_lstsq(H, torch, L, args)
+        return
     n, NB, IB = args.n, args.nb, args.ib
 
     peak_fp64 = L.hqr_fp64_peak_tflops(None)
