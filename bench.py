@@ -343,17 +343,25 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
     pa = ctypes.cast(hA.data_ptr(), DP)
     pq = ctypes.cast(hQ.data_ptr(), DP)
     pt = ctypes.cast(hTAU.data_ptr(), DP)
-    times = []
+    times, t_qr, t_mq = [], [], []
+    clocks = ClockSampler(torch.cuda.current_device())
     for it in range(1 + steps):
+        if it == 1:
+            clocks.start()
         hA.copy_(hA0)
         hQ.zero_()
         t0 = time.perf_counter()
         L.Hybrid_tile_QR(ctypes.byref(st), pa, pt, 0, 1, IB)
         H.check(L.hqr_last_error(), "Hybrid_tile_QR")
+        t1 = time.perf_counter()
         L.Hybrid_make_Q(ctypes.byref(st), pq, pa, pt, 0, 1, IB)
         H.check(L.hqr_last_error(), "Hybrid_make_Q")
         if it > 0:
-            times.append(time.perf_counter() - t0)
+            t2 = time.perf_counter()
+            times.append(t2 - t0)
+            t_qr.append(t1 - t0)
+            t_mq.append(t2 - t1)
+    clk = clocks.stop()
     L.hqr_set_default_precision(H.HQR_PREC_FP64)
     t_e2e = sum(times)
     if dist:
@@ -367,6 +375,9 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
             "h2d_bytes_per_step": nbytes + tau_b + 2 * nbytes + tau_b,
             "d2h_bytes_per_step": nbytes + tau_b + 2 * nbytes,
             "steps": steps, "warmup": 1, "precision": precision,
+            "phases_ms": {"Hybrid_tile_QR": round(1e3 * float(np.mean(t_qr)), 3),
+                          "Hybrid_make_Q": round(1e3 * float(np.mean(t_mq)), 3)},
+            "clocks": clk,
             "api": "Hybrid_tile_QR + Hybrid_make_Q (pinned host arrays)"}
 
 
@@ -522,6 +533,11 @@ def main():
                        world, True, not args.no_check, init)
     value = main_run["flops"] / main_run["elapsed"] / 1e12
 
+    e2e = None
+    e2e_steps = args.e2e_steps if args.e2e_steps is not None else args.steps
+    if e2e_steps > 0:
+        e2e = measure_e2e(H, torch, L, args.precision, n, NB, IB, e2e_steps, dist, world)
+
     compare = None
     if args.precision == "split" and not args.no_compare:
         fp = measure(H, torch, L, args, "fp64", n, args.fp64_nb, IB, 1, 1, dist, world, False,
@@ -532,11 +548,6 @@ def main():
                    "phases_ms": {"factor": round(1e3 * fp["fact_s"][0], 3),
                                  "make_q": round(1e3 * fp["mq_s"][0], 3)},
                    "accuracy": fp["acc"], "split_over_fp64": round(value / fv, 3)}
-
-    e2e = None
-    e2e_steps = args.e2e_steps if args.e2e_steps is not None else args.steps
-    if e2e_steps > 0:
-        e2e = measure_e2e(H, torch, L, args.precision, n, NB, IB, e2e_steps, dist, world)
 
     cpu = None
     if rank == 0 and not args.no_cpu:

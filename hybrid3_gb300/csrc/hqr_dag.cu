@@ -44,7 +44,8 @@ int make_geometry(long M, long N, int NB, int IB, Geometry* g) {
   SmemPlan sp = SmemPlan::make(sh);
   g->smem_bytes = (size_t)sp.total * sizeof(double);
   if (g->smem_bytes > smem_cap) return HQR_ERR_UNSUPPORTED;
-  if ((long long)g->steps * g->MT + (long long)g->steps * g->NT * g->MT * g->NC > 0x3fffffffLL)
+  if ((long long)g->steps * g->MT * (g->NB / g->w + 1) + (long long)g->steps * g->NT * g->MT * g->NC >
+      0x3fffffffLL)
     return HQR_ERR_UNSUPPORTED;
   return HQR_OK;
 }
@@ -161,11 +162,12 @@ int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, d
   p.timeout_ns = timeout_ns;
   set_oz(p, g, ozw);
   p.prep = p.oz;
-  // tasks: per step i, 1 GEQRT + (MT-1-i) TSQRT [+ as many OZPREP] +
-  // NC*(NT-1-i)*(MT-i) updates
+  p.nblk = g.NB / g.w;
+  // tasks: per step i, nblk inner blocks of 1 GEQRT and (MT-1-i) TSQRT [+ one
+  // OZPREP per panel tile] + NC*(NT-1-i)*(MT-i) updates
   long long n = 0;
   for (int i = 0; i < g.steps; i++)
-    n += (long long)(g.MT - i) * (p.prep ? 2 : 1) + (long long)p.NC * (g.NT - 1 - i) * (g.MT - i);
+    n += (long long)(g.MT - i) * (p.nblk + (p.prep ? 1 : 0)) + (long long)p.NC * (g.NT - 1 - i) * (g.MT - i);
   p.n_tasks = (int)n;
   return run_dag(p, ws, g, stream);
 }
@@ -188,6 +190,7 @@ int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, doubl
   p.timeout_ns = timeout_ns;
   set_oz(p, g, ozw);
   p.prep = 0;
+  p.nblk = 1;
   long long n = 0;
   for (int i = 0; i < g.steps; i++) n += (g.MT - i) + (long long)p.NC * CT * (g.MT - i);
   p.n_tasks = (int)n;
@@ -212,6 +215,7 @@ int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double
   p.timeout_ns = timeout_ns;
   set_oz(p, g, ozw);
   p.prep = 0;
+  p.nblk = 1;
   // per step i: MT - i panel tasks and NC (NT - i) (MT - i) updates
   long long n = 0;
   for (int i = 0; i < g.steps; i++) n += (g.MT - i) + (long long)p.NC * (g.NT - i) * (g.MT - i);
@@ -240,7 +244,7 @@ size_t oz_slice_bytes(const Geometry& g) { return panel_tiles(g) * oz::panel_sli
 size_t oz_exp_bytes(const Geometry& g) { return panel_tiles(g) * 3 * (size_t)g.NB * sizeof(int); }
 
 size_t factor_task_ids(const Geometry& g) {
-  return (size_t)g.steps * g.MT + (size_t)g.steps * g.NT * g.MT * g.NC;
+  return (size_t)g.steps * g.MT * (g.NB / g.w) + (size_t)g.steps * g.NT * g.MT * g.NC;
 }
 
 int launch_factor_external(const Geometry& g, const ExternalScratch& x, double* dA, double* dTAU,
@@ -255,12 +259,13 @@ int launch_factor_external(const Geometry& g, const ExternalScratch& x, double* 
   p.NC = g.NC;
   p.steps = g.steps;
   p.J = g.NT;
+  p.nblk = g.NB / g.w;
   p.sh = shape_of(g);
   p.sp = SmemPlan::make(p.sh);
   p.n_ids = (int)factor_task_ids(g);
   long long n = 0;
   for (int i = 0; i < g.steps; i++)
-    n += (g.MT - i) + (long long)g.NC * (g.NT - 1 - i) * (g.MT - i);
+    n += (long long)(g.MT - i) * p.nblk + (long long)g.NC * (g.NT - 1 - i) * (g.MT - i);
   p.n_tasks = (int)n;
   p.A = dA;
   p.T = x.T;

@@ -22,7 +22,11 @@
 //
 // LARFB and SSRFB tasks are split into NC column blocks (the columns of a
 // trailing tile are independent), which multiplies the parallelism of a step
-// by NC.  Every wait is bounded in time: when a wait runs out the kernel sets
+// by NC.  The factorization's panel tasks are split into their w-column inner
+// blocks: block b of the TSQRT of tile k needs block b of tile k-1's panel
+// (the last writer of R's rows [b w, (b+1) w)) and block b-1 of its own tile,
+// so the TS chain down a panel column runs as a wavefront, MT + NB/w block
+// steps deep instead of MT NB/w.  Every wait is bounded in time: when a wait runs out the kernel sets
 // an error bit and every CTA returns, so a broken DAG never hangs the GPU.
 #pragma once
 #include "hqr_oztasks.cuh"
@@ -57,6 +61,7 @@ enum Ctl : int { kHiHead = 0, kHiTail = 1, kLoHead = 2, kLoTail = 3, kDone = 4, 
 struct DagParams {
   int mode;
   int MT, NT, CT, NC, steps, J;   // J = tile columns spanned by update ids
+  int nblk;                        // panel inner blocks per panel task id (factorization: NB / w)
   TileShape sh;
   SmemPlan sp;
   double* A;        // factored matrix: R above, V below the diagonal
@@ -81,17 +86,20 @@ struct DagParams {
 constexpr int kNever = 0x3fffffff;
 
 // --- task ids ----------------------------------------------------------------
-//   panel  (i, k)        : i*MT + k                              (k >= i)
+//   panel  (i, k, b)     : (i*MT + k)*nblk + b                   (k >= i)
 //   prep   (i, k)        : P0 + i*MT + k   (factorization with split precision)
 //   update (i, j, k, c)  : U0 + ((i*J + j)*MT + k)*NC + c        (k >= i)
-__host__ __device__ __forceinline__ int panel_id(const DagParams& p, int i, int k) {
-  return i * p.MT + k;
+__host__ __device__ __forceinline__ int panel_id(const DagParams& p, int i, int k, int b = 0) {
+  return (i * p.MT + k) * p.nblk + b;
+}
+__host__ __device__ __forceinline__ int panel_end(const DagParams& p) {
+  return p.steps * p.MT * p.nblk;
 }
 __host__ __device__ __forceinline__ int prep_id(const DagParams& p, int i, int k) {
-  return p.steps * p.MT + i * p.MT + k;
+  return panel_end(p) + i * p.MT + k;
 }
 __host__ __device__ __forceinline__ int update_base(const DagParams& p) {
-  return p.steps * p.MT * (p.prep ? 2 : 1);
+  return panel_end(p) + (p.prep ? p.steps * p.MT : 0);
 }
 __host__ __device__ __forceinline__ int update_id(const DagParams& p, int i, int j, int k, int c) {
   return update_base(p) + ((i * p.J + j) * p.MT + k) * p.NC + c;
@@ -102,18 +110,19 @@ __host__ __device__ __forceinline__ size_t panel_slot(int MT, int i, int k) {
 }
 
 struct TaskDesc {
-  int type, i, j, k, c;
+  int type, i, j, k, c;   // c: column block of an update, inner block of a panel task
 };
 
 __device__ __forceinline__ TaskDesc decode(const DagParams& p, int id) {
   TaskDesc t;
-  const int P0 = p.steps * p.MT;
+  const int P0 = panel_end(p);
   const int U0 = update_base(p);
   if (id < P0) {
-    t.i = id / p.MT;
-    t.k = id % p.MT;
+    const int tile = id / p.nblk;
+    t.i = tile / p.MT;
+    t.k = tile % p.MT;
     t.j = t.i;
-    t.c = 0;
+    t.c = id % p.nblk;
     if (p.mode == kModeFactor)
       t.type = (t.k == t.i) ? kGEQRT : kTSQRT;
     else
@@ -228,13 +237,17 @@ __global__ void dag_init_kernel(DagParams p) {
   p.qhi[id] = -1;
   p.qlo[id] = -1;
   int deps = kNever;
-  const int P0 = p.steps * p.MT;
+  const int P0 = panel_end(p);
   const int U0 = update_base(p);
   if (id < P0) {
-    const int i = id / p.MT, k = id % p.MT;
+    const int tile = id / p.nblk, b = id % p.nblk;
+    const int i = tile / p.MT, k = tile % p.MT;
     if (k >= i) {
+      // block 0: the previous step's update of the tile (NC column blocks);
+      // block b > 0: block b - 1 of the same tile; a TSQRT block also waits
+      // for the same block of the tile above (its rows of R)
       if (p.mode == kModeFactor)
-        deps = (k == i ? 0 : 1) + (i > 0 ? p.NC : 0);
+        deps = (b == 0 ? (i > 0 ? p.NC : 0) : 1) + (k > i ? 1 : 0);
       else
         deps = 0;
     }
@@ -269,6 +282,13 @@ __global__ void dag_seed_kernel(DagParams p) {
 __device__ void release_dependents(const DagParams& p, const TaskDesc& t, int* keep) {
   if (t.type == kGEQRT || t.type == kTSQRT || t.type == kTBUILD || t.type == kOZPREP) {
     const bool feeds_prep = (t.type == kGEQRT || t.type == kTSQRT) && p.prep;
+    const bool panel = (t.type == kGEQRT || t.type == kTSQRT);
+    if (panel) {
+      // the next inner block of this tile, the same block of the tile below
+      if (t.c + 1 < p.nblk) release(p, panel_id(p, t.i, t.k, t.c + 1));
+      if (t.k + 1 < p.MT) release(p, panel_id(p, t.i, t.k + 1, t.c));
+      if (t.c + 1 < p.nblk) return;   // the tile's V, T, TAU are complete after its last block
+    }
     if (feeds_prep) {
       release(p, prep_id(p, t.i, t.k));
     } else {
@@ -277,7 +297,6 @@ __device__ void release_dependents(const DagParams& p, const TaskDesc& t, int* k
       for (int j = j0; j < j1; j++)
         for (int c = 0; c < p.NC; c++) release(p, update_id(p, t.i, j, t.k, c));
     }
-    if ((t.type == kGEQRT || t.type == kTSQRT) && t.k + 1 < p.MT) release(p, panel_id(p, t.i, t.k + 1));
     return;
   }
   if (p.mode == kModeBuildQ) {
@@ -292,7 +311,7 @@ __device__ void release_dependents(const DagParams& p, const TaskDesc& t, int* k
   // MEM to the next step (only SSRFB: LARFB's tile row is final)
   if (t.type == kSSRFB && t.i + 1 < p.steps) {
     if (p.mode == kModeFactor && t.j == t.i + 1)
-      release(p, panel_id(p, t.i + 1, t.k));
+      release(p, panel_id(p, t.i + 1, t.k, 0));
     else
       release(p, update_id(p, t.i + 1, t.j, t.k, t.c), keep);
   }
@@ -362,12 +381,13 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
     switch (t.type) {
       case kGEQRT: {
         const size_t o = tile_off(t.i, t.i, p.MT, NB);
-        task_geqrt(p.A + o, p.T + o, p.TAU + tau_off(t.i, t.i, p.MT, NB), p.sh, smem, p.sp);
+        task_geqrt_blk(p.A + o, p.T + o, p.TAU + tau_off(t.i, t.i, p.MT, NB), p.sh, smem, p.sp, t.c);
         break;
       }
       case kTSQRT: {
         const size_t o1 = tile_off(t.i, t.i, p.MT, NB), o2 = tile_off(t.k, t.i, p.MT, NB);
-        task_tsqrt(p.A + o1, p.A + o2, p.T + o2, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.sh, smem, p.sp);
+        task_tsqrt_blk(p.A + o1, p.A + o2, p.T + o2, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.sh, smem, p.sp,
+                       t.c);
         break;
       }
       case kTBUILD: {

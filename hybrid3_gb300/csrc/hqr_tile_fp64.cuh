@@ -86,6 +86,40 @@ __device__ __forceinline__ double block_max(double v, double* red) {
   return s;
 }
 
+// The scalar part of dlarfg for alpha = a, ||x|| = xnorm, ss = ||x||^2; plain:
+// ss lies where its square root needs no scaling.  beta = -sign(a) ||[a; x]||,
+// tau = (beta - a) / beta, scal = 1 / (a - beta) (x is scaled by scal after
+// knt rescalings by 1/safmin, as LAPACK does for tiny columns).
+__device__ __forceinline__ void larfg_scalars(double a, double xnorm, double ss, bool plain,
+                                              double& tau, double& scal, int& knt, double& beta) {
+  tau = 0.0;
+  beta = a;
+  scal = 1.0;
+  knt = 0;
+  const double aa = fabs(a);
+  if (xnorm != 0.0 && plain && aa < 1e140 && (aa > 1e-140 || a == 0.0)) {
+    // dlapy2(alpha, ||x||) as sqrt(alpha^2 + ||x||^2): no overflow or
+    // underflow in this range, one square root instead of two
+    beta = -copysign(sqrt(fma(a, a, ss)), a);
+    tau = (beta - a) / beta;
+    scal = 1.0 / (a - beta);
+  } else if (xnorm != 0.0) {
+    const double safmin = DBL_MIN / (DBL_EPSILON * 0.5);
+    const double rsafmn = 1.0 / safmin;
+    double xn = xnorm;
+    beta = -copysign(hypot(a, xn), a);
+    while (fabs(beta) < safmin && knt < 20) {
+      knt++;
+      a *= rsafmn;
+      xn *= rsafmn;
+      beta = -copysign(hypot(a, xn), a);
+    }
+    tau = (beta - a) / beta;
+    scal = 1.0 / (a - beta);
+    for (int j = 0; j < knt; j++) beta *= safmin;
+  }
+}
+
 __device__ void block_larfg(double* alpha, double* x, int n, double* tau_out, double* red) {
   double ss = 0.0;
   for (int r = threadIdx.x; r < n; r += kThreads) {
@@ -114,30 +148,9 @@ __device__ void block_larfg(double* alpha, double* x, int n, double* tau_out, do
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double a = *alpha, tau = 0.0, beta = a, scal = 1.0;
-    int knt = 0;
-    const double aa = fabs(a);
-    if (xnorm != 0.0 && plain && aa < 1e140 && (aa > 1e-140 || a == 0.0)) {
-      // dlapy2(alpha, ||x||) as sqrt(alpha^2 + ||x||^2): no overflow or
-      // underflow in this range, one square root instead of two
-      beta = -copysign(sqrt(fma(a, a, ss)), a);
-      tau = (beta - a) / beta;
-      scal = 1.0 / (a - beta);
-    } else if (xnorm != 0.0) {
-      const double safmin = DBL_MIN / (DBL_EPSILON * 0.5);
-      const double rsafmn = 1.0 / safmin;
-      double xn = xnorm;
-      beta = -copysign(hypot(a, xn), a);
-      while (fabs(beta) < safmin && knt < 20) {
-        knt++;
-        a *= rsafmn;
-        xn *= rsafmn;
-        beta = -copysign(hypot(a, xn), a);
-      }
-      tau = (beta - a) / beta;
-      scal = 1.0 / (a - beta);
-      for (int j = 0; j < knt; j++) beta *= safmin;
-    }
+    double tau, scal, beta;
+    int knt;
+    larfg_scalars(*alpha, xnorm, ss, plain, tau, scal, knt, beta);
     red[kBcast + 0] = tau;
     red[kBcast + 1] = scal;
     red[kBcast + 2] = (double)knt;
@@ -161,53 +174,168 @@ __device__ void block_larfg(double* alpha, double* x, int n, double* tau_out, do
   __syncthreads();
 }
 
-// ---------------------------------------------------------------------------
-// Unblocked QR of a shared panel (dgeqr2 semantics): P is m x w, ld ldp.
-// ---------------------------------------------------------------------------
-__device__ void panel_qr_ge(double* P, int ldp, int m, int w, double* tau, double* red) {
+// dlarfg on [alpha; x] by one warp (x: n contiguous shared doubles), with the
+// arithmetic of block_larfg; every lane computes the (identical) scalars.
+__device__ void warp_larfg(double* alpha, double* x, int n, double* tau_out) {
+  const int lane = threadIdx.x & 31;
+  double ss = 0.0;
+  for (int r = lane; r < n; r += 32) {
+    const double v = x[r];
+    ss = fma(v, v, ss);
+  }
+  ss = warp_sum(ss);
+  double xnorm;
+  bool plain = false;
+  if (ss == 0.0) {
+    xnorm = 0.0;
+  } else if (ss >= 1e-290 && ss <= 1e290) {
+    xnorm = sqrt(ss);
+    plain = true;
+  } else {
+    double amax = 0.0;
+    for (int r = lane; r < n; r += 32) amax = fmax(amax, fabs(x[r]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+    double s2 = 0.0;
+    for (int r = lane; r < n; r += 32) {
+      const double v = x[r] / amax;
+      s2 = fma(v, v, s2);
+    }
+    s2 = warp_sum(s2);
+    xnorm = amax * sqrt(s2);
+  }
+  double tau, scal, beta;
+  int knt;
+  larfg_scalars(*alpha, xnorm, ss, plain, tau, scal, knt, beta);
+  if (tau != 0.0) {
+    const double rsafmn = 1.0 / (DBL_MIN / (DBL_EPSILON * 0.5));
+    for (int r = lane; r < n; r += 32) {
+      double v = x[r];
+      for (int j = 0; j < knt; j++) v *= rsafmn;
+      x[r] = v * scal;
+    }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    *alpha = beta;
+    *tau_out = tau;
+  }
+  __syncwarp();
+}
+
+// The warp that runs work item `it` of a panel column step: item 0 (the next
+// column, whose reflector is on the critical path) has warp 0 to itself, the
+// other items go round the remaining warps.
+__device__ __forceinline__ bool panel_item_mine(int it, int warp) {
+  return it == 0 ? warp == 0 : (warp != 0 && (it - 1) % (kWarps - 1) == warp - 1);
+}
+
+// Unblocked QR of the triangle-on-square panel [R; A] (R w x w, upper part
+// used; A m x w dense), the per-column loop of CORE_dtsqrt, with the Gram
+// matrix of the reflectors for the T build: G(b, c) = v_b . v_c, b < c (ld w).
+// Column c's reflector acts on [R(c,c); A(:,c)]; A(:, c) becomes v_c.  At
+// step c, the warp that applies reflector c to column c + 1 also forms
+// reflector c + 1 (warp_larfg), the other warps apply reflector c to the
+// remaining columns and compute G(:, c): one barrier per column.
+__device__ void panel_qr_ts_fused(double* R, int ldr, double* A, int lda, int m, int w, double* tau,
+                                  double* G) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int c = 0; c < w && c < m; c++) {
-    double* pc = P + (size_t)c * ldp;
-    block_larfg(pc + c, pc + c + 1, m - c - 1, tau + c, red);
+  if (warp == 0) warp_larfg(R, A, m, tau);
+  __syncthreads();
+  for (int c = 0; c < w; c++) {
     const double t = tau[c];
-    if (t != 0.0) {
-      for (int j = c + 1 + warp; j < w; j += kWarps) {
-        double* pj = P + (size_t)j * ldp;
-        const double pcj = pj[c];
+    const double* ac = A + (size_t)c * lda;
+    const int nupd = w - 1 - c;   // items 0..nupd-1: columns c+1..w-1; then G(b, c), b < c
+    for (int it = 0; it < nupd + c; it++) {
+      if (!panel_item_mine(it, warp)) continue;
+      if (it < nupd) {
+        const int j = c + 1 + it;
+        double* aj = A + (size_t)j * lda;
+        if (t != 0.0) {
+          double* rcj = R + c + (size_t)j * ldr;
+          const double r0 = *rcj;
+          double s = 0.0;
+          for (int r = lane; r < m; r += 32) s = fma(ac[r], aj[r], s);
+          s = (warp_sum(s) + r0) * t;
+          if (lane == 0) *rcj = r0 - s;
+          for (int r = lane; r < m; r += 32) aj[r] = fma(-s, ac[r], aj[r]);
+        }
+        if (it == 0) {
+          __syncwarp();
+          warp_larfg(R + j + (size_t)j * ldr, aj, m, tau + j);
+        }
+      } else {
+        const int b = it - nupd;
+        const double* vb = A + (size_t)b * lda;
         double s = 0.0;
-        for (int r = c + 1 + lane; r < m; r += 32) s = fma(pc[r], pj[r], s);
-        s = (warp_sum(s) + pcj) * t;
-        if (lane == 0) pj[c] = pcj - s;
-        for (int r = c + 1 + lane; r < m; r += 32) pj[r] = fma(-s, pc[r], pj[r]);
+        for (int r = lane; r < m; r += 32) s = fma(vb[r], ac[r], s);
+        s = warp_sum(s);
+        if (lane == 0) G[b + c * w] = s;
       }
     }
     __syncthreads();
   }
 }
 
-// Unblocked QR of the triangle-on-square panel [R; A]: R is w x w (upper part
-// used), A is m x w (dense).  Column c's reflector acts on [R(c,c); A(:,c)];
-// A(:, c) becomes v_c.  This is the per-column loop of CORE_dtsqrt.
-__device__ void panel_qr_ts(double* R, int ldr, double* A, int lda, int m, int w, double* tau,
-                            double* red) {
+// Unblocked QR of a shared panel (dgeqr2 semantics, P m x w, ld ldp, m >= w)
+// with the Gram matrix of the unit-lower reflectors, G(b, c) = v_b . v_c =
+// P(c, b) + sum_{r > c} P(r, b) P(r, c), b < c (ld w); the same one-barrier
+// column step as panel_qr_ts_fused.
+__device__ void panel_qr_ge_fused(double* P, int ldp, int m, int w, double* tau, double* G) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp == 0) warp_larfg(P, P + 1, m - 1, tau);
+  __syncthreads();
   for (int c = 0; c < w; c++) {
-    double* ac = A + (size_t)c * lda;
-    block_larfg(R + c + (size_t)c * ldr, ac, m, tau + c, red);
     const double t = tau[c];
-    if (t != 0.0) {
-      for (int j = c + 1 + warp; j < w; j += kWarps) {
-        double* aj = A + (size_t)j * lda;
-        double* rcj = R + c + (size_t)j * ldr;
-        const double r0 = *rcj;
+    const double* pc = P + (size_t)c * ldp;
+    const int nupd = w - 1 - c;
+    for (int it = 0; it < nupd + c; it++) {
+      if (!panel_item_mine(it, warp)) continue;
+      if (it < nupd) {
+        const int j = c + 1 + it;
+        double* pj = P + (size_t)j * ldp;
+        if (t != 0.0) {
+          const double pcj = pj[c];
+          double s = 0.0;
+          for (int r = c + 1 + lane; r < m; r += 32) s = fma(pc[r], pj[r], s);
+          s = (warp_sum(s) + pcj) * t;
+          if (lane == 0) pj[c] = pcj - s;
+          for (int r = c + 1 + lane; r < m; r += 32) pj[r] = fma(-s, pc[r], pj[r]);
+        }
+        if (it == 0) {
+          __syncwarp();
+          warp_larfg(pj + j, pj + j + 1, m - j - 1, tau + j);
+        }
+      } else {
+        const int b = it - nupd;
+        const double* pb = P + (size_t)b * ldp;
         double s = 0.0;
-        for (int r = lane; r < m; r += 32) s = fma(ac[r], aj[r], s);
-        s = (warp_sum(s) + r0) * t;
-        if (lane == 0) *rcj = r0 - s;
-        for (int r = lane; r < m; r += 32) aj[r] = fma(-s, ac[r], aj[r]);
+        for (int r = c + 1 + lane; r < m; r += 32) s = fma(pb[r], pc[r], s);
+        s = warp_sum(s);
+        if (lane == 0) G[b + c * w] = s + pb[c];
       }
     }
     __syncthreads();
+  }
+}
+
+// T (w x w upper, ld w) of a block of w reflectors (dlarft 'F','C') from tau
+// and the Gram G(b, c), b < c: T(c, c) = tau_c, T(0:c, c) = -tau_c T(0:c,
+// 0:c) G(0:c, c).  One warp, lane a owns row a of T: a row depends only on
+// itself, so no synchronisation between the columns.
+__device__ void t_from_gram(const double* G, const double* tau, double* T, int w) {
+  const int a = threadIdx.x & 31;
+  if (a >= w) return;
+  for (int c = 0; c < w; c++) {
+    double v;
+    if (a < c) {
+      double s = 0.0;
+      for (int b = a; b < c; b++) s = fma(T[a + b * w], G[b + c * w], s);
+      v = (tau[c] == 0.0) ? 0.0 : -tau[c] * s;
+    } else {
+      v = (a == c) ? tau[c] : 0.0;
+    }
+    T[a + c * w] = v;
   }
 }
 
@@ -390,22 +518,26 @@ __device__ void store_block(double* g, int ldg, const double* s, int lds, int m,
   }
 }
 
-// CORE_dgeqrt(NB, NB, IB, A, NB, T, NB, TAU)
-__device__ void task_geqrt(double* A, double* T, double* tau_g, const TileShape& sh, double* smem,
-                           const SmemPlan& sp) {
+// Inner block b of CORE_dgeqrt(NB, NB, IB, A, NB, T, NB, TAU): the QR of
+// columns [b w, (b+1) w) from row b w down (blocks 0..b-1 done), its T block,
+// and its application to the columns right of it.  It writes rows >= b w of
+// the tile only: rows [b w, (b+1) w) of R are final afterwards.
+__device__ void task_geqrt_blk(double* A, double* T, double* tau_g, const TileShape& sh, double* smem,
+                               const SmemPlan& sp, int b) {
   const int NB = sh.NB, w = sh.w;
   double* sP = smem + sp.off_c1;
   double* sTau = smem + sp.off_tau;
-  double* red = smem + sp.off_red;
   double* sG = smem + sp.off_g;
   double* sTb = smem + sp.off_t;
-  for (int i0 = 0; i0 < NB; i0 += w) {
+  {
+    const int i0 = b * w;
     const int m = NB - i0;
     __syncthreads();
     load_block(sP, NB, A + i0 + (size_t)i0 * NB, NB, m, w);
     __syncthreads();
-    panel_qr_ge(sP, NB, m, w, sTau, red);
-    build_t_block(sP, NB, m, w, true, sTau, sG, sTb);
+    panel_qr_ge_fused(sP, NB, m, w, sTau, sG);
+    if (threadIdx.x < 32) t_from_gram(sG, sTau, sTb, w);
+    __syncthreads();
     store_block(A + i0 + (size_t)i0 * NB, NB, sP, NB, m, w);
     store_block(T + i0 + (size_t)i0 * NB, NB, sTb, w, w, w);
     for (int e = threadIdx.x; e < w; e += kThreads) stg_cg(tau_g + i0 + e, sTau[e]);
@@ -424,24 +556,36 @@ __device__ void task_geqrt(double* A, double* T, double* tau_g, const TileShape&
   __syncthreads();
 }
 
-// CORE_dtsqrt(NB, NB, IB, A1, NB, A2, NB, T, NB, TAU): A1 holds R (upper part)
-// above the GEQRT's V (strict lower part, left untouched).
-__device__ void task_tsqrt(double* A1, double* A2, double* T, double* tau_g, const TileShape& sh,
-                           double* smem, const SmemPlan& sp) {
+// CORE_dgeqrt(NB, NB, IB, A, NB, T, NB, TAU)
+__device__ void task_geqrt(double* A, double* T, double* tau_g, const TileShape& sh, double* smem,
+                           const SmemPlan& sp) {
+  for (int b = 0; b < sh.NB / sh.w; b++) task_geqrt_blk(A, T, tau_g, sh, smem, sp, b);
+}
+
+// Inner block b of CORE_dtsqrt(NB, NB, IB, A1, NB, A2, NB, T, NB, TAU): A1
+// holds R (upper part) above the GEQRT's V (strict lower part, left
+// untouched).  The QR of [R(bw:(b+1)w, bw:(b+1)w); A2(:, bw:(b+1)w)] (blocks
+// 0..b-1 of this tile done), its T block, and its application to the columns
+// right of it.  Of A1 it touches rows [b w, (b+1) w) only, and those rows are
+// touched by no other block of this TSQRT: once block b is done here, block b
+// of the TSQRT of the next tile below may run.
+__device__ void task_tsqrt_blk(double* A1, double* A2, double* T, double* tau_g, const TileShape& sh,
+                               double* smem, const SmemPlan& sp, int b) {
   const int NB = sh.NB, w = sh.w;
   double* sA = smem + sp.off_c1;     // NB x w panel of A2
   double* sR = smem + sp.off_vt;     // w x w block of R
   double* sTau = smem + sp.off_tau;
-  double* red = smem + sp.off_red;
   double* sG = smem + sp.off_g;
   double* sTb = smem + sp.off_t;
-  for (int i0 = 0; i0 < NB; i0 += w) {
+  {
+    const int i0 = b * w;
     __syncthreads();
     load_block(sA, NB, A2 + (size_t)i0 * NB, NB, NB, w);
     load_block(sR, w, A1 + i0 + (size_t)i0 * NB, NB, w, w);
     __syncthreads();
-    panel_qr_ts(sR, w, sA, NB, NB, w, sTau, red);
-    build_t_block(sA, NB, NB, w, false, sTau, sG, sTb);
+    panel_qr_ts_fused(sR, w, sA, NB, NB, w, sTau, sG);
+    if (threadIdx.x < 32) t_from_gram(sG, sTau, sTb, w);
+    __syncthreads();
     store_block(A2 + (size_t)i0 * NB, NB, sA, NB, NB, w);
     for (int e = threadIdx.x; e < w * w; e += kThreads) {
       const int r = e % w, c = e / w;
@@ -465,6 +609,12 @@ __device__ void task_tsqrt(double* A1, double* A2, double* T, double* tau_g, con
     }
   }
   __syncthreads();
+}
+
+// CORE_dtsqrt(NB, NB, IB, A1, NB, A2, NB, T, NB, TAU)
+__device__ void task_tsqrt(double* A1, double* A2, double* T, double* tau_g, const TileShape& sh,
+                           double* smem, const SmemPlan& sp) {
+  for (int b = 0; b < sh.NB / sh.w; b++) task_tsqrt_blk(A1, A2, T, tau_g, sh, smem, sp, b);
 }
 
 // CORE_dormqr(Left, Trans, NB, ncol, NB, IB, V, NB, T, NB, C, NB) on columns

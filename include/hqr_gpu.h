@@ -45,7 +45,9 @@ typedef struct hqr_plan hqr_plan_t;
  * summed over CTAs).  Index: 0 GEQRT, 1 TSQRT, 2 LARFB, 3 SSRFB, 4 T-build,
  * 5 split-precision panel preparation (full T + operand slices), 6 the
  * scheduler itself (thread 0 of each CTA popping tasks and releasing their
- * dependents; count = tasks). */
+ * dependents; count = tasks).  GEQRT and TSQRT are counted per inner block
+ * of w = min(IB, 32) columns (w = 16 with HQR_PREC_OZAKI): each inner block is
+ * its own task. */
 typedef struct {
     unsigned long long count[7];
     unsigned long long cycles[7];

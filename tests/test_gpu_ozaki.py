@@ -64,7 +64,10 @@ def test_split_factorization_matches_oracle(env, M, N, NB, IB):
     steps = min(MT, NT)
     panels = sum(MT - i for i in range(steps))
     assert st["count"][5] == panels            # one preparation per panel tile
-    assert st["count"][0] == steps
+    # panel tasks run per inner block: the split path's panels use w = 16
+    nblk = NB // 16
+    assert st["count"][0] == steps * nblk
+    assert st["count"][1] == (panels - steps) * nblk
     plan.close()
 
 

@@ -164,9 +164,11 @@ def test_extended_api_device_pointers(H):
     st = plan.stats(s)
     MT = NT = M // NB
     NC = {128: 1}.get(NB, None)
-    # GEQRT and TSQRT counts are fixed by the grid
-    assert st["count"][0] == MT
-    assert st["count"][1] == MT * (MT - 1) // 2
+    # GEQRT and TSQRT counts are fixed by the grid, one task per inner block
+    # of w = min(IB, 32) columns
+    nblk = NB // min(IB, 32)
+    assert st["count"][0] == MT * nblk
+    assert st["count"][1] == MT * (MT - 1) // 2 * nblk
     # make_q with the persisted T factors equals the rebuild path
     dQ = torch.zeros(M * N, dtype=torch.float64, device="cuda")
     dR = dA.clone()
