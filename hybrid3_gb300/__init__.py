@@ -106,6 +106,8 @@ SIGNATURES = {
     "hqr_make_q_async": (_I, [_vp, _vp, _vp, _vp, _I, _vp]),
     "hqr_ormqr_t": (_I, [_vp, _vp, _vp, _vp, _I, _I, _vp]),
     "hqr_lstsq": (_I, [_vp, _vp, _vp, _I, _I, _vp, _I, _I, _vp, _vp]),
+    "hqr_colmajor_to_tiles_padded": (_I, [_L, _L, _L, _I, _vp, _vp, _vp]),
+    "hqr_tiles_to_colmajor_padded": (_I, [_L, _L, _L, _I, _vp, _vp, _vp]),
     "hqr_dgemm_tn": (_I, [_L, _I, _vp, _vp, _vp, _vp]),
     "hqr_make_identity": (_I, [_L, _L, _I, _vp, _vp]),
     "hqr_fill_uniform": (_I, [_L, _L, _I, ctypes.c_uint64, _vp, _vp]),

@@ -376,6 +376,20 @@ int hqr_colmajor_to_tiles(long M, long N, int NB, const double* dCM, double* dT,
   return cuda_rc(cudaGetLastError());
 }
 
+int hqr_colmajor_to_tiles_padded(long M, long N, long ld, int NB, const double* dCM, double* dT,
+                                 void* stream) {
+  if (!dT || !dCM || NB <= 0 || M <= 0 || N <= 0 || ld < M) return HQR_ERR_INVALID;
+  hqr::colmajor_to_tiles_padded(dCM, ld, M, N, NB, dT, (cudaStream_t)stream);
+  return cuda_rc(cudaGetLastError());
+}
+
+int hqr_tiles_to_colmajor_padded(long M, long N, long ld, int NB, const double* dT, double* dCM,
+                                 void* stream) {
+  if (!dT || !dCM || NB <= 0 || M <= 0 || N <= 0 || ld < M) return HQR_ERR_INVALID;
+  hqr::tiles_to_colmajor_padded(dT, ld, M, N, NB, dCM, (cudaStream_t)stream);
+  return cuda_rc(cudaGetLastError());
+}
+
 double hqr_fp64_peak_tflops(void* stream) {
   return hqr::measure_fp64_peak_tflops((cudaStream_t)stream);
 }

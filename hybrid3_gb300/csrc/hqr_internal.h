@@ -28,6 +28,10 @@ int record_cuda_error(cudaError_t e, const char* where);
 // and exit, or print and remember for hqr_last_error); returns rc.
 int report_error(const char* fn, int rc);
 
+// Column-major (M x N, ld) <-> tile layout padded to whole tiles (hqr_util.cu).
+void colmajor_to_tiles_padded(const double* dIn, long ld, long M, long N, int NB, double* dT, cudaStream_t s);
+void tiles_to_colmajor_padded(const double* dT, long ld, long M, long N, int NB, double* dOut, cudaStream_t s);
+
 // Least-squares helpers (hqr_lstsq.cu).  Right-hand sides: column-major
 // M x nrhs; C: tile layout with MT = M / NB tile rows and CT tile columns.
 void pack_rhs(const double* dB, long ldb, int nrhs, double* dC, long M, int NB, int CT, cudaStream_t s);

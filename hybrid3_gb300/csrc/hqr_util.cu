@@ -170,6 +170,29 @@ __global__ void k_tiles_to_colmajor(const double* T, double* out, long M, long N
   }
 }
 
+// Padded conversions: the tile array holds an (MT NB) x (NT NB) matrix, MT =
+// ceil(M / NB), NT = ceil(N / NB); the column-major matrix is M x N with
+// leading dimension ld.  Into tiles the tail rows and columns are zero; out of
+// tiles only the leading M x N block is written.  One thread per tile element.
+__global__ void k_colmajor_to_tiles_padded(const double* __restrict__ in, long ld, long M, long N, int NB,
+                                           int MT, int NT, double* __restrict__ T) {
+  const size_t n = (size_t)MT * NT * NB * NB;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    long r, c;
+    tile_rc(e, MT, NB, &r, &c);
+    T[e] = (r < M && c < N) ? in[(size_t)c * ld + r] : 0.0;
+  }
+}
+__global__ void k_tiles_to_colmajor_padded(const double* __restrict__ T, long ld, long M, long N, int NB,
+                                           int MT, double* __restrict__ out) {
+  const size_t n = (size_t)M * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const long r = (long)(e % (size_t)M), c = (long)(e / (size_t)M);
+    const size_t t = ((size_t)(r / NB) + (size_t)(c / NB) * MT) * NB * NB + (size_t)(c % NB) * NB + (r % NB);
+    out[(size_t)c * ld + r] = T[t];
+  }
+}
+
 __global__ void k_max_col_abs_sum(const double* X, long M, long N, unsigned long long* out_bits) {
   for (long c = blockIdx.x; c < N; c += gridDim.x) {
     double s = 0.0;
@@ -263,6 +286,14 @@ void tiles_to_colmajor(const double* dT, double* dOut, long M, long N, int NB, c
 }
 void colmajor_to_tiles(const double* dIn, double* dT, long M, long N, int NB, cudaStream_t s) {
   k_tiles_to_colmajor<<<grid_for((size_t)M * N), 256, 0, s>>>(dIn, dT, M, N, NB, 0);
+}
+void colmajor_to_tiles_padded(const double* dIn, long ld, long M, long N, int NB, double* dT, cudaStream_t s) {
+  const int MT = (int)((M + NB - 1) / NB), NT = (int)((N + NB - 1) / NB);
+  k_colmajor_to_tiles_padded<<<grid_for((size_t)MT * NT * NB * NB), 256, 0, s>>>(dIn, ld, M, N, NB, MT, NT, dT);
+}
+void tiles_to_colmajor_padded(const double* dT, long ld, long M, long N, int NB, double* dOut, cudaStream_t s) {
+  const int MT = (int)((M + NB - 1) / NB);
+  k_tiles_to_colmajor_padded<<<grid_for((size_t)M * N), 256, 0, s>>>(dT, ld, M, N, NB, MT, dOut);
 }
 void max_col_abs_sum(const double* dColMajor, long M, long N, double* d_out, cudaStream_t s) {
   cudaMemsetAsync(d_out, 0, sizeof(double), s);

@@ -137,6 +137,16 @@ int hqr_frob2(long M, long N, int NB, const double *dX, const double *dY, double
 /* Tile layout <-> column-major (ld = M). */
 int hqr_tiles_to_colmajor(long M, long N, int NB, const double *dT, double *dCM, void *stream);
 int hqr_colmajor_to_tiles(long M, long N, int NB, const double *dCM, double *dT, void *stream);
+/* Any M x N column-major matrix (leading dimension ld >= M) <-> the tile
+ * layout padded to whole tiles: dT holds ceil(M/NB) x ceil(N/NB) tiles of
+ * NB x NB, the rows and columns beyond M, N zero (to tiles) or ignored (from
+ * tiles).  Zero padding leaves a QR's R (and Q's leading M x N block) that of
+ * the unpadded matrix: the padded rows and columns add reflectors with tau 0.
+ * The reference has a one-way printing version (mat_dprint, mat_prod.c:260). */
+int hqr_colmajor_to_tiles_padded(long M, long N, long ld, int NB, const double *dCM, double *dT,
+                                 void *stream);
+int hqr_tiles_to_colmajor_padded(long M, long N, long ld, int NB, const double *dT, double *dCM,
+                                 void *stream);
 /* The split-precision product engine on its own (diagnostics / tests):
  * dC = dX dY for dX NB x NB and dY NB x 64, column-major device arrays,
  * NB = 128; same slicing, tensor-core products and recombination as
