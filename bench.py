@@ -423,6 +423,8 @@ def run_lstsq(H, torch, L, args):
     dB = b.T.contiguous()                       # column-major m x nrhs
     dX = torch.zeros(nrhs, n, dtype=f64, device="cuda")   # column-major n x nrhs
     plan = H.Plan(m, n, NB, IB, prec)
+    if args.tree:
+        plan.set_tree(args.tree)
     torch.cuda.synchronize()
     for _ in range(args.warmup):
         plan.lstsq(dA.data_ptr(), dB.data_ptr(), nrhs, dX.data_ptr(), refine_steps=args.refine)
@@ -451,7 +453,7 @@ def run_lstsq(H, torch, L, args):
                                f"geometric 1..1/kappa), kappa={kappa:g}, {nrhs} right-hand sides, "
                                f"b = A x_true + 1e-8 noise",
                    "m": m, "n": n, "nrhs": nrhs, "kappa": kappa, "NB": NB, "IB": IB,
-                   "refine_steps": args.refine,
+                   "refine_steps": args.refine, "tree_domain_tiles": args.tree,
                    "precision": ("split (Ozaki BF16 slices on tcgen05, FP64 panels)"
                                  if args.precision == "split" else "fp64 (plain)")},
         "accuracy": {"forward_error_vs_fp64_lstsq": rel(x, x_ref),
@@ -489,6 +491,8 @@ def main():
     ap.add_argument("--m", type=int, default=32768, help="rows of A for --lstsq")
     ap.add_argument("--nrhs", type=int, default=16, help="right-hand sides for --lstsq")
     ap.add_argument("--refine", type=int, default=1, help="FP64 refinement steps for --lstsq")
+    ap.add_argument("--tree", type=int, default=0,
+                    help="domain tree of this many tiles for the TS reduction (0: the flat tree)")
     args = ap.parse_args()
     if args.n is None:
         args.n = 8192 if args.lstsq else 16384

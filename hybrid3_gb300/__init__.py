@@ -106,6 +106,7 @@ SIGNATURES = {
     "hqr_make_q_async": (_I, [_vp, _vp, _vp, _vp, _I, _vp]),
     "hqr_ormqr_t": (_I, [_vp, _vp, _vp, _vp, _I, _I, _vp]),
     "hqr_lstsq": (_I, [_vp, _vp, _vp, _I, _I, _vp, _I, _I, _vp, _vp]),
+    "hqr_plan_set_tree": (_I, [_vp, _I]),
     "hqr_colmajor_to_tiles_padded": (_I, [_L, _L, _L, _I, _vp, _vp, _vp]),
     "hqr_tiles_to_colmajor_padded": (_I, [_L, _L, _L, _I, _vp, _vp, _vp]),
     "hqr_dgemm_tn": (_I, [_L, _I, _vp, _vp, _vp, _vp]),
@@ -189,6 +190,10 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+    def set_tree(self, domain_tiles: int):
+        """Domain tree of domain_tiles tiles for the factorizations on this plan (0: flat)."""
+        check(lib().hqr_plan_set_tree(self.h, domain_tiles), "hqr_plan_set_tree")
 
     def lstsq(self, dA, dB, nrhs, dX, refine_steps=1, ldb=None, ldx=None, stream=None):
         """hqr_lstsq on device addresses (tile-layout A of this plan's shape,

@@ -20,6 +20,7 @@ struct hqr_plan {
   double* dT;
   hqr::DagWorkspace ws;
   hqr::OzWorkspace oz;   // allocated for HQR_PREC_OZAKI only
+  hqr::TreeWorkspace tree;   // domain tree (hqr_plan_set_tree); S = 0: flat
 };
 
 namespace {
@@ -119,6 +120,12 @@ size_t tau_len(const hqr::Geometry& g) { return (size_t)g.MT * g.NT * g.NB; }
 int build_qt(hqr_plan* plan, double* dQ, const double* dRY, const double* dTAU, bool rebuild_t,
              cudaStream_t s) {
   const hqr::Geometry& g = plan->g;
+  if (plan->tree.S > 0) {   // a tree's merges live in the plan: forward application on I
+    if (rebuild_t) return HQR_ERR_UNSUPPORTED;
+    hqr::make_identity(dQ, g.M, g.N, g.NB, true, s);
+    return hqr::launch_apply_qt_tree(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g.NT, g_timeout_ns, s,
+                                     &plan->oz, &plan->tree);
+  }
   if (g.M == g.N && g.NB % 32 == 0) {
     hqr::make_identity(dQ, g.M, g.N, g.NB, true, s);
     TRY(hqr::launch_build_q(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g_timeout_ns, s, &plan->oz));
@@ -209,8 +216,46 @@ int hqr_plan_create(hqr_plan_t** plan, long M, long N, int NB, int IB, int preci
   return HQR_OK;
 }
 
+namespace {
+void free_tree(hqr::TreeWorkspace* t) {
+  cudaFree(t->T2);
+  cudaFree(t->TAU2);
+  cudaFree(t->slices2);
+  cudaFree(t->sexp2);
+  *t = hqr::TreeWorkspace{};
+}
+}  // namespace
+
+int hqr_plan_set_tree(hqr_plan_t* plan, int domain_tiles) {
+  if (!plan || domain_tiles < 0) return HQR_ERR_INVALID;
+  free_tree(&plan->tree);
+  const hqr::Geometry& g = plan->g;
+  const size_t slots = hqr::tree_slots(g, domain_tiles);
+  if (slots == 0) return HQR_OK;   // one domain: the flat tree
+  // the task ids of the tree DAG must fit an int
+  const long long dmax = (g.MT + domain_tiles - 1) / domain_tiles;
+  const long long extra = (long long)g.steps * dmax * ((long long)g.NB / g.w + 1 + (long long)g.NT * 2);
+  if (extra > 0x1fffffffLL) return HQR_ERR_UNSUPPORTED;
+  hqr::TreeWorkspace t;
+  t.S = domain_tiles;
+  const size_t nb = (size_t)g.NB;
+  bool ok = cudaMalloc(&t.T2, slots * nb * nb * sizeof(double)) == cudaSuccess &&
+            cudaMalloc(&t.TAU2, slots * nb * sizeof(double)) == cudaSuccess;
+  if (ok && plan->precision == HQR_PREC_OZAKI)
+    ok = cudaMalloc(&t.slices2, slots * hqr::oz_panel_bytes()) == cudaSuccess &&
+         cudaMalloc(&t.sexp2, slots * 3 * nb * sizeof(int)) == cudaSuccess;
+  if (!ok) {
+    free_tree(&t);
+    return HQR_ERR_NOMEM;
+  }
+  cudaMemset(t.T2, 0, slots * nb * nb * sizeof(double));
+  plan->tree = t;
+  return HQR_OK;
+}
+
 int hqr_plan_destroy(hqr_plan_t* plan) {
   if (!plan) return HQR_ERR_INVALID;
+  free_tree(&plan->tree);
   if (plan->dT) cudaFree(plan->dT);
   if (plan->oz.slices) cudaFree(plan->oz.slices);
   if (plan->oz.sexp) cudaFree(plan->oz.sexp);
@@ -224,7 +269,7 @@ double* hqr_plan_t_factors(hqr_plan_t* plan) { return plan ? plan->dT : nullptr;
 int hqr_geqrf_async(hqr_plan_t* plan, double* dA, double* dTAU, void* stream) {
   if (!plan || !dA || !dTAU) return HQR_ERR_INVALID;
   return hqr::launch_factor(plan->g, &plan->ws, dA, plan->dT, dTAU, g_timeout_ns,
-                            (cudaStream_t)stream, &plan->oz);
+                            (cudaStream_t)stream, &plan->oz, &plan->tree);
 }
 
 int hqr_plan_status(hqr_plan_t* plan, void* stream) {
@@ -268,8 +313,14 @@ int hqr_make_q(hqr_plan_t* plan, double* dQ, double* dRY, const double* dTAU, in
 int hqr_ormqr_t(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT,
                 int use_plan_t, void* stream) {
   if (!plan || !dRY || !dTAU || !dC || CT <= 0) return HQR_ERR_INVALID;
-  TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, !use_plan_t,
-                           g_timeout_ns, (cudaStream_t)stream, &plan->oz));
+  if (plan->tree.S > 0) {
+    if (!use_plan_t) return HQR_ERR_UNSUPPORTED;   // the merges' T factors live in the plan
+    TRY(hqr::launch_apply_qt_tree(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, g_timeout_ns,
+                                  (cudaStream_t)stream, &plan->oz, &plan->tree));
+  } else {
+    TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, !use_plan_t,
+                             g_timeout_ns, (cudaStream_t)stream, &plan->oz));
+  }
   return hqr_plan_status(plan, stream);
 }
 

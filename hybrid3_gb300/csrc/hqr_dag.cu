@@ -114,7 +114,7 @@ static int launch_exec(const DagParams& p, const Geometry& g, cudaStream_t strea
 static int run_dag(DagParams& p, DagWorkspace* ws, const Geometry& g, cudaStream_t stream) {
   p.sh = shape_of(g);
   p.sp = SmemPlan::make(p.sh);
-  p.n_ids = update_base(p) + p.steps * p.J * p.MT * p.NC;
+  p.n_ids = id_end(p);
   int rc = dag_workspace_reserve(ws, (size_t)p.n_ids);
   if (rc != HQR_OK) return rc;
   p.cnt = ws->cnt;
@@ -146,8 +146,25 @@ static void set_oz(DagParams& p, const Geometry& g, const OzWorkspace* oz) {
   }
 }
 
+// Domains and merge storage of a domain tree (tw null or tw->S == 0: flat).
+static void set_tree(DagParams& p, const Geometry& g, const TreeWorkspace* tw) {
+  if (!tw || tw->S <= 0 || tw->S >= g.MT) {
+    p.tree = 0;
+    p.dmax = 0;
+    return;
+  }
+  p.tree = tw->S;
+  p.dmax = (g.MT + tw->S - 1) / tw->S;
+  p.T2 = tw->T2;
+  p.TAU2 = tw->TAU2;
+  p.slices2 = tw->slices2;
+  p.sexp2 = tw->sexp2;
+}
+static long long merges_of_step(const DagParams& p, int i) { return n_domains(p, i) - 1; }
+
 int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, double* dTAU,
-                  long long timeout_ns, cudaStream_t stream, const OzWorkspace* ozw) {
+                  long long timeout_ns, cudaStream_t stream, const OzWorkspace* ozw,
+                  const TreeWorkspace* tw) {
   DagParams p{};
   p.mode = kModeFactor;
   p.MT = g.MT;
@@ -163,11 +180,16 @@ int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, d
   set_oz(p, g, ozw);
   p.prep = p.oz;
   p.nblk = g.NB / g.w;
-  // tasks: per step i, nblk inner blocks of 1 GEQRT and (MT-1-i) TSQRT [+ one
-  // OZPREP per panel tile] + NC*(NT-1-i)*(MT-i) updates
+  set_tree(p, g, tw);
+  // tasks: per step i, nblk inner blocks of each of the MT-i panel tiles [+ one
+  // OZPREP per panel tile] + NC*(NT-1-i)*(MT-i) updates; a tree adds per merge
+  // nblk blocks [+ one OZPREP] + NC*(NT-1-i) merge updates
   long long n = 0;
-  for (int i = 0; i < g.steps; i++)
+  for (int i = 0; i < g.steps; i++) {
+    const long long m = merges_of_step(p, i);
     n += (long long)(g.MT - i) * (p.nblk + (p.prep ? 1 : 0)) + (long long)p.NC * (g.NT - 1 - i) * (g.MT - i);
+    n += m * (p.nblk + (p.prep ? 1 : 0)) + m * p.NC * (g.NT - 1 - i);
+  }
   p.n_tasks = (int)n;
   return run_dag(p, ws, g, stream);
 }
@@ -195,6 +217,33 @@ int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, doubl
   for (int i = 0; i < g.steps; i++) n += (g.MT - i) + (long long)p.NC * CT * (g.MT - i);
   p.n_tasks = (int)n;
   (void)rebuild_t;   // panel tasks always rebuild T: O(NB^2 w) (FP64) or O(NB^3) (split) per tile
+  return run_dag(p, ws, g, stream);
+}
+
+int launch_apply_qt_tree(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT,
+                         const double* dTAU, double* dC, int CT, long long timeout_ns, cudaStream_t stream,
+                         const OzWorkspace* ozw, const TreeWorkspace* tw) {
+  if (CT <= 0 || !tw || tw->S <= 0) return HQR_ERR_INVALID;
+  DagParams p{};
+  p.mode = kModeApplyQt;
+  p.MT = g.MT;
+  p.NT = g.NT;
+  p.CT = CT;
+  p.steps = g.steps;
+  p.J = CT;
+  p.A = const_cast<double*>(dA);
+  p.T = dT;
+  p.TAU = const_cast<double*>(dTAU);
+  p.C = dC;
+  p.timeout_ns = timeout_ns;
+  set_oz(p, g, ozw);
+  p.prep = 0;
+  p.nblk = 1;
+  p.skip_panels = 1;   // the T factors / slices of the factorization on this plan
+  set_tree(p, g, tw);
+  long long n = 0;
+  for (int i = 0; i < g.steps; i++) n += (long long)p.NC * CT * ((g.MT - i) + merges_of_step(p, i));
+  p.n_tasks = (int)n;
   return run_dag(p, ws, g, stream);
 }
 
@@ -241,7 +290,13 @@ static size_t panel_tiles(const Geometry& g) {
   return panel_slot(g.MT, g.steps, g.steps);   // slots of every (k, i), k >= i, i < steps
 }
 size_t oz_slice_bytes(const Geometry& g) { return panel_tiles(g) * oz::panel_slice_bytes(); }
+size_t oz_panel_bytes() { return oz::panel_slice_bytes(); }
 size_t oz_exp_bytes(const Geometry& g) { return panel_tiles(g) * 3 * (size_t)g.NB * sizeof(int); }
+
+size_t tree_slots(const Geometry& g, int S) {
+  if (S <= 0 || S >= g.MT) return 0;
+  return (size_t)g.steps * ((g.MT + S - 1) / S);
+}
 
 size_t factor_task_ids(const Geometry& g) {
   return (size_t)g.steps * g.MT * (g.NB / g.w) + (size_t)g.steps * g.NT * g.MT * g.NC;

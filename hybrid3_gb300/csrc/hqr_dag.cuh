@@ -48,8 +48,13 @@ enum DagMode : int {
 // panel tile gets an OZPREP task (in the factorization it follows the
 // GEQRT/TSQRT; in the Q^T application it replaces the T-build).
 enum TaskType : int {
-  kGEQRT = 0, kTSQRT = 1, kLARFB = 2, kSSRFB = 3, kTBUILD = 4, kOZPREP = 5, kNumTypes = 6
+  kGEQRT = 0, kTSQRT = 1, kLARFB = 2, kSSRFB = 3, kTBUILD = 4, kOZPREP = 5, kNumTypes = 6,
+  // the merges of a domain tree (counted with TSQRT, OZPREP and SSRFB)
+  kTTQRT = 6, kTTPREP = 7, kTTMQR = 8
 };
+__host__ __device__ __forceinline__ int stat_slot(int type) {
+  return type == kTTQRT ? kTSQRT : type == kTTPREP ? kOZPREP : type == kTTMQR ? kSSRFB : type;
+}
 // Statistics slots: one per task type, then the scheduler's own time (thread
 // 0 of each CTA: popping the next task and releasing the dependents).
 constexpr int kStatSched = kNumTypes, kNumStats = kNumTypes + 1;
@@ -62,6 +67,16 @@ struct DagParams {
   int mode;
   int MT, NT, CT, NC, steps, J;   // J = tile columns spanned by update ids
   int nblk;                        // panel inner blocks per panel task id (factorization: NB / w)
+  // Domain tree (tree > 0): at step i the tile rows i.. are cut into domains of
+  // `tree` tiles; each domain runs the flat TS chain on its own top tile, then
+  // the domain tops' R are merged into R(i, i) one after the other by TT
+  // kernels (CORE_dttqrt / CORE_dttmqr).  tree = 0: one domain (flat tree).
+  int tree, dmax;                  // domain size, maximum number of domains
+  int skip_panels;                 // 1: the panel tasks' T / slices come from the factorization
+  double* T2;                      // T of each merge, compact: tile (i * dmax + d)
+  double* TAU2;                    // TAU of each merge, compact: (i * dmax + d) * NB
+  uint8_t* slices2;                // split: the merges' prepared operands, compact
+  int* sexp2;
   TileShape sh;
   SmemPlan sp;
   double* A;        // factored matrix: R above, V below the diagonal
@@ -85,10 +100,28 @@ struct DagParams {
 
 constexpr int kNever = 0x3fffffff;
 
+// --- domains -------------------------------------------------------------------
+__host__ __device__ __forceinline__ int dom_size(const DagParams& p) { return p.tree > 0 ? p.tree : p.MT; }
+__host__ __device__ __forceinline__ int dom_of(const DagParams& p, int i, int k) { return (k - i) / dom_size(p); }
+__host__ __device__ __forceinline__ int dom_top(const DagParams& p, int i, int d) { return i + d * dom_size(p); }
+__host__ __device__ __forceinline__ int dom_end(const DagParams& p, int i, int d) {
+  const int e = i + (d + 1) * dom_size(p);
+  return e < p.MT ? e : p.MT;
+}
+__host__ __device__ __forceinline__ int n_domains(const DagParams& p, int i) {
+  return p.tree > 0 ? (p.MT - i + p.tree - 1) / p.tree : 1;
+}
+__host__ __device__ __forceinline__ bool is_top(const DagParams& p, int i, int k) {
+  return (k - i) % dom_size(p) == 0;
+}
+
 // --- task ids ----------------------------------------------------------------
 //   panel  (i, k, b)     : (i*MT + k)*nblk + b                   (k >= i)
 //   prep   (i, k)        : P0 + i*MT + k   (factorization with split precision)
 //   update (i, j, k, c)  : U0 + ((i*J + j)*MT + k)*NC + c        (k >= i)
+//   merge  (i, d, b)     : M0 + (i*dmax + d)*nblk + b            (1 <= d < domains)
+//   merge prep (i, d)    : Q0 + i*dmax + d     (split precision)
+//   merge update (i, j, d, c): X0 + ((i*J + j)*dmax + d)*NC + c
 __host__ __device__ __forceinline__ int panel_id(const DagParams& p, int i, int k, int b = 0) {
   return (i * p.MT + k) * p.nblk + b;
 }
@@ -103,6 +136,31 @@ __host__ __device__ __forceinline__ int update_base(const DagParams& p) {
 }
 __host__ __device__ __forceinline__ int update_id(const DagParams& p, int i, int j, int k, int c) {
   return update_base(p) + ((i * p.J + j) * p.MT + k) * p.NC + c;
+}
+__host__ __device__ __forceinline__ int update_end(const DagParams& p) {
+  return update_base(p) + p.steps * p.J * p.MT * p.NC;
+}
+__host__ __device__ __forceinline__ int merge_id(const DagParams& p, int i, int d, int b) {
+  return update_end(p) + (i * p.dmax + d) * p.nblk + b;
+}
+__host__ __device__ __forceinline__ int ttprep_base(const DagParams& p) {
+  return update_end(p) + p.steps * p.dmax * p.nblk;
+}
+__host__ __device__ __forceinline__ int ttprep_id(const DagParams& p, int i, int d) {
+  return ttprep_base(p) + i * p.dmax + d;
+}
+__host__ __device__ __forceinline__ int ttmqr_base(const DagParams& p) {
+  return ttprep_base(p) + (p.prep ? p.steps * p.dmax : 0);
+}
+__host__ __device__ __forceinline__ int ttmqr_id(const DagParams& p, int i, int j, int d, int c) {
+  return ttmqr_base(p) + ((i * p.J + j) * p.dmax + d) * p.NC + c;
+}
+__host__ __device__ __forceinline__ int id_end(const DagParams& p) {
+  return ttmqr_base(p) + p.steps * p.J * p.dmax * p.NC;
+}
+// Compact index of merge (i, d) into T2 / TAU2 / slices2.
+__host__ __device__ __forceinline__ size_t merge_slot(const DagParams& p, int i, int d) {
+  return (size_t)i * p.dmax + d;
 }
 // Compact index of panel tile (k, i), k >= i, into the slice store.
 __host__ __device__ __forceinline__ size_t panel_slot(int MT, int i, int k) {
@@ -124,7 +182,7 @@ __device__ __forceinline__ TaskDesc decode(const DagParams& p, int id) {
     t.j = t.i;
     t.c = id % p.nblk;
     if (p.mode == kModeFactor)
-      t.type = (t.k == t.i) ? kGEQRT : kTSQRT;
+      t.type = is_top(p, t.i, t.k) ? kGEQRT : kTSQRT;
     else
       t.type = p.oz ? kOZPREP : kTBUILD;
   } else if (id < U0) {
@@ -133,13 +191,37 @@ __device__ __forceinline__ TaskDesc decode(const DagParams& p, int id) {
     t.j = t.i;
     t.c = 0;
     t.type = kOZPREP;
-  } else {
+  } else if (id < update_end(p)) {
     int u = id - U0;
     t.c = u % p.NC; u /= p.NC;
     t.k = u % p.MT; u /= p.MT;
     t.j = u % p.J;
     t.i = u / p.J;
-    t.type = (t.k == t.i) ? kLARFB : kSSRFB;
+    t.type = is_top(p, t.i, t.k) ? kLARFB : kSSRFB;
+  } else if (id < ttprep_base(p)) {
+    int u = id - update_end(p);
+    t.c = u % p.nblk; u /= p.nblk;
+    const int d = u % p.dmax;
+    t.i = u / p.dmax;
+    t.j = t.i;
+    t.k = dom_top(p, t.i, d);
+    t.type = kTTQRT;
+  } else if (id < ttmqr_base(p)) {
+    const int u = id - ttprep_base(p);
+    const int d = u % p.dmax;
+    t.i = u / p.dmax;
+    t.j = t.i;
+    t.k = dom_top(p, t.i, d);
+    t.c = 0;
+    t.type = kTTPREP;
+  } else {
+    int u = id - ttmqr_base(p);
+    t.c = u % p.NC; u /= p.NC;
+    const int d = u % p.dmax; u /= p.dmax;
+    t.j = u % p.J;
+    t.i = u / p.J;
+    t.k = dom_top(p, t.i, d);
+    t.type = kTTMQR;
   }
   return t;
 }
@@ -152,7 +234,9 @@ __device__ __forceinline__ bool update_valid(const DagParams& p, int i, int j) {
 
 __device__ __forceinline__ bool is_high_priority(const DagParams& p, int id) {
   const TaskDesc t = decode(p, id);
-  if (t.type == kGEQRT || t.type == kTSQRT || t.type == kTBUILD || t.type == kOZPREP) return true;
+  if (t.type == kGEQRT || t.type == kTSQRT || t.type == kTBUILD || t.type == kOZPREP ||
+      t.type == kTTQRT || t.type == kTTPREP)
+    return true;
   return p.mode == kModeFactor && t.j == t.i + 1;   // look-ahead: next panel column
 }
 
@@ -239,34 +323,54 @@ __global__ void dag_init_kernel(DagParams p) {
   int deps = kNever;
   const int P0 = panel_end(p);
   const int U0 = update_base(p);
+  const int U1 = update_end(p);
   if (id < P0) {
     const int tile = id / p.nblk, b = id % p.nblk;
     const int i = tile / p.MT, k = tile % p.MT;
-    if (k >= i) {
+    if (k >= i && !p.skip_panels) {
       // block 0: the previous step's update of the tile (NC column blocks);
       // block b > 0: block b - 1 of the same tile; a TSQRT block also waits
-      // for the same block of the tile above (its rows of R)
+      // for the same block of the tile above (its domain top's rows of R)
       if (p.mode == kModeFactor)
-        deps = (b == 0 ? (i > 0 ? p.NC : 0) : 1) + (k > i ? 1 : 0);
+        deps = (b == 0 ? (i > 0 ? p.NC : 0) : 1) + (is_top(p, i, k) ? 0 : 1);
       else
         deps = 0;
     }
   } else if (id < U0) {
     const int i = (id - P0) / p.MT, k = (id - P0) % p.MT;
     if (k >= i) deps = 1;   // its panel task
-  } else {
+  } else if (id < U1) {
     int u = id - U0;
-    const int c = u % p.NC; u /= p.NC;
+    u /= p.NC;
     const int k = u % p.MT; u /= p.MT;
     const int j = u % p.J;
     const int i = u / p.J;
-    (void)c;
     if (k >= i && i < p.steps && update_valid(p, i, j)) {
       if (p.mode == kModeBuildQ)   // panel + chain from the tile below + step i+1's write of (k, j)
         deps = 1 + (k < p.MT - 1 ? 1 : 0) + ((k > i && j > i && i + 1 < p.steps) ? 1 : 0);
-      else
-        deps = 1 + (k > i ? 1 : 0) + (i > 0 ? 1 : 0);
+      else   // panel (unless given) + the chain above in the domain + the previous step's write
+        deps = (p.skip_panels ? 0 : 1) + (is_top(p, i, k) ? 0 : 1) + (i > 0 ? 1 : 0);
     }
+  } else if (id < ttprep_base(p)) {
+    // merge block b of domain d: block b - 1, domain d's chain (its last tile,
+    // block b), the previous merge's block b (domain 0's chain for d = 1)
+    int u = id - U1;
+    const int b = u % p.nblk; u /= p.nblk;
+    const int d = u % p.dmax, i = u / p.dmax;
+    if (i < p.steps && d >= 1 && d < n_domains(p, i) && !p.skip_panels) deps = (b > 0 ? 1 : 0) + 2;
+  } else if (id < ttmqr_base(p)) {
+    const int u = id - ttprep_base(p);
+    const int d = u % p.dmax, i = u / p.dmax;
+    if (i < p.steps && d >= 1 && d < n_domains(p, i) && !p.skip_panels) deps = 1;
+  } else {
+    // merge update: the merge (unless given), domain d's chain on column j,
+    // the previous merge update (domain 0's chain for d = 1)
+    int u = id - ttmqr_base(p);
+    u /= p.NC;
+    const int d = u % p.dmax; u /= p.dmax;
+    const int j = u % p.J, i = u / p.J;
+    if (i < p.steps && d >= 1 && d < n_domains(p, i) && update_valid(p, i, j))
+      deps = (p.skip_panels ? 0 : 1) + 2;
   }
   p.cnt[id] = deps;
 }
@@ -278,15 +382,30 @@ __global__ void dag_seed_kernel(DagParams p) {
 }
 
 // --- releases after a task ---------------------------------------------------------
+// Step i has finished tile (k, j): its next consumer is step i + 1's update
+// (or, in the factorization, its panel task when j = i + 1).
+__device__ __forceinline__ void release_mem(const DagParams& p, int i, int j, int k, int c, int* keep) {
+  if (i + 1 >= p.steps) return;
+  if (p.mode == kModeFactor && j == i + 1)
+    release(p, panel_id(p, i + 1, k, 0));
+  else
+    release(p, update_id(p, i + 1, j, k, c), keep);
+}
+
 // keep: receives at most one ready low-priority dependent to run next.
 __device__ void release_dependents(const DagParams& p, const TaskDesc& t, int* keep) {
   if (t.type == kGEQRT || t.type == kTSQRT || t.type == kTBUILD || t.type == kOZPREP) {
     const bool feeds_prep = (t.type == kGEQRT || t.type == kTSQRT) && p.prep;
     const bool panel = (t.type == kGEQRT || t.type == kTSQRT);
     if (panel) {
-      // the next inner block of this tile, the same block of the tile below
+      // the next inner block of this tile; the same block of the tile below in
+      // the domain, or, from a domain's last tile, of the domain's merge
+      const int d = dom_of(p, t.i, t.k);
       if (t.c + 1 < p.nblk) release(p, panel_id(p, t.i, t.k, t.c + 1));
-      if (t.k + 1 < p.MT) release(p, panel_id(p, t.i, t.k + 1, t.c));
+      if (t.k + 1 < dom_end(p, t.i, d))
+        release(p, panel_id(p, t.i, t.k + 1, t.c));
+      else if (n_domains(p, t.i) > 1)
+        release(p, merge_id(p, t.i, d >= 1 ? d : 1, t.c));
       if (t.c + 1 < p.nblk) return;   // the tile's V, T, TAU are complete after its last block
     }
     if (feeds_prep) {
@@ -299,6 +418,27 @@ __device__ void release_dependents(const DagParams& p, const TaskDesc& t, int* k
     }
     return;
   }
+  if (t.type == kTTQRT || t.type == kTTPREP) {
+    const int d = dom_of(p, t.i, t.k);
+    if (t.type == kTTQRT) {
+      if (t.c + 1 < p.nblk) release(p, merge_id(p, t.i, d, t.c + 1));
+      if (d + 1 < n_domains(p, t.i)) release(p, merge_id(p, t.i, d + 1, t.c));
+      if (t.c + 1 < p.nblk) return;
+      if (p.prep) {
+        release(p, ttprep_id(p, t.i, d));
+        return;
+      }
+    }
+    for (int j = t.i + 1; j < p.NT; j++)
+      for (int c = 0; c < p.NC; c++) release(p, ttmqr_id(p, t.i, j, d, c));
+    return;
+  }
+  if (t.type == kTTMQR) {
+    const int d = dom_of(p, t.i, t.k);
+    if (d + 1 < n_domains(p, t.i)) release(p, ttmqr_id(p, t.i, t.j, d + 1, t.c), keep);
+    release_mem(p, t.i, t.j, t.k, t.c, keep);   // the domain top's tile row is final
+    return;
+  }
   if (p.mode == kModeBuildQ) {
     // the chain runs from the bottom tile up to the LARFB; the step before
     // (i - 1) next writes tile (k, j), which this task wrote last
@@ -306,15 +446,16 @@ __device__ void release_dependents(const DagParams& p, const TaskDesc& t, int* k
     if (t.i >= 1) release(p, update_id(p, t.i - 1, t.j, t.k, t.c), keep);
     return;
   }
-  // LARFB / SSRFB: LIN to the next task of this column chain
-  if (t.k + 1 < p.MT) release(p, update_id(p, t.i, t.j, t.k + 1, t.c), keep);
-  // MEM to the next step (only SSRFB: LARFB's tile row is final)
-  if (t.type == kSSRFB && t.i + 1 < p.steps) {
-    if (p.mode == kModeFactor && t.j == t.i + 1)
-      release(p, panel_id(p, t.i + 1, t.k, 0));
-    else
-      release(p, update_id(p, t.i + 1, t.j, t.k, t.c), keep);
-  }
+  // LARFB / SSRFB: LIN to the next task of this domain's column chain, or from
+  // the domain's last tile to its merge update
+  const int d = dom_of(p, t.i, t.k);
+  if (t.k + 1 < dom_end(p, t.i, d))
+    release(p, update_id(p, t.i, t.j, t.k + 1, t.c), keep);
+  else if (n_domains(p, t.i) > 1)
+    release(p, ttmqr_id(p, t.i, t.j, d >= 1 ? d : 1, t.c), keep);
+  // MEM: an SSRFB's lower tile is final for this step (a LARFB's tile row is
+  // final, or, at a domain top, finished by the merge update)
+  if (t.type == kSSRFB) release_mem(p, t.i, t.j, t.k, t.c, keep);
 }
 
 // --- T build for the Q^T application (diagonal w x w blocks from V, TAU) -------
@@ -379,13 +520,14 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
     const long long c0 = clock64();
     if (threadIdx.x == 0) local_cyc[kStatSched] += (unsigned long long)(c0 - cp);
     switch (t.type) {
-      case kGEQRT: {
-        const size_t o = tile_off(t.i, t.i, p.MT, NB);
-        task_geqrt_blk(p.A + o, p.T + o, p.TAU + tau_off(t.i, t.i, p.MT, NB), p.sh, smem, p.sp, t.c);
+      case kGEQRT: {   // the diagonal tile or a domain's top tile
+        const size_t o = tile_off(t.k, t.i, p.MT, NB);
+        task_geqrt_blk(p.A + o, p.T + o, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.sh, smem, p.sp, t.c);
         break;
       }
-      case kTSQRT: {
-        const size_t o1 = tile_off(t.i, t.i, p.MT, NB), o2 = tile_off(t.k, t.i, p.MT, NB);
+      case kTSQRT: {   // R of the domain's top tile over tile (k, i)
+        const int top = dom_top(p, t.i, dom_of(p, t.i, t.k));
+        const size_t o1 = tile_off(top, t.i, p.MT, NB), o2 = tile_off(t.k, t.i, p.MT, NB);
         task_tsqrt_blk(p.A + o1, p.A + o2, p.T + o2, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.sh, smem, p.sp,
                        t.c);
         break;
@@ -399,18 +541,19 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
         if (OZ) {
           const size_t o = tile_off(t.k, t.i, p.MT, NB);
           const size_t slot = panel_slot(p.MT, t.i, t.k);
-          task_ozprep(p.A + o, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.T + o, t.k == t.i,
+          task_ozprep(p.A + o, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.T + o,
+                      is_top(p, t.i, t.k) ? kVUnitLower : kVDense,
                       p.slices + slot * oz::panel_slice_bytes(), p.sexp + slot * 3 * NB,
                       reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr, p.mode != kModeBuildQ);
         }
         break;
       }
-      case kLARFB: {
-        const size_t ov = tile_off(t.i, t.i, p.MT, NB), oc = tile_off(t.i, t.j, p.MT, NB);
+      case kLARFB: {   // tile row k = the diagonal or a domain top
+        const size_t ov = tile_off(t.k, t.i, p.MT, NB), oc = tile_off(t.k, t.j, p.MT, NB);
         if (OZ) {
           oz::Ctx c;
           oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
-          const size_t slot = panel_slot(p.MT, t.i, t.i);
+          const size_t slot = panel_slot(p.MT, t.i, t.k);
           task_ozapply(c, p.slices + slot * oz::panel_slice_bytes(), p.sexp + slot * 3 * NB, nullptr,
                        p.C + oc + (size_t)t.c * oz::kN * NB);
         } else {
@@ -419,9 +562,10 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
         }
         break;
       }
-      case kSSRFB: {
+      case kSSRFB: {   // A1 = the domain top's tile row
+        const int top = dom_top(p, t.i, dom_of(p, t.i, t.k));
         const size_t ov = tile_off(t.k, t.i, p.MT, NB);
-        const size_t o1 = tile_off(t.i, t.j, p.MT, NB), o2 = tile_off(t.k, t.j, p.MT, NB);
+        const size_t o1 = tile_off(top, t.j, p.MT, NB), o2 = tile_off(t.k, t.j, p.MT, NB);
         if (OZ) {
           oz::Ctx c;
           oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
@@ -435,6 +579,36 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
         }
         break;
       }
+      case kTTQRT: {   // merge of domain top t.k's R into R(i, i): FP64 on the panel path
+        const size_t slot = merge_slot(p, t.i, dom_of(p, t.i, t.k));
+        task_tsqrt_blk(p.A + tile_off(t.i, t.i, p.MT, NB), p.A + tile_off(t.k, t.i, p.MT, NB),
+                       p.T2 + slot * tsz, p.TAU2 + slot * NB, p.sh, smem, p.sp, t.c, true);
+        break;
+      }
+      case kTTPREP: {
+        if (OZ) {
+          const size_t slot = merge_slot(p, t.i, dom_of(p, t.i, t.k));
+          task_ozprep(p.A + tile_off(t.k, t.i, p.MT, NB), p.TAU2 + slot * NB, p.T2 + slot * tsz, kVUpper,
+                      p.slices2 + slot * oz::panel_slice_bytes(), p.sexp2 + slot * 3 * NB,
+                      reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr, true);
+        }
+        break;
+      }
+      case kTTMQR: {   // the merge's reflectors on [row i; the domain top's row] of column j
+        const size_t slot = merge_slot(p, t.i, dom_of(p, t.i, t.k));
+        const size_t o1 = tile_off(t.i, t.j, p.MT, NB), o2 = tile_off(t.k, t.j, p.MT, NB);
+        if (OZ) {
+          oz::Ctx c;
+          oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
+          const size_t cofs = (size_t)t.c * oz::kN * NB;
+          task_ozapply(c, p.slices2 + slot * oz::panel_slice_bytes(), p.sexp2 + slot * 3 * NB,
+                       p.C + o1 + cofs, p.C + o2 + cofs);
+        } else {
+          task_ssrfb(p.C + o1, p.C + o2, p.A + tile_off(t.k, t.i, p.MT, NB), p.T2 + slot * tsz,
+                     t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp, false, true);
+        }
+        break;
+      }
       default:
         if (threadIdx.x == 0) atomicOr((int*)(p.ctl + kErr), kErrBadTask);
     }
@@ -442,9 +616,9 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
-      local_cnt[t.type]++;
+      local_cnt[stat_slot(t.type)]++;
       const long long c1 = clock64();
-      local_cyc[t.type] += (unsigned long long)(c1 - c0);
+      local_cyc[stat_slot(t.type)] += (unsigned long long)(c1 - c0);
       release_dependents(p, t, &next);
       __threadfence();
       atomicAdd(p.ctl + kDone, 1u);

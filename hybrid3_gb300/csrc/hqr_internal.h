@@ -65,13 +65,33 @@ struct OzWorkspace {
 // Bytes of the split-precision workspace for a geometry (NB = 128).
 size_t oz_slice_bytes(const Geometry& g);
 size_t oz_exp_bytes(const Geometry& g);
+size_t oz_panel_bytes();   // prepared operands of one panel tile
 bool oz_supported(const Geometry& g);
 // Inner block width of the FP64 panels for the split path (see hqr_dag.cu).
 int narrow_panels(Geometry* g);
 
+// Domain tree of a plan: domains of S tiles (0: the flat tree) and the
+// merges' storage, compact per (step i, domain d): T2 tile (i*dmax + d), TAU2
+// (i*dmax + d)*NB, and for split precision their prepared operands.
+struct TreeWorkspace {
+  int S = 0;
+  double* T2 = nullptr;
+  double* TAU2 = nullptr;
+  uint8_t* slices2 = nullptr;
+  int* sexp2 = nullptr;
+};
+// Number of merge slots of a tree with domains of S tiles (steps * dmax).
+size_t tree_slots(const Geometry& g, int S);
+
 // Enqueue a factorization DAG on `stream` (no synchronisation).
 int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, double* dTAU,
-                  long long timeout_ns, cudaStream_t stream, const OzWorkspace* oz = nullptr);
+                  long long timeout_ns, cudaStream_t stream, const OzWorkspace* oz = nullptr,
+                  const TreeWorkspace* tw = nullptr);
+// C <- Q^T C for a factorization with a domain tree, from the T factors (or
+// split slices) that factorization left in dT / tw / oz.
+int launch_apply_qt_tree(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT,
+                         const double* dTAU, double* dC, int CT, long long timeout_ns, cudaStream_t stream,
+                         const OzWorkspace* oz, const TreeWorkspace* tw);
 // Enqueue C <- Q^T C (C has CT tile columns, same MT/NB as A); the panel
 // tasks rebuild T from V/TAU (FP64: diagonal blocks; split: full T + slices).
 int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT,

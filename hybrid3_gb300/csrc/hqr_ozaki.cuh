@@ -317,9 +317,10 @@ __device__ __forceinline__ void y_exponents(Ctx& c) {
 }
 
 // Stage the right operand Y (kK x kN, column-major, ld ldy, global) in
-// shared memory.  unit_col >= 0: Y is the column block starting at column
-// unit_col of a unit-lower V (zero above the diagonal, one on it).
-__device__ __forceinline__ void stage_y(Ctx& c, const double* Y, int ldy, int unit_col) {
+// shared memory.  col0 >= 0: Y is the column block starting at column col0 of
+// a unit-lower V (zero above the diagonal, one on it), or with `upper` of an
+// upper-triangular V (zero below the diagonal).
+__device__ __forceinline__ void stage_y(Ctx& c, const double* Y, int ldy, int col0, bool upper = false) {
   static_assert(kK * kN / 2 % kThreads == 0, "staging loop");
   constexpr int kIter = kK * kN / 2 / kThreads;   // pairs per thread
 #pragma unroll 4
@@ -327,10 +328,15 @@ __device__ __forceinline__ void stage_y(Ctx& c, const double* Y, int ldy, int un
     const int e = threadIdx.x + it * kThreads;
     const int col = e / (kK / 2), r = 2 * (e % (kK / 2));
     double2 v = __ldcg(reinterpret_cast<const double2*>(Y + (size_t)col * ldy + r));
-    if (unit_col >= 0) {
-      const int gc = unit_col + col;
-      v.x = (r > gc) ? v.x : (r == gc ? 1.0 : 0.0);
-      v.y = (r + 1 > gc) ? v.y : (r + 1 == gc ? 1.0 : 0.0);
+    if (col0 >= 0) {
+      const int gc = col0 + col;
+      if (upper) {
+        v.x = (r <= gc) ? v.x : 0.0;
+        v.y = (r + 1 <= gc) ? v.y : 0.0;
+      } else {
+        v.x = (r > gc) ? v.x : (r == gc ? 1.0 : 0.0);
+        v.y = (r + 1 > gc) ? v.y : (r + 1 == gc ? 1.0 : 0.0);
+      }
     }
     *reinterpret_cast<double2*>(c.sY + col * kLdY + r) = v;
   }
@@ -614,6 +620,8 @@ enum Kind : int {
   kDense = 0,
   kUnitLower = 1,    // V of a GEQRT tile: zero above the diagonal, one on it
   kUnitUpper = 2,    // V^T of a GEQRT tile
+  kUpperIncl = 3,    // V of a TT merge: upper triangle with the diagonal, zero below
+  kLowerIncl = 4,    // V^T of a TT merge
 };
 
 // Slice the 128 x 128 left operand X(r, k) = acc(r, k) (shared memory) into
@@ -662,6 +670,8 @@ struct StagedAcc {
     const double x = s[r * rs + k * ks];
     if (kind == kUnitLower) return (r > k) ? x : (r == k ? 1.0 : 0.0);
     if (kind == kUnitUpper) return (k > r) ? x : (k == r ? 1.0 : 0.0);
+    if (kind == kUpperIncl) return (r <= k) ? x : 0.0;
+    if (kind == kLowerIncl) return (r >= k) ? x : 0.0;
     return x;
   }
 };

@@ -59,13 +59,19 @@ inline __device__ void t_recurrence(const double* sG, double* sT, const double* 
   }
 }
 
-// OZPREP of panel tile V (global, NB x NB; unit: the V of a GEQRT tile, else
-// the dense V of a TSQRT tile) with TAU tau.  G: NB x NB global scratch.
+// Shape of a panel tile's reflectors V.
+enum VKind : int {
+  kVDense = 0,       // TSQRT: the whole tile
+  kVUnitLower = 1,   // GEQRT: strictly below the diagonal, unit diagonal
+  kVUpper = 2,       // TT merge: the upper triangle with the diagonal
+};
+
+// OZPREP of panel tile V (global, NB x NB, of shape vkind) with TAU tau.  G: NB x NB global scratch.
 // slices / exps: this tile's prepared operands and row exponents; the middle
 // operand is T^T (applying H^T) or, with t_transposed false, T (applying H).
 // sm: the CTA's dynamic shared memory (oz::kSmemBytes).  False on a device
 // time-out.
-inline __device__ bool task_ozprep(const double* V, const double* tau, double* G, bool unit,
+inline __device__ bool task_ozprep(const double* V, const double* tau, double* G, int vkind,
                                    uint8_t* slices, int* exps, uint8_t* sm, uint32_t tmem,
                                    unsigned* err, bool t_transposed) {
   using namespace oz;
@@ -75,10 +81,10 @@ inline __device__ bool task_ozprep(const double* V, const double* tau, double* G
     double* sV = reinterpret_cast<double*>(sm);
     int* sE = reinterpret_cast<int*>(sm + kLdT * kK * 8);
     stage_tile(sV, V);
-    slice_left(StagedAcc{sV, kLdT, 1, unit ? kUnitUpper : kDense}, slices + kOzVT * ob,
-               exps + kOzVT * kK, sE);
-    slice_left(StagedAcc{sV, 1, kLdT, unit ? kUnitLower : kDense}, slices + kOzV * ob,
-               exps + kOzV * kK, sE);
+    const int kt = vkind == kVUnitLower ? kUnitUpper : vkind == kVUpper ? kLowerIncl : kDense;
+    const int kv = vkind == kVUnitLower ? kUnitLower : vkind == kVUpper ? kUpperIncl : kDense;
+    slice_left(StagedAcc{sV, kLdT, 1, kt}, slices + kOzVT * ob, exps + kOzVT * kK, sE);
+    slice_left(StagedAcc{sV, 1, kLdT, kv}, slices + kOzV * ob, exps + kOzV * kK, sE);
   }
   // 2. G = V^T V on the tensor cores, by 64-column blocks, into G (global)
   {
@@ -86,7 +92,7 @@ inline __device__ bool task_ozprep(const double* V, const double* tau, double* G
     ctx_init(c, sm, tmem, err);
     for (int cb = 0; cb < kK / kN; cb++) {
       prefetch(c, slices + kOzVT * ob);
-      stage_y(c, V + (size_t)cb * kN * kK, kK, unit ? cb * kN : -1);
+      stage_y(c, V + (size_t)cb * kN * kK, kK, vkind == kVDense ? -1 : cb * kN, vkind == kVUpper);
       if (!product(c, slices + kOzVT * ob, (cb + 1 < kK / kN) ? slices + kOzVT * ob : nullptr,
                    exps + kOzVT * kK, kEpiStore, G + (size_t)cb * kN * kK, kK, nullptr, 0))
         return false;

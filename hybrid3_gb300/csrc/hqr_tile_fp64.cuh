@@ -384,11 +384,14 @@ __device__ void build_t_block(const double* V, int ldv, int m, int w, bool unit,
 // (notrans: H itself, W = T W).
 // Vt: w x w unit lower (unit_top) or the identity; Vb: mb x w.  V and T are
 // read from global memory (ld ldv / ldt).  ncol must be a multiple of 8.
+// v_col0 >= 0: Vb is upper triangular (a TT merge's reflectors, stored in the
+// upper triangle of a tile whose lower part holds other data): element
+// (mb_off + r, c) is used when mb_off + r <= v_col0 + c, else taken as zero.
 // ---------------------------------------------------------------------------
 __device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off,
                               const double* __restrict__ gT, int ldt, int w, int mb, bool unit_top,
                               double* Ct, int ldct, double* Cb, int ldcb, int ncol, double* smem,
-                              const SmemPlan& sp, int RC, bool notrans = false) {
+                              const SmemPlan& sp, int RC, bool notrans = false, int v_col0 = -1) {
   double* sVb = smem + sp.off_vb;
   double* sVt = smem + sp.off_vt;
   double* sT = smem + sp.off_t;
@@ -423,7 +426,8 @@ __device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off
     __syncthreads();
     for (int e = tid; e < rc * w; e += kThreads) {
       const int r = e % rc, c = e / rc;
-      sVb[r + c * ldvs] = ldg_cg(gV + mb_off + r0 + r + (size_t)c * ldv);
+      sVb[r + c * ldvs] = (v_col0 < 0 || mb_off + r0 + r <= v_col0 + c)
+                              ? ldg_cg(gV + mb_off + r0 + r + (size_t)c * ldv) : 0.0;
     }
     __syncthreads();
     if (active) {
@@ -479,7 +483,8 @@ __device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off
     __syncthreads();
     for (int e = tid; e < rc * w; e += kThreads) {
       const int r = e % rc, c = e / rc;
-      sVb[r + c * ldvs] = ldg_cg(gV + mb_off + r0 + r + (size_t)c * ldv);
+      sVb[r + c * ldvs] = (v_col0 < 0 || mb_off + r0 + r <= v_col0 + c)
+                              ? ldg_cg(gV + mb_off + r0 + r + (size_t)c * ldv) : 0.0;
     }
     __syncthreads();
     for (int e = tid; e < rc * G8; e += kThreads) {
@@ -515,6 +520,20 @@ __device__ void store_block(double* g, int ldg, const double* s, int lds, int m,
   for (int e = threadIdx.x; e < m * n; e += kThreads) {
     const int r = e % m, c = e / m;
     stg_cg(g + r + (size_t)c * ldg, s[r + (size_t)c * lds]);
+  }
+}
+// The upper part (row r <= col0 + c) of an m x n block, zero below; and its
+// store (a TT merge's panel columns).
+__device__ void load_block_upper(double* s, int lds, const double* g, int ldg, int m, int n, int col0) {
+  for (int e = threadIdx.x; e < m * n; e += kThreads) {
+    const int r = e % m, c = e / m;
+    s[r + (size_t)c * lds] = (r <= col0 + c) ? ldg_cg(g + r + (size_t)c * ldg) : 0.0;
+  }
+}
+__device__ void store_block_upper(double* g, int ldg, const double* s, int lds, int m, int n, int col0) {
+  for (int e = threadIdx.x; e < m * n; e += kThreads) {
+    const int r = e % m, c = e / m;
+    if (r <= col0 + c) stg_cg(g + r + (size_t)c * ldg, s[r + (size_t)c * lds]);
   }
 }
 
@@ -569,8 +588,13 @@ __device__ void task_geqrt(double* A, double* T, double* tau_g, const TileShape&
 // right of it.  Of A1 it touches rows [b w, (b+1) w) only, and those rows are
 // touched by no other block of this TSQRT: once block b is done here, block b
 // of the TSQRT of the next tile below may run.
+// a2_upper: the TT merge (CORE_dttqrt): A2 is upper triangular (the R of a
+// domain's top tile; its strict lower part holds that tile's GEQRT reflectors
+// and is neither read nor written).  The reflectors keep A2's shape, so the
+// same arithmetic on A2 with zeros below the diagonal is exact, and only the
+// upper triangle is stored back.
 __device__ void task_tsqrt_blk(double* A1, double* A2, double* T, double* tau_g, const TileShape& sh,
-                               double* smem, const SmemPlan& sp, int b) {
+                               double* smem, const SmemPlan& sp, int b, bool a2_upper = false) {
   const int NB = sh.NB, w = sh.w;
   double* sA = smem + sp.off_c1;     // NB x w panel of A2
   double* sR = smem + sp.off_vt;     // w x w block of R
@@ -580,13 +604,19 @@ __device__ void task_tsqrt_blk(double* A1, double* A2, double* T, double* tau_g,
   {
     const int i0 = b * w;
     __syncthreads();
-    load_block(sA, NB, A2 + (size_t)i0 * NB, NB, NB, w);
+    if (a2_upper)
+      load_block_upper(sA, NB, A2 + (size_t)i0 * NB, NB, NB, w, i0);
+    else
+      load_block(sA, NB, A2 + (size_t)i0 * NB, NB, NB, w);
     load_block(sR, w, A1 + i0 + (size_t)i0 * NB, NB, w, w);
     __syncthreads();
     panel_qr_ts_fused(sR, w, sA, NB, NB, w, sTau, sG);
     if (threadIdx.x < 32) t_from_gram(sG, sTau, sTb, w);
     __syncthreads();
-    store_block(A2 + (size_t)i0 * NB, NB, sA, NB, NB, w);
+    if (a2_upper)
+      store_block_upper(A2 + (size_t)i0 * NB, NB, sA, NB, NB, w, i0);
+    else
+      store_block(A2 + (size_t)i0 * NB, NB, sA, NB, NB, w);
     for (int e = threadIdx.x; e < w * w; e += kThreads) {
       const int r = e % w, c = e / w;
       if (r <= c) stg_cg(A1 + i0 + r + (size_t)(i0 + c) * NB, sR[r + c * w]);
@@ -599,13 +629,17 @@ __device__ void task_tsqrt_blk(double* A1, double* A2, double* T, double* tau_g,
       double* sCt = smem + sp.off_c1;  // w x ncol rows of R (the panel area is free now)
       double* sCb = smem + sp.off_c1 + w * sh.CB;  // NB x ncol of A2 after the R rows
       __syncthreads();
+      // A TT merge's block reflectors reach rows < i0 + w of A2 only: the rows
+      // below belong to the domain top's own later blocks, which its chain may
+      // still be updating, so they are neither read nor written here.
+      const int mrows = a2_upper ? i0 + w : NB;
       load_block(sCt, w, A1 + i0 + (size_t)c0 * NB, NB, w, ncol);
-      load_block(sCb, NB, A2 + (size_t)c0 * NB, NB, NB, ncol);
+      load_block(sCb, NB, A2 + (size_t)c0 * NB, NB, mrows, ncol);
       __syncthreads();
-      apply_block_t(A2 + (size_t)i0 * NB, NB, 0, T + i0 + (size_t)i0 * NB, NB, w, NB, false, sCt, w,
-                    sCb, NB, ncol, smem, sp, sh.RC);
+      apply_block_t(A2 + (size_t)i0 * NB, NB, 0, T + i0 + (size_t)i0 * NB, NB, w, mrows, false, sCt, w,
+                    sCb, NB, ncol, smem, sp, sh.RC, false, a2_upper ? i0 : -1);
       store_block(A1 + i0 + (size_t)c0 * NB, NB, sCt, w, w, ncol);
-      store_block(A2 + (size_t)c0 * NB, NB, sCb, NB, NB, ncol);
+      store_block(A2 + (size_t)c0 * NB, NB, sCb, NB, mrows, ncol);
     }
   }
   __syncthreads();
@@ -638,10 +672,11 @@ __device__ void task_larfb(const double* V, const double* T, double* C, int c0, 
 
 // CORE_dtsmqr(Left, Trans, NB, ncol, NB, ncol, NB, IB, A1, NB, A2, NB, V, NB,
 // T, NB) on columns [c0, c0+ncol) of A1 and A2 (notrans: Left, NoTrans, the
-// inner blocks in reverse order).
+// inner blocks in reverse order).  v_upper: CORE_dttmqr, V is the upper
+// triangle (with the diagonal) of its tile.
 __device__ void task_ssrfb(double* A1, double* A2, const double* V, const double* T, int c0,
                            int ncol, const TileShape& sh, double* smem, const SmemPlan& sp,
-                           bool notrans = false) {
+                           bool notrans = false, bool v_upper = false) {
   const int NB = sh.NB, w = sh.w;
   double* s1 = smem + sp.off_c1;
   double* s2 = smem + sp.off_c2;
@@ -652,7 +687,7 @@ __device__ void task_ssrfb(double* A1, double* A2, const double* V, const double
   for (int b = 0; b < NB / w; b++) {
     const int i0 = (notrans ? NB / w - 1 - b : b) * w;
     apply_block_t(V + (size_t)i0 * NB, NB, 0, T + i0 + (size_t)i0 * NB, NB, w, NB, false, s1 + i0, NB,
-                  s2, NB, ncol, smem, sp, sh.RC, notrans);
+                  s2, NB, ncol, smem, sp, sh.RC, notrans, v_upper ? i0 : -1);
   }
   store_block(A1 + (size_t)c0 * NB, NB, s1, NB, NB, ncol);
   store_block(A2 + (size_t)c0 * NB, NB, s2, NB, NB, ncol);

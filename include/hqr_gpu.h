@@ -72,6 +72,19 @@ void hqr_set_timeout_ms(long long ms);
  * to 512; IB a divisor of NB (inner blocks of min(IB, 32) columns are used). */
 int hqr_plan_create(hqr_plan_t **plan, long M, long N, int NB, int IB, int precision);
 int hqr_plan_destroy(hqr_plan_t *plan);
+/* No counterpart in the reference (its TS reduction is the flat tree).  Domain
+ * tree for the factorizations on this plan: at step i the tile rows i.. are
+ * cut into domains of domain_tiles tiles; each domain runs the flat TS chain
+ * on its own top tile (GEQRT + TSQRT), then the domain tops' R are merged into
+ * R(i, i) one after the other by triangle-on-triangle QRs (CORE_dttqrt /
+ * CORE_dttmqr).  The TS chain down a panel shrinks from MT - i tiles to
+ * domain_tiles + the number of domains, for tall-skinny matrices.  0 (the
+ * default) or domain_tiles >= MT: the flat tree of the reference.  With a tree,
+ * R is the same (up to the signs of its rows) but the reflectors differ: the
+ * merges' T factors and TAU live in the plan, so hqr_ormqr_t and hqr_make_q
+ * need use_plan_t = 1 (HQR_ERR_UNSUPPORTED otherwise) and Q is built by the
+ * forward application.  Allocates the merges' storage. */
+int hqr_plan_set_tree(hqr_plan_t *plan, int domain_tiles);
 /* Device T factors of the last factorization: NB x NB upper-triangular tile
  * per panel tile, same tile layout as A (only the w x w diagonal blocks are
  * written by the factorization). */
