@@ -519,6 +519,19 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
     const TaskDesc t = decode(p, id);
     const long long c0 = clock64();
     if (threadIdx.x == 0) local_cyc[kStatSched] += (unsigned long long)(c0 - cp);
+    // Each heavy task body has one call site (the split engine, the panel
+    // preparation and the TS/TT panel block are large when inlined): the
+    // cases only pick their operands.
+    const uint8_t* oz_slices = nullptr;   // an update on the tensor cores
+    const int* oz_exps = nullptr;
+    double *oz_top = nullptr, *oz_bot = nullptr;
+    const double *prep_v = nullptr, *prep_tau = nullptr;   // a split panel preparation
+    double* prep_g = nullptr;
+    uint8_t* prep_slices = nullptr;
+    int* prep_exps = nullptr;
+    int prep_kind = kVDense;
+    double *ts_a1 = nullptr, *ts_a2 = nullptr, *ts_t = nullptr, *ts_tau = nullptr;   // a TS/TT panel block
+    bool ts_upper = false;
     switch (t.type) {
       case kGEQRT: {   // the diagonal tile or a domain's top tile
         const size_t o = tile_off(t.k, t.i, p.MT, NB);
@@ -527,9 +540,20 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
       }
       case kTSQRT: {   // R of the domain's top tile over tile (k, i)
         const int top = dom_top(p, t.i, dom_of(p, t.i, t.k));
-        const size_t o1 = tile_off(top, t.i, p.MT, NB), o2 = tile_off(t.k, t.i, p.MT, NB);
-        task_tsqrt_blk(p.A + o1, p.A + o2, p.T + o2, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.sh, smem, p.sp,
-                       t.c);
+        const size_t o2 = tile_off(t.k, t.i, p.MT, NB);
+        ts_a1 = p.A + tile_off(top, t.i, p.MT, NB);
+        ts_a2 = p.A + o2;
+        ts_t = p.T + o2;
+        ts_tau = p.TAU + tau_off(t.k, t.i, p.MT, NB);
+        break;
+      }
+      case kTTQRT: {   // merge of domain top t.k's R into R(i, i): FP64 on the panel path
+        const size_t slot = merge_slot(p, t.i, dom_of(p, t.i, t.k));
+        ts_a1 = p.A + tile_off(t.i, t.i, p.MT, NB);
+        ts_a2 = p.A + tile_off(t.k, t.i, p.MT, NB);
+        ts_t = p.T2 + slot * tsz;
+        ts_tau = p.TAU2 + slot * NB;
+        ts_upper = true;
         break;
       }
       case kTBUILD: {
@@ -538,79 +562,69 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
         break;
       }
       case kOZPREP: {
-        if (OZ) {
-          const size_t o = tile_off(t.k, t.i, p.MT, NB);
-          const size_t slot = panel_slot(p.MT, t.i, t.k);
-          task_ozprep(p.A + o, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.T + o,
-                      is_top(p, t.i, t.k) ? kVUnitLower : kVDense,
-                      p.slices + slot * oz::panel_slice_bytes(), p.sexp + slot * 3 * NB,
-                      reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr, p.mode != kModeBuildQ);
-        }
+        const size_t o = tile_off(t.k, t.i, p.MT, NB);
+        const size_t slot = panel_slot(p.MT, t.i, t.k);
+        prep_v = p.A + o;
+        prep_tau = p.TAU + tau_off(t.k, t.i, p.MT, NB);
+        prep_g = p.T + o;
+        prep_kind = is_top(p, t.i, t.k) ? kVUnitLower : kVDense;
+        prep_slices = p.slices + slot * oz::panel_slice_bytes();
+        prep_exps = p.sexp + slot * 3 * NB;
+        break;
+      }
+      case kTTPREP: {
+        const size_t slot = merge_slot(p, t.i, dom_of(p, t.i, t.k));
+        prep_v = p.A + tile_off(t.k, t.i, p.MT, NB);
+        prep_tau = p.TAU2 + slot * NB;
+        prep_g = p.T2 + slot * tsz;
+        prep_kind = kVUpper;
+        prep_slices = p.slices2 + slot * oz::panel_slice_bytes();
+        prep_exps = p.sexp2 + slot * 3 * NB;
         break;
       }
       case kLARFB: {   // tile row k = the diagonal or a domain top
         const size_t ov = tile_off(t.k, t.i, p.MT, NB), oc = tile_off(t.k, t.j, p.MT, NB);
         if (OZ) {
-          oz::Ctx c;
-          oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
           const size_t slot = panel_slot(p.MT, t.i, t.k);
-          task_ozapply(c, p.slices + slot * oz::panel_slice_bytes(), p.sexp + slot * 3 * NB, nullptr,
-                       p.C + oc + (size_t)t.c * oz::kN * NB);
+          oz_slices = p.slices + slot * oz::panel_slice_bytes();
+          oz_exps = p.sexp + slot * 3 * NB;
+          oz_bot = p.C + oc + (size_t)t.c * oz::kN * NB;
         } else {
           task_larfb(p.A + ov, p.T + ov, p.C + oc, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp,
                      p.mode == kModeBuildQ);
         }
         break;
       }
-      case kSSRFB: {   // A1 = the domain top's tile row
-        const int top = dom_top(p, t.i, dom_of(p, t.i, t.k));
+      case kSSRFB:     // A1 = the domain top's tile row
+      case kTTMQR: {   // the merge's reflectors on [row i; the domain top's row] of column j
+        const bool tt = t.type == kTTMQR;
+        const int top = tt ? t.i : dom_top(p, t.i, dom_of(p, t.i, t.k));
         const size_t ov = tile_off(t.k, t.i, p.MT, NB);
         const size_t o1 = tile_off(top, t.j, p.MT, NB), o2 = tile_off(t.k, t.j, p.MT, NB);
+        const size_t slot = tt ? merge_slot(p, t.i, dom_of(p, t.i, t.k)) : panel_slot(p.MT, t.i, t.k);
         if (OZ) {
-          oz::Ctx c;
-          oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
-          const size_t slot = panel_slot(p.MT, t.i, t.k);
           const size_t cofs = (size_t)t.c * oz::kN * NB;
-          task_ozapply(c, p.slices + slot * oz::panel_slice_bytes(), p.sexp + slot * 3 * NB,
-                       p.C + o1 + cofs, p.C + o2 + cofs);
+          oz_slices = (tt ? p.slices2 : p.slices) + slot * oz::panel_slice_bytes();
+          oz_exps = (tt ? p.sexp2 : p.sexp) + slot * 3 * NB;
+          oz_top = p.C + o1 + cofs;
+          oz_bot = p.C + o2 + cofs;
         } else {
-          task_ssrfb(p.C + o1, p.C + o2, p.A + ov, p.T + ov, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp,
-                     p.mode == kModeBuildQ);
-        }
-        break;
-      }
-      case kTTQRT: {   // merge of domain top t.k's R into R(i, i): FP64 on the panel path
-        const size_t slot = merge_slot(p, t.i, dom_of(p, t.i, t.k));
-        task_tsqrt_blk(p.A + tile_off(t.i, t.i, p.MT, NB), p.A + tile_off(t.k, t.i, p.MT, NB),
-                       p.T2 + slot * tsz, p.TAU2 + slot * NB, p.sh, smem, p.sp, t.c, true);
-        break;
-      }
-      case kTTPREP: {
-        if (OZ) {
-          const size_t slot = merge_slot(p, t.i, dom_of(p, t.i, t.k));
-          task_ozprep(p.A + tile_off(t.k, t.i, p.MT, NB), p.TAU2 + slot * NB, p.T2 + slot * tsz, kVUpper,
-                      p.slices2 + slot * oz::panel_slice_bytes(), p.sexp2 + slot * 3 * NB,
-                      reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr, true);
-        }
-        break;
-      }
-      case kTTMQR: {   // the merge's reflectors on [row i; the domain top's row] of column j
-        const size_t slot = merge_slot(p, t.i, dom_of(p, t.i, t.k));
-        const size_t o1 = tile_off(t.i, t.j, p.MT, NB), o2 = tile_off(t.k, t.j, p.MT, NB);
-        if (OZ) {
-          oz::Ctx c;
-          oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
-          const size_t cofs = (size_t)t.c * oz::kN * NB;
-          task_ozapply(c, p.slices2 + slot * oz::panel_slice_bytes(), p.sexp2 + slot * 3 * NB,
-                       p.C + o1 + cofs, p.C + o2 + cofs);
-        } else {
-          task_ssrfb(p.C + o1, p.C + o2, p.A + tile_off(t.k, t.i, p.MT, NB), p.T2 + slot * tsz,
-                     t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp, false, true);
+          task_ssrfb(p.C + o1, p.C + o2, p.A + ov, tt ? p.T2 + slot * tsz : p.T + ov, t.c * p.sh.CB,
+                     p.sh.CB, p.sh, smem, p.sp, p.mode == kModeBuildQ, tt);
         }
         break;
       }
       default:
         if (threadIdx.x == 0) atomicOr((int*)(p.ctl + kErr), kErrBadTask);
+    }
+    if (ts_a1) task_tsqrt_blk(ts_a1, ts_a2, ts_t, ts_tau, p.sh, smem, p.sp, t.c, ts_upper);
+    if (OZ && prep_v)
+      task_ozprep(prep_v, prep_tau, prep_g, prep_kind, prep_slices, prep_exps, reinterpret_cast<uint8_t*>(smem),
+                  s_tmem, p.ctl + kErr, p.mode != kModeBuildQ);
+    if (OZ && oz_bot) {
+      oz::Ctx c;
+      oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
+      task_ozapply(c, oz_slices, oz_exps, oz_top, oz_bot);
     }
     (void)tsz;
     __threadfence();

@@ -67,11 +67,14 @@ __host__ __device__ constexpr size_t panel_slice_bytes() { return 3 * operand_by
 // Pipeline depth: A chunks (bulk TMA) and sliced B chunks in flight.
 constexpr int kAStages = 3;
 constexpr int kBStages = 4;
+// done barriers: one per chunk in flight on either ring, so that no two
+// chunks a wait may still refer to share a barrier (parity waits stay exact)
+constexpr int kDoneStages = kAStages > kBStages ? kAStages : kBStages;
 constexpr int kSlicerWarps = kWarps - 1;   // warp 0 issues the copies and the MMAs
 // Barriers: a_full[kAStages] (TMA bytes), b_full[kBStages] (one arrival per
-// slicer warp), done[kBStages] (tcgen05.commit of one chunk's MMAs).
+// slicer warp), done[kDoneStages] (tcgen05.commit of one chunk's MMAs).
 constexpr int kBarAFull = 0, kBarBFull = kAStages, kBarDone = kAStages + kBStages;
-constexpr int kNumBars = kAStages + 2 * kBStages;
+constexpr int kNumBars = kAStages + kBStages + kDoneStages;
 // Shared-memory map of the engine.
 constexpr int kOffB = kAStages * kAChunkBytes;
 constexpr int kOffBar = kOffB + kBStages * kBChunkBytes;
@@ -428,21 +431,21 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
                      dB + (uint64_t)((q * kSliceBBytes) >> 4), id, acc);
           }
         }
-        mma_commit(c.bar + kBarDone + n % kBStages);
-        // refill the A stage of chunk n - 1 with chunk n + 2 once its MMAs are done
-        if (j >= 1 && j + 2 < kChunks) {
-          if (!wait_chunk(c, kBarDone, kBStages, n - 1)) {
+        mma_commit(c.bar + kBarDone + n % kDoneStages);
+        // refill the A stage of chunk n - 1 with chunk n - 1 + kAStages once its MMAs are done
+        if (j >= 1 && j + kAStages - 1 < kChunks) {
+          if (!wait_chunk(c, kBarDone, kDoneStages, n - 1)) {
             ok = false;
             break;
           }
-          issue_a(c, X, j + 2, n + 2);
-          c.na = n + 3;
+          issue_a(c, X, j + kAStages - 1, n + kAStages - 1);
+          c.na = n + kAStages;
         }
       }
-      // prefetch the next product's first chunks into the stages of the last three
+      // prefetch the next product's first chunks into the stages of the last kAStages
       if (ok && Xnext) {
         for (int j = 0; j < kAStages; j++) {
-          if (!wait_chunk(c, kBarDone, kBStages, n0 + kChunks - kAStages + j)) {
+          if (!wait_chunk(c, kBarDone, kDoneStages, n0 + kChunks - kAStages + j)) {
             ok = false;
             break;
           }
@@ -459,7 +462,7 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
     int g = ts;
     for (int j = 0; j < kChunks && ok; j++) {
       const int n = n0 + j;
-      if (n >= kBStages && !wait_chunk(c, kBarDone, kBStages, n - kBStages)) {
+      if (n >= kBStages && !wait_chunk(c, kBarDone, kDoneStages, n - kBStages)) {
         ok = false;
         break;
       }
@@ -471,7 +474,7 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
     }
   }
   // every thread: the last chunk's MMAs (and with them all earlier ones) are done
-  if (ok && !wait_chunk(c, kBarDone, kBStages, n0 + kChunks - 1)) ok = false;
+  if (ok && !wait_chunk(c, kBarDone, kDoneStages, n0 + kChunks - 1)) ok = false;
   tc_fence_after();
   c.n = n0 + kChunks;
   ok = __syncthreads_and(ok) != 0;   // uniform across the CTA
