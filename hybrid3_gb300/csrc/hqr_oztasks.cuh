@@ -28,33 +28,56 @@ struct PackedTAcc {
   }
 };
 
-// T recurrence (dlarft 'F','C', k = NB = 128) in shared memory:
-//   T(c, c) = tau_c;  T(0:c, c) = -tau_c T(0:c, 0:c) G(0:c, c)  (zero when tau_c = 0)
+// T recurrence (dlarft 'F','C', k = NB = 128) in shared memory,
+//   T(c, c) = tau_c;  T(0:c, c) = -tau_c T(0:c, 0:c) G(0:c, c)  (zero when tau_c = 0),
+// regrouped by blocks of 16 columns: first the diagonal 16 x 16 blocks (each
+// row runs its own scalar recurrence over its own row: no barrier), then for
+// block columns b = 1..7
+//   X = G(0:bw, bw:bw+16) T_bb,   T(0:bw, bw:bw+16) = -T(0:bw, 0:bw) X,
+// the same sums (tau_c = 0 leaves column c zero either way).  FP64 on this
+// part issues one warp instruction per ~19 cycles per SM, so the work is laid
+// out for full warps: the triangular product pairs rows r and bw-1-r, whose
+// dots add up to bw + 1 terms.  The scalar column recurrence left most lanes
+// of a warp idle on the short rows and took 2.6x longer.
 // sG: strictly upper part of G = V^T V, packed: G(b, c) (b < c) at c (c - 1) / 2 + b.
-// sT: the result, packed upper (see PackedTTAcc).  kTPR adjacent threads per
-// row split the sum over b.
-inline __device__ void t_recurrence(const double* sG, double* sT, const double* tau) {
-  constexpr int kTPR = kThreads / oz::kK;
-  static_assert(kTPR >= 1 && kTPR <= 32 && (kTPR & (kTPR - 1)) == 0, "row split");
-  const int a = threadIdx.x / kTPR, h = threadIdx.x % kTPR;
-  for (int c = 0; c < oz::kK; c++) {
-    const double tc = __ldcg(tau + c);
-    double s0 = 0.0, s1 = 0.0;
-    if (a < c) {
-      const int len = c - a;
-      const int b0 = a + (len * h) / kTPR, b1 = a + (len * (h + 1)) / kTPR;
-      const double* g = sG + c * (c - 1) / 2;
-      int b = b0;
-      for (; b + 1 < b1; b += 2) {
-        s0 = fma(sT[b * (b + 1) / 2 + a], g[b], s0);
-        s1 = fma(sT[(b + 1) * (b + 2) / 2 + a], g[b + 1], s1);
+// sT: the result, packed upper: T(a, b) (a <= b) at b (b + 1) / 2 + a.
+// sX: (NB - 16) x 16 doubles of scratch.
+inline __device__ void t_recurrence(const double* sG, double* sT, double* sX, const double* tau) {
+  constexpr int K = oz::kK, BS = 16;
+  const int tid = threadIdx.x;
+  if (tid < K) {
+    const int b = tid / BS, a = tid % BS;
+    for (int c = a; c < BS; c++) {
+      const int gc = b * BS + c;
+      const double tc = __ldcg(tau + gc);
+      double s = 0.0;
+      for (int d = a; d < c; d++) {
+        const int gd = b * BS + d;
+        s = fma(sT[gd * (gd + 1) / 2 + tid], sG[gc * (gc - 1) / 2 + gd], s);
       }
-      if (b < b1) s0 = fma(sT[b * (b + 1) / 2 + a], g[b], s0);
+      sT[gc * (gc + 1) / 2 + tid] = (c == a) ? tc : (tc == 0.0 ? 0.0 : -tc * s);
     }
-    double s = s0 + s1;
-#pragma unroll
-    for (int o = 1; o < kTPR; o <<= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (h == 0 && a <= c) sT[c * (c + 1) / 2 + a] = (a == c) ? tc : (tc == 0.0 ? 0.0 : -tc * s);
+  }
+  __syncthreads();
+  for (int b = 1; b < K / BS; b++) {
+    const int bw = b * BS;
+    for (int e = tid; e < bw * BS; e += kThreads) {
+      const int r = e % bw, j = e / bw;
+      double s = 0.0;
+      for (int d = 0; d <= j; d++)
+        s = fma(sG[(bw + d) * (bw + d - 1) / 2 + r], sT[(bw + j) * (bw + j + 1) / 2 + bw + d], s);
+      sX[r + j * bw] = s;
+    }
+    __syncthreads();
+    for (int e = tid; e < (bw / 2) * BS; e += kThreads) {
+      const int r0 = e % (bw / 2), j = e / (bw / 2), r1 = bw - 1 - r0;
+      double s0 = 0.0, s1 = 0.0;
+      for (int d = r0; d < bw; d++) s0 = fma(sT[d * (d + 1) / 2 + r0], sX[d + j * bw], s0);
+      for (int d = r1; d < bw; d++) s1 = fma(sT[d * (d + 1) / 2 + r1], sX[d + j * bw], s1);
+      const int cj = bw + j;
+      sT[cj * (cj + 1) / 2 + r0] = -s0;
+      sT[cj * (cj + 1) / 2 + r1] = -s1;
+    }
     __syncthreads();
   }
 }
@@ -104,6 +127,9 @@ inline __device__ bool task_ozprep(const double* V, const double* tau, double* G
   double* sG = reinterpret_cast<double*>(sm);
   double* sT = sG + kK * (kK - 1) / 2;
   int* sE = reinterpret_cast<int*>(sT + kK * (kK + 1) / 2);
+  double* sX = reinterpret_cast<double*>(sE + kK);
+  static_assert((kK * (kK - 1) / 2 + kK * (kK + 1) / 2) * 8 + kK * 4 + (kK - 16) * 16 * 8 <= kSmemBytes,
+                "T recurrence scratch");
   constexpr int kPacked = kK * (kK - 1) / 2;
 #pragma unroll 4
   for (int idx = threadIdx.x; idx < kPacked; idx += kThreads) {
@@ -114,7 +140,7 @@ inline __device__ bool task_ozprep(const double* V, const double* tau, double* G
     sG[idx] = __ldcg(G + (idx - c * (c - 1) / 2) + (size_t)c * kK);
   }
   __syncthreads();
-  t_recurrence(sG, sT, tau);
+  t_recurrence(sG, sT, sX, tau);
   // 4. T^T or T
   slice_left(PackedTAcc{sT, t_transposed}, slices + kOzTT * ob, exps + kOzTT * kK, sE);
   return true;
