@@ -100,6 +100,14 @@ struct DagParams {
 
 constexpr int kNever = 0x3fffffff;
 
+// Release / acquire fence at GPU scope.  A task's results reach its
+// dependents by message passing: every thread fences its writes, the CTA
+// synchronises, thread 0 decrements the dependents' counters; the CTA that
+// takes a dependent fences after observing its counter reach zero.  That
+// needs acquire-release ordering only, not the sequentially consistent fence
+// of __threadfence().
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
 // --- domains -------------------------------------------------------------------
 __host__ __device__ __forceinline__ int dom_size(const DagParams& p) { return p.tree > 0 ? p.tree : p.MT; }
 __host__ __device__ __forceinline__ int dom_of(const DagParams& p, int i, int k) { return (k - i) / dom_size(p); }
@@ -265,6 +273,30 @@ __device__ __forceinline__ void release(const DagParams& p, int id, int* keep = 
   }
 }
 
+// release() for up to 4 dependents at once: the counter decrements go out
+// back to back, so their round trips to L2 overlap, then the ones that became
+// ready are queued or kept (the first low-priority one, as release() keeps).
+// True when one of them went to the high-priority queue.
+__device__ __forceinline__ bool release_n(const DagParams& p, const int (&ids)[4], int n, int* keep) {
+  bool hi = false;
+  int old[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++)
+    if (q < n) old[q] = atomicSub(p.cnt + ids[q], 1);
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    if (q < n && old[q] == 1) {
+      const bool h = is_high_priority(p, ids[q]);
+      hi = hi || h;
+      if (keep && *keep < 0 && !h)
+        *keep = ids[q];
+      else
+        push_ready(p, ids[q]);
+    }
+  }
+  return hi;
+}
+
 // Wait (bounded) until slot of queue q has been written; returns the id or -1.
 __device__ int wait_slot(const DagParams& p, int* q, unsigned slot) {
   const uint64_t t0 = global_ns();
@@ -301,7 +333,7 @@ __device__ int pop_task(const DagParams& p) {
     int id = try_claim(p, p.qhi, kHiHead, kHiTail);
     if (id == -2) id = try_claim(p, p.qlo, kLoHead, kLoTail);
     if (id >= 0) {
-      __threadfence();   // acquire: the producers' tile writes are visible
+      fence_acq_rel_gpu();   // acquire: the producers' tile writes are visible
       return id;
     }
     if (id == -1) return -1;
@@ -383,17 +415,20 @@ __global__ void dag_seed_kernel(DagParams p) {
 
 // --- releases after a task ---------------------------------------------------------
 // Step i has finished tile (k, j): its next consumer is step i + 1's update
-// (or, in the factorization, its panel task when j = i + 1).
-__device__ __forceinline__ void release_mem(const DagParams& p, int i, int j, int k, int c, int* keep) {
-  if (i + 1 >= p.steps) return;
-  if (p.mode == kModeFactor && j == i + 1)
-    release(p, panel_id(p, i + 1, k, 0));
-  else
-    release(p, update_id(p, i + 1, j, k, c), keep);
+// (or, in the factorization, its panel task when j = i + 1); -1 at the last step.
+__device__ __forceinline__ int mem_consumer(const DagParams& p, int i, int j, int k, int c) {
+  if (i + 1 >= p.steps) return -1;
+  if (p.mode == kModeFactor && j == i + 1) return panel_id(p, i + 1, k, 0);
+  return update_id(p, i + 1, j, k, c);
+}
+__device__ __forceinline__ void push_id(int (&ids)[4], int& n, int id) {
+  if (id >= 0) ids[n++] = id;
 }
 
 // keep: receives at most one ready low-priority dependent to run next.
-__device__ void release_dependents(const DagParams& p, const TaskDesc& t, int* keep) {
+// Returns true when a high-priority task may have become ready (panel-type
+// tasks always report so).
+__device__ bool release_dependents(const DagParams& p, const TaskDesc& t, int* keep) {
   if (t.type == kGEQRT || t.type == kTSQRT || t.type == kTBUILD || t.type == kOZPREP) {
     const bool feeds_prep = (t.type == kGEQRT || t.type == kTSQRT) && p.prep;
     const bool panel = (t.type == kGEQRT || t.type == kTSQRT);
@@ -406,7 +441,7 @@ __device__ void release_dependents(const DagParams& p, const TaskDesc& t, int* k
         release(p, panel_id(p, t.i, t.k + 1, t.c));
       else if (n_domains(p, t.i) > 1)
         release(p, merge_id(p, t.i, d >= 1 ? d : 1, t.c));
-      if (t.c + 1 < p.nblk) return;   // the tile's V, T, TAU are complete after its last block
+      if (t.c + 1 < p.nblk) return true;   // the tile's V, T, TAU are complete after its last block
     }
     if (feeds_prep) {
       release(p, prep_id(p, t.i, t.k));
@@ -416,46 +451,46 @@ __device__ void release_dependents(const DagParams& p, const TaskDesc& t, int* k
       for (int j = j0; j < j1; j++)
         for (int c = 0; c < p.NC; c++) release(p, update_id(p, t.i, j, t.k, c));
     }
-    return;
+    return true;
   }
   if (t.type == kTTQRT || t.type == kTTPREP) {
     const int d = dom_of(p, t.i, t.k);
     if (t.type == kTTQRT) {
       if (t.c + 1 < p.nblk) release(p, merge_id(p, t.i, d, t.c + 1));
       if (d + 1 < n_domains(p, t.i)) release(p, merge_id(p, t.i, d + 1, t.c));
-      if (t.c + 1 < p.nblk) return;
+      if (t.c + 1 < p.nblk) return true;
       if (p.prep) {
         release(p, ttprep_id(p, t.i, d));
-        return;
+        return true;
       }
     }
     for (int j = t.i + 1; j < p.NT; j++)
       for (int c = 0; c < p.NC; c++) release(p, ttmqr_id(p, t.i, j, d, c));
-    return;
+    return true;
   }
+  int ids[4], n = 0;
   if (t.type == kTTMQR) {
     const int d = dom_of(p, t.i, t.k);
-    if (d + 1 < n_domains(p, t.i)) release(p, ttmqr_id(p, t.i, t.j, d + 1, t.c), keep);
-    release_mem(p, t.i, t.j, t.k, t.c, keep);   // the domain top's tile row is final
-    return;
-  }
-  if (p.mode == kModeBuildQ) {
+    if (d + 1 < n_domains(p, t.i)) push_id(ids, n, ttmqr_id(p, t.i, t.j, d + 1, t.c));
+    push_id(ids, n, mem_consumer(p, t.i, t.j, t.k, t.c));   // the domain top's tile row is final
+  } else if (p.mode == kModeBuildQ) {
     // the chain runs from the bottom tile up to the LARFB; the step before
     // (i - 1) next writes tile (k, j), which this task wrote last
-    if (t.k - 1 >= t.i) release(p, update_id(p, t.i, t.j, t.k - 1, t.c), keep);
-    if (t.i >= 1) release(p, update_id(p, t.i - 1, t.j, t.k, t.c), keep);
-    return;
+    if (t.k - 1 >= t.i) push_id(ids, n, update_id(p, t.i, t.j, t.k - 1, t.c));
+    if (t.i >= 1) push_id(ids, n, update_id(p, t.i - 1, t.j, t.k, t.c));
+  } else {
+    // LARFB / SSRFB: LIN to the next task of this domain's column chain, or
+    // from the domain's last tile to its merge update
+    const int d = dom_of(p, t.i, t.k);
+    if (t.k + 1 < dom_end(p, t.i, d))
+      push_id(ids, n, update_id(p, t.i, t.j, t.k + 1, t.c));
+    else if (n_domains(p, t.i) > 1)
+      push_id(ids, n, ttmqr_id(p, t.i, t.j, d >= 1 ? d : 1, t.c));
+    // MEM: an SSRFB's lower tile is final for this step (a LARFB's tile row
+    // is final, or, at a domain top, finished by the merge update)
+    if (t.type == kSSRFB) push_id(ids, n, mem_consumer(p, t.i, t.j, t.k, t.c));
   }
-  // LARFB / SSRFB: LIN to the next task of this domain's column chain, or from
-  // the domain's last tile to its merge update
-  const int d = dom_of(p, t.i, t.k);
-  if (t.k + 1 < dom_end(p, t.i, d))
-    release(p, update_id(p, t.i, t.j, t.k + 1, t.c), keep);
-  else if (n_domains(p, t.i) > 1)
-    release(p, ttmqr_id(p, t.i, t.j, d >= 1 ? d : 1, t.c), keep);
-  // MEM: an SSRFB's lower tile is final for this step (a LARFB's tile row is
-  // final, or, at a domain top, finished by the merge update)
-  if (t.type == kSSRFB) release_mem(p, t.i, t.j, t.k, t.c, keep);
+  return release_n(p, ids, n, keep);
 }
 
 // --- T build for the Q^T application (diagonal w x w blocks from V, TAU) -------
@@ -497,14 +532,14 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
     oz::tc_fence_after();
   }
   int next = -1;   // thread 0: a continuation kept from the last release
+  bool cont_ok = false;   // thread 0: no error and no high-priority task waiting (read before the releases)
   for (;;) {
     const long long cp = clock64();
     if (threadIdx.x == 0) {
       // A kept continuation runs next unless a high-priority task is waiting:
       // then it goes to the queue like any other ready task.
-      volatile unsigned* ctl = p.ctl;
-      if (next >= 0 && ctl[kErr] == 0u && ctl[kHiHead] >= ctl[kHiTail]) {
-        __threadfence();   // acquire: the other producers' tile writes are visible
+      if (next >= 0 && cont_ok) {
+        fence_acq_rel_gpu();   // acquire: the other producers' tile writes are visible
         s_id = next;
       } else {
         if (next >= 0) push_ready(p, next);
@@ -627,15 +662,19 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
       task_ozapply(c, oz_slices, oz_exps, oz_top, oz_bot);
     }
     (void)tsz;
-    __threadfence();
+    fence_acq_rel_gpu();   // release: this task's writes before its dependents' counters
     __syncthreads();
     if (threadIdx.x == 0) {
       local_cnt[stat_slot(t.type)]++;
       const long long c1 = clock64();
       local_cyc[stat_slot(t.type)] += (unsigned long long)(c1 - c0);
-      release_dependents(p, t, &next);
-      __threadfence();
-      atomicAdd(p.ctl + kDone, 1u);
+      // the control words are read before the releases so that their round
+      // trips overlap the releases' atomics
+      volatile unsigned* ctl = p.ctl;
+      const unsigned err_now = ctl[kErr], hi_head = ctl[kHiHead], hi_tail = ctl[kHiTail];
+      const bool pushed_hi = release_dependents(p, t, &next);
+      cont_ok = err_now == 0u && hi_head >= hi_tail && !pushed_hi;
+      atomicAdd(p.ctl + kDone, 1u);   // termination count only: no ordering needed
       local_cnt[kStatSched]++;
       local_cyc[kStatSched] += (unsigned long long)(clock64() - c1);
     }
