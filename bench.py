@@ -467,6 +467,211 @@ def run_lstsq(H, torch, L, args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# batched uneven QR (hqr_batch_*)
+# ---------------------------------------------------------------------------
+BATCH_METRIC = "batched uneven QR + dormqr TFLOP/s (FP64)"
+
+
+def batch_shapes(count: int, seed: int):
+    """m uniform in {64..2048} step 32, n uniform in {32..m} step 32."""
+    rng = np.random.default_rng(seed)
+    m = [32 * int(x) for x in rng.integers(2, 65, size=count)]
+    n = [32 * int(rng.integers(1, mi // 32 + 1)) for mi in m]
+    return m, n
+
+
+def batch_cpu_sample(m, n, nrhs: int, threads: int, budget_s: float = 15.0):
+    """The oracle's restatement of Hybrid_tile_QR + Hybrid_dormqr (NB 32, IB
+    32) on matrices of the same workload, one matrix per host thread, until
+    about budget_s of wall time.  Returns (flops per second, matrices done)."""
+    import concurrent.futures as cf
+    import oracle as O
+    from hybrid3_gb300 import autotune as AT
+    O.set_threads(1)
+
+    def one(b):
+        mm, nn = m[b], n[b]
+        A = O.to_tiles(O.uniform_matrix(mm, nn, 5000 + b), 32)
+        C = O.to_tiles(O.uniform_matrix(mm, 32, 6000 + b), 32)
+        t0 = time.perf_counter()
+        a, tau = O.tile_qr(A, mm, nn, 32, 32)
+        O.dormqr(a, tau, C, mm, nn, 32, 1)
+        return time.perf_counter() - t0, AT.qr_flops(mm, nn) + AT.ormqr_flops(mm, nn, nrhs)
+
+    flops, done, t_start = 0.0, 0, time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        b = 0
+        while time.perf_counter() - t_start < budget_s and b < len(m):
+            futs = [ex.submit(one, i) for i in range(b, min(b + threads, len(m)))]
+            b += len(futs)
+            for f in futs:
+                flops += f.result()[1]
+                done += 1
+    return flops / (time.perf_counter() - t_start), done
+
+
+def run_batched(H, torch, L, args):
+    """4096 independent FP64 QRs of uneven shapes plus dormqr on nrhs
+    right-hand sides each, every step two persistent launches over all the
+    matrices (hqr_batch_geqrf, hqr_batch_ormqr_t).  NB / IB per size class
+    come from the autotuner (timed on samples of the same shapes, outside the
+    timed region); matrices are zero-padded to NB multiples and the padding's
+    flops are not counted."""
+    from hybrid3_gb300 import autotune as AT
+    count, nrhs = args.batch, args.batch_nrhs
+    m, n = batch_shapes(count, 20151130)
+    t0 = time.perf_counter()
+    if args.batch_nb:
+        nb_ib = tuple(int(x) for x in args.batch_nb.split("/"))
+        table = {c: {"nb": nb_ib[0], "ib": nb_ib[1], "n_range": list(r), "fixed": True}
+                 for c, r in enumerate(AT.CLASSES)}
+    else:
+        table = AT.tune_batch(H, torch, m, n, nrhs)
+    tune_s = time.perf_counter() - t0
+    nb = [AT.choose(table, x)[0] for x in n]
+    ib = [AT.choose(table, x)[1] for x in n]
+    stream = torch.cuda.Stream()
+    s = stream.cuda_stream
+    d = AT.BatchData(H, torch, m, n, nb, ib, nrhs, 20151130, stream)
+    bt = d.batch(H)
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+
+    def step(rec=None):
+        with torch.cuda.stream(stream):
+            d.restore()
+            if rec:
+                rec[0].record(stream)
+            bt.geqrf(d.pa, d.pt, stream=s, wait=False)
+            if rec:
+                rec[1].record(stream)
+            bt.ormqr_t(d.pa, d.pt, d.pc, nrhs, stream=s, wait=False)
+            if rec:
+                rec[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    bt.status(s)
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    recs = [[ev(), ev(), ev()] for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    t_start, t_end = ev(), ev()
+    with torch.cuda.stream(stream):
+        t_start.record(stream)
+    for r in recs:
+        step(r)
+    with torch.cuda.stream(stream):
+        t_end.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    bt.status(s)
+    elapsed = t_start.elapsed_time(t_end) / 1e3 / args.steps
+    fact = float(np.mean([r[0].elapsed_time(r[1]) for r in recs])) / 1e3
+    appl = float(np.mean([r[1].elapsed_time(r[2]) for r in recs])) / 1e3
+    stats = bt.stats(s)
+
+    # accuracy on a sample (check only): R^T R against A^T A, and the
+    # least-squares solution R \ (Q^T c)(1:n) against an FP64 solver's
+    acc = {"gram_rel_max": 0.0, "lstsq_rel_max": 0.0, "sample": 0}
+    f64 = torch.float64
+    for b in range(0, count, max(1, count // 24)):
+        mm, nn, NB = m[b], n[b], nb[b]
+        Mp, Np = d.Mp[b], d.Np[b]
+        cmA = torch.empty(Np * Mp, dtype=f64, device="cuda")
+        cmA0 = torch.empty_like(cmA)
+        Cw = -(-nrhs // NB) * NB
+        cmC = torch.empty(Cw * Mp, dtype=f64, device="cuda")
+        cmC0 = torch.empty_like(cmC)
+        for src, dst, cols, off in ((d.A, cmA, Np, d.a_off), (d.A0, cmA0, Np, d.a_off),
+                                    (d.C, cmC, Cw, d.c_off), (d.C0, cmC0, Cw, d.c_off)):
+            H.check(L.hqr_tiles_to_colmajor_padded(Mp, cols, Mp, NB, src.data_ptr() + 8 * int(off[b]),
+                                                   dst.data_ptr(), None), "from tiles")
+        A0 = cmA0.view(Np, Mp).T[:mm, :nn]
+        R = torch.triu(cmA.view(Np, Mp).T[:nn, :nn])
+        QtC = cmC.view(Cw, Mp).T[:nn, :nrhs]
+        C0 = cmC0.view(Cw, Mp).T[:mm, :nrhs]
+        G = A0.T @ A0
+        acc["gram_rel_max"] = max(acc["gram_rel_max"], float(torch.linalg.norm(R.T @ R - G) / torch.linalg.norm(G)))
+        x = torch.linalg.solve_triangular(R, QtC, upper=True)
+        xr = torch.linalg.lstsq(A0, C0).solution
+        acc["lstsq_rel_max"] = max(acc["lstsq_rel_max"], float(torch.linalg.norm(x - xr) / torch.linalg.norm(xr)))
+        acc["sample"] += 1
+    torch.cuda.synchronize()
+
+    # end to end: pinned host arrays in, R + reflectors, TAU and Q^T C out
+    e2e = None
+    if args.e2e_steps is None or args.e2e_steps > 0:
+        ks = args.e2e_steps if args.e2e_steps is not None else args.steps
+        hA0 = torch.empty(d.A0.numel(), dtype=f64).pin_memory()
+        hC0 = torch.empty(d.C0.numel(), dtype=f64).pin_memory()
+        hA0.copy_(d.A0.cpu())
+        hC0.copy_(d.C0.cpu())
+        hA = torch.empty_like(hA0).pin_memory()
+        hC = torch.empty_like(hC0).pin_memory()
+        hT = torch.empty(d.TAU.numel(), dtype=f64).pin_memory()
+        times = []
+        for it in range(1 + ks):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            with torch.cuda.stream(stream):
+                d.A.copy_(hA0, non_blocking=True)
+                d.C.copy_(hC0, non_blocking=True)
+            bt.geqrf(d.pa, d.pt, stream=s, wait=False)
+            bt.ormqr_t(d.pa, d.pt, d.pc, nrhs, stream=s, wait=False)
+            with torch.cuda.stream(stream):
+                hA.copy_(d.A, non_blocking=True)
+                hT.copy_(d.TAU, non_blocking=True)
+                hC.copy_(d.C, non_blocking=True)
+            bt.status(s)
+            if it > 0:
+                times.append(time.perf_counter() - t0)
+        e2e = {"value": round(d.flops / float(np.mean(times)) / 1e12, 6), "unit": "TFLOP/s",
+               "h2d_bytes_per_step": 8 * (d.A0.numel() + d.C0.numel()),
+               "d2h_bytes_per_step": 8 * (d.A0.numel() + d.TAU.numel() + d.C0.numel()),
+               "steps": ks, "warmup": 1,
+               "api": "hqr_batch_geqrf_async + hqr_batch_ormqr_t_async, pinned host arrays"}
+        del hA0, hC0, hA, hC, hT
+
+    cpu = None
+    if not args.no_cpu:
+        thr = os.cpu_count() or 1
+        v, done = batch_cpu_sample(m, n, nrhs, thr)
+        cpu = {"value": round(v / 1e12, 6), "unit": "TFLOP/s", "cores": thr, "kind": "port",
+               "sample": f"{done} matrices of the workload (oracle Hybrid_tile_QR + Hybrid_dormqr, NB 32, "
+                         f"one matrix per thread)"}
+    peak = L.hqr_fp64_peak_tflops(None)
+    value = d.flops / elapsed / 1e12
+    padded_flops = sum(AT.qr_flops(a, b) + AT.ormqr_flops(a, b, nrhs) for a, b in zip(d.Mp, d.Np))
+    line = {
+        "metric": BATCH_METRIC, "value": round(value, 6), "unit": "TFLOP/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * elapsed, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"{count} independent FP64 matrices, m uniform in {{64..2048}} step 32, "
+                               f"n uniform in {{32..m}} step 32, entries uniform[-1,1) seeded per matrix; "
+                               f"factorization + dormqr on {nrhs} right-hand sides each",
+                   "count": count, "nrhs": nrhs,
+                   "nb_ib_per_class": {str(k): v for k, v in table.items()}, "tune_s": round(tune_s, 2),
+                   "l2": f"inputs ({8 * d.A0.numel() / 2**30:.1f} GiB) exceed the 129 MB L2; no flush",
+                   "parallelism": "one GPU"},
+        "phases_ms": {"geqrf": round(1e3 * fact, 3), "ormqr": round(1e3 * appl, 3)},
+        "accuracy": acc,
+        "roofline": {"kernel": "dag_exec_kernel<fp64, batch>", "bound": "fp64",
+                     "achieved": round(d.flops / elapsed / 1e12, 4), "peak": round(peak, 4),
+                     "unit": "TFLOP/s", "frac": round(value / peak, 4) if peak > 0 else None,
+                     "padded_flops_frac": round(padded_flops / d.flops, 4),
+                     "peak_source": "FP64 FMA issue rate measured in this run (hqr_fp64_peak_tflops)",
+                     "traffic": None},
+        "task_counts": stats["count"],
+        "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": 2 * 3 * args.steps,
+        "clocks": clk,
+    }
+    bt.close()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -491,6 +696,11 @@ def main():
     ap.add_argument("--m", type=int, default=32768, help="rows of A for --lstsq")
     ap.add_argument("--nrhs", type=int, default=16, help="right-hand sides for --lstsq")
     ap.add_argument("--refine", type=int, default=1, help="FP64 refinement steps for --lstsq")
+    ap.add_argument("--batched", action="store_true",
+                    help="batched uneven QR + dormqr workload through hqr_batch_*")
+    ap.add_argument("--batch", type=int, default=4096, help="matrices in the --batched workload")
+    ap.add_argument("--batch-nrhs", type=int, default=4, help="right-hand sides per matrix for --batched")
+    ap.add_argument("--batch-nb", default=None, help="fixed NB/IB for --batched (default: autotuned)")
     ap.add_argument("--tree", type=int, default=0,
                     help="domain tree of this many tiles for the TS reduction (0: the flat tree)")
     args = ap.parse_args()
@@ -522,6 +732,10 @@ def main():
     if args.lstsq:
         if rank == 0:
             run_lstsq(H, torch, L, args)
+        return
+    if args.batched:
+        if rank == 0:
+            run_batched(H, torch, L, args)
         return
     n, NB, IB = args.n, args.nb, args.ib
 

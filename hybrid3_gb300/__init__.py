@@ -109,6 +109,16 @@ SIGNATURES = {
     "hqr_plan_set_tree": (_I, [_vp, _I]),
     "hqr_colmajor_to_tiles_padded": (_I, [_L, _L, _L, _I, _vp, _vp, _vp]),
     "hqr_tiles_to_colmajor_padded": (_I, [_L, _L, _L, _I, _vp, _vp, _vp]),
+    "hqr_batch_create": (_I, [ctypes.POINTER(_vp), _I, ctypes.POINTER(_L), ctypes.POINTER(_L),
+                              ctypes.POINTER(_I), ctypes.POINTER(_I), _I]),
+    "hqr_batch_destroy": (_I, [_vp]),
+    "hqr_batch_geqrf": (_I, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), _vp]),
+    "hqr_batch_geqrf_async": (_I, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), _vp]),
+    "hqr_batch_ormqr_t": (_I, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp), _I, _vp]),
+    "hqr_batch_ormqr_t_async": (_I, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp), _I,
+                                     _vp]),
+    "hqr_batch_status": (_I, [_vp, _vp]),
+    "hqr_batch_stats": (_I, [_vp, ctypes.POINTER(HqrStats), _vp]),
     "hqr_dgemm_tn": (_I, [_L, _I, _vp, _vp, _vp, _vp]),
     "hqr_make_identity": (_I, [_L, _L, _I, _vp, _vp]),
     "hqr_fill_uniform": (_I, [_L, _L, _I, ctypes.c_uint64, _vp, _vp]),
@@ -206,4 +216,53 @@ class Plan:
     def stats(self, stream=None):
         s = HqrStats()
         check(lib().hqr_plan_stats(self.h, ctypes.byref(s), stream), "hqr_plan_stats")
+        return {"count": list(s.count), "cycles": list(s.cycles)}
+
+
+def _ptrs(xs):
+    return (_vp * len(xs))(*[_vp(int(x)) for x in xs])
+
+
+class Batch:
+    """Owns an hqr_batch_t: independent FP64 tile QRs of uneven shapes, each
+    call one persistent launch over every matrix's tasks."""
+
+    def __init__(self, M, N, NB, IB, max_nrhs: int = 1):
+        n = len(M)
+        h = _vp()
+        check(lib().hqr_batch_create(ctypes.byref(h), n, (_L * n)(*M), (_L * n)(*N), (_I * n)(*NB),
+                                     (_I * n)(*IB), max_nrhs), "hqr_batch_create")
+        self.h = h
+        self.count = n
+        self._keep = []
+
+    def close(self):
+        if self.h:
+            lib().hqr_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def geqrf(self, dA, dTAU, stream=None, wait=True):
+        """Factor matrix b in place at device address dA[b] (TAU to dTAU[b])."""
+        a, t = _ptrs(dA), _ptrs(dTAU)
+        fn = lib().hqr_batch_geqrf if wait else lib().hqr_batch_geqrf_async
+        check(fn(self.h, a, t, stream), "hqr_batch_geqrf")
+
+    def ormqr_t(self, dA, dTAU, dC, nrhs: int, stream=None, wait=True):
+        """First nrhs columns of dC[b] <- Q_b^T dC[b] for the last factorization."""
+        a, t, c = _ptrs(dA), _ptrs(dTAU), _ptrs(dC)
+        fn = lib().hqr_batch_ormqr_t if wait else lib().hqr_batch_ormqr_t_async
+        check(fn(self.h, a, t, c, nrhs, stream), "hqr_batch_ormqr_t")
+
+    def status(self, stream=None):
+        check(lib().hqr_batch_status(self.h, stream), "hqr_batch_status")
+
+    def stats(self, stream=None):
+        s = HqrStats()
+        check(lib().hqr_batch_stats(self.h, ctypes.byref(s), stream), "hqr_batch_stats")
         return {"count": list(s.count), "cycles": list(s.cycles)}

@@ -1,0 +1,138 @@
+"""Per-shape choice of the tile order NB and inner block IB for batched FP64
+QR (hqr_batch_*), measured on the device.
+
+The reference fixes NB and IB per run (main.c takes them from the command
+line).  A batch of uneven shapes has no single best pair: small matrices want
+small tiles (more tasks per matrix, less zero padding), large ones large tiles
+(fewer scheduling passes per flop).  The tuner splits the workload's shapes
+into size classes by their column count n, and for each class times every
+candidate (NB, IB) on a sample of the workload's own shapes in that class --
+the matrices zero-padded to NB multiples, as the batch runs them -- and keeps
+the fastest by algorithmic (unpadded) flops per second.
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+# column-count classes (inclusive bounds) and the candidates tried in each
+CLASSES = ((1, 160), (161, 448), (449, 1024), (1025, 1 << 30))
+CANDIDATES = ((32, 32), (64, 32), (64, 16), (128, 32))
+
+
+def class_of(n: int) -> int:
+    for c, (lo, hi) in enumerate(CLASSES):
+        if lo <= n <= hi:
+            return c
+    raise ValueError(n)
+
+
+def padded(x: int, nb: int) -> int:
+    return -(-x // nb) * nb
+
+
+def qr_flops(m: int, n: int) -> float:
+    return 2.0 * m * n * n - 2.0 * n ** 3 / 3.0
+
+
+def ormqr_flops(m: int, n: int, nrhs: int) -> float:
+    """C <- Q^T C for n reflectors of an m-row Q on nrhs columns."""
+    return 2.0 * nrhs * n * (2.0 * m - n)
+
+
+class BatchData:
+    """Device buffers of one batch: matrices (zero-padded tile layout, each
+    ceil(m/NB) x ceil(n/NB) tiles of NB), TAU, right-hand sides (ceil(m/NB)
+    x ceil(nrhs/NB) tiles), with pristine copies of A and C, contiguous."""
+
+    def __init__(self, H, torch, m, n, nb, ib, nrhs: int, seed: int, stream=None):
+        f64 = torch.float64
+        self.m, self.n, self.nb, self.ib, self.nrhs = list(m), list(n), list(nb), list(ib), nrhs
+        cnt = len(self.m)
+        self.Mp = [padded(a, b) for a, b in zip(self.m, self.nb)]
+        self.Np = [padded(a, b) for a, b in zip(self.n, self.nb)]
+        a_len = [mp * np_ for mp, np_ in zip(self.Mp, self.Np)]
+        t_len = [(mp // b) * (np_ // b) * b for mp, np_, b in zip(self.Mp, self.Np, self.nb)]
+        c_len = [mp * padded(nrhs, b) for mp, b in zip(self.Mp, self.nb)]
+        off = lambda L: np.concatenate([[0], np.cumsum(L)]).astype(np.int64)
+        self.a_off, self.t_off, self.c_off = off(a_len), off(t_len), off(c_len)
+        self.A0 = torch.zeros(int(self.a_off[-1]), dtype=f64, device="cuda")
+        self.A = torch.empty_like(self.A0)
+        self.TAU = torch.zeros(int(self.t_off[-1]), dtype=f64, device="cuda")
+        self.C0 = torch.zeros(int(self.c_off[-1]), dtype=f64, device="cuda")
+        self.C = torch.empty_like(self.C0)
+        L = H.lib()
+        s = stream.cuda_stream if stream is not None else None
+        g = torch.Generator(device="cuda")
+        for b in range(cnt):
+            # entries uniform[-1, 1), seeded per matrix; column-major m x n and m x nrhs
+            g.manual_seed(seed + b)
+            x = torch.rand(self.n[b], self.m[b], dtype=f64, device="cuda", generator=g) * 2.0 - 1.0
+            H.check(L.hqr_colmajor_to_tiles_padded(self.m[b], self.n[b], self.m[b], self.nb[b], x.data_ptr(),
+                                                   self.A0.data_ptr() + 8 * int(self.a_off[b]), s), "to tiles")
+            y = torch.rand(nrhs, self.m[b], dtype=f64, device="cuda", generator=g) * 2.0 - 1.0
+            H.check(L.hqr_colmajor_to_tiles_padded(self.m[b], nrhs, self.m[b], self.nb[b], y.data_ptr(),
+                                                   self.C0.data_ptr() + 8 * int(self.c_off[b]), s), "to tiles")
+        torch.cuda.synchronize()
+        base = lambda t, o: [t.data_ptr() + 8 * int(x) for x in o[:-1]]
+        self.pa, self.pt, self.pc = base(self.A, self.a_off), base(self.TAU, self.t_off), base(self.C, self.c_off)
+        self.flops = sum(qr_flops(a, b) + ormqr_flops(a, b, nrhs) for a, b in zip(self.m, self.n))
+
+    def restore(self):
+        self.A.copy_(self.A0, non_blocking=True)
+        self.C.copy_(self.C0, non_blocking=True)
+
+    def batch(self, H):
+        return H.Batch(self.Mp, self.Np, self.nb, self.ib, max_nrhs=self.nrhs)
+
+
+def tune_batch(H, torch, m, n, nrhs: int, candidates=CANDIDATES, sample_flops: float = 1.5e11,
+               max_sample: int = 600, seed: int = 7):
+    """(NB, IB) per size class for a workload of shapes (m[b], n[b]): a dict
+    class index -> {"nb", "ib", "n_range", "tflops": {candidate: measured}}."""
+    rng = np.random.default_rng(seed)
+    m, n = np.asarray(m), np.asarray(n)
+    table = {}
+    stream = torch.cuda.Stream()
+    for c, (lo, hi) in enumerate(CLASSES):
+        idx = np.nonzero((n >= lo) & (n <= hi))[0]
+        if idx.size == 0:
+            continue
+        rng.shuffle(idx)
+        take, acc = [], 0.0
+        for b in idx:
+            take.append(b)
+            acc += qr_flops(int(m[b]), int(n[b]))
+            if acc >= sample_flops or len(take) >= max_sample:
+                break
+        sm, sn = m[take].tolist(), n[take].tolist()
+        res = {}
+        for nb, ib in candidates:
+            d = BatchData(H, torch, sm, sn, [nb] * len(sm), [ib] * len(sm), nrhs, 1000 + c, stream)
+            bt = d.batch(H)
+            try:
+                times = []
+                for rep in range(2):   # the first run uploads the task tables
+                    with torch.cuda.stream(stream):
+                        d.restore()
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    bt.geqrf(d.pa, d.pt, stream=stream.cuda_stream)
+                    bt.ormqr_t(d.pa, d.pt, d.pc, nrhs, stream=stream.cuda_stream)
+                    times.append(time.perf_counter() - t0)
+                res[(nb, ib)] = d.flops / times[-1] / 1e12
+            finally:
+                bt.close()
+                del d
+                torch.cuda.empty_cache()
+        best = max(res, key=res.get)
+        table[c] = {"nb": best[0], "ib": best[1], "n_range": [lo, hi], "sample": len(sm),
+                    "tflops": {f"{k[0]}/{k[1]}": round(v, 4) for k, v in res.items()}}
+    return table
+
+
+def choose(table, n: int, default=(64, 32)):
+    """(NB, IB) for a matrix with n columns from a tune_batch table."""
+    e = table.get(class_of(n))
+    return (e["nb"], e["ib"]) if e else default

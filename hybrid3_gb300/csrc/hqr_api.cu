@@ -5,11 +5,13 @@
 // in tile layout, void return, abort on error -- Hybrid_tile_QR.c:992-999 and
 // friends call MPI_Abort): each call stages its operands in device buffers
 // owned by the library, runs the tile DAG on the GPU and copies results back.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "Hybrid_tile_QR.h"
 #include "hqr_internal.h"
@@ -587,6 +589,175 @@ void Hybrid_remv_Y(mat_stat_t* status, double* RY, int my_rank, int Proc_num) {
 void Hybrid_dgemm(mat_stat_t* status, double* A, double* B, double* C, int my_rank, int Proc_num) {
   std::lock_guard<std::mutex> lk(g_mu);
   report("Hybrid_dgemm", do_simple(status, my_rank, Proc_num, 2, A, B, C));
+}
+
+}  // extern "C"
+
+// --- batches -------------------------------------------------------------------------
+// Task tables of the two launch kinds (factorization, Q^T C): written on the
+// host, uploaded through a pinned buffer when the pointers change, kept on
+// the device for later calls (and graph replays) with the same pointers.
+struct hqr_batch {
+  int count = 0;
+  std::vector<hqr::Geometry> g;
+  std::vector<double*> T;    // per matrix, into dT
+  double* dT = nullptr;
+  hqr::DagWorkspace ws;
+  size_t smem = 0;
+  int max_nrhs = 0;
+  struct Table {
+    std::vector<unsigned char> host;   // the descriptors last uploaded
+    unsigned char* pinned = nullptr;
+    void* dev = nullptr;
+    cudaEvent_t uploaded = nullptr;
+    int n_ids = 0, n_tasks = 0, nrhs = -1;
+    bool valid = false;
+  } tab[2];
+};
+
+namespace {
+void free_batch(hqr_batch* b) {
+  cudaFree(b->dT);
+  hqr::dag_workspace_free(&b->ws);
+  for (auto& t : b->tab) {
+    cudaFreeHost(t.pinned);
+    cudaFree(t.dev);
+    if (t.uploaded) cudaEventDestroy(t.uploaded);
+  }
+  delete b;
+}
+
+// Make the device task table of launch kind `apply` describe these pointers.
+int batch_table(hqr_batch* b, bool apply, double* const* dA, double* const* dTAU, double* const* dC,
+                int nrhs, cudaStream_t s) {
+  hqr_batch::Table& t = b->tab[apply ? 1 : 0];
+  const size_t bytes = (size_t)b->count * hqr::mat_desc_bytes();
+  std::vector<unsigned char> desc(bytes);
+  int n_ids = 0, n_tasks = 0;
+  TRY(hqr::batch_describe(apply, b->count, b->g.data(), dA, b->T.data(), dTAU, dC, nrhs, desc.data(), &n_ids,
+                          &n_tasks));
+  if (t.valid && t.nrhs == nrhs && desc == t.host) return HQR_OK;   // the device copy is current
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  TRY(cuda_rc(cudaStreamIsCapturing(s, &cs)));
+  if (cs != cudaStreamCaptureStatusNone) return HQR_ERR_UNSUPPORTED;   // upload outside a capture first
+  TRY(cuda_rc(cudaEventSynchronize(t.uploaded)));   // the pinned buffer's previous copy is done
+  memcpy(t.pinned, desc.data(), bytes);
+  TRY(cuda_rc(cudaMemcpyAsync(t.dev, t.pinned, bytes, cudaMemcpyHostToDevice, s)));
+  TRY(cuda_rc(cudaEventRecord(t.uploaded, s)));
+  t.host.swap(desc);
+  t.n_ids = n_ids;
+  t.n_tasks = n_tasks;
+  t.nrhs = nrhs;
+  t.valid = true;
+  return HQR_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int hqr_batch_create(hqr_batch_t** batch, int count, const long* M, const long* N, const int* NB,
+                     const int* IB, int max_nrhs) {
+  if (!batch) return HQR_ERR_INVALID;
+  *batch = nullptr;
+  if (count <= 0 || !M || !N || !NB || !IB || max_nrhs < 0) return HQR_ERR_INVALID;
+  hqr_batch* b = new hqr_batch();
+  b->count = count;
+  b->max_nrhs = max_nrhs;
+  b->g.resize(count);
+  size_t t_elems = 0;
+  long long ids = 0, ids_apply = 0;
+  for (int i = 0; i < count; i++) {
+    const int rc = hqr::make_geometry(M[i], N[i], NB[i], IB[i], &b->g[i]);
+    if (rc != HQR_OK) {
+      free_batch(b);
+      return rc;
+    }
+    t_elems += (size_t)M[i] * N[i];
+    b->smem = std::max(b->smem, b->g[i].smem_bytes);
+    ids += hqr::batch_ids(false, b->g[i], 1);
+    if (max_nrhs > 0) ids_apply += hqr::batch_ids(true, b->g[i], max_nrhs);
+  }
+  if (std::max(ids, ids_apply) > 0x3fffffffLL) {
+    free_batch(b);
+    return HQR_ERR_UNSUPPORTED;
+  }
+  const size_t bytes = (size_t)count * hqr::mat_desc_bytes();
+  int rc = HQR_OK;
+  if (cudaMalloc(&b->dT, t_elems * sizeof(double)) != cudaSuccess) rc = HQR_ERR_NOMEM;
+  for (auto& t : b->tab) {
+    if (rc != HQR_OK) break;
+    if (cudaMallocHost(&t.pinned, bytes) != cudaSuccess || cudaMalloc(&t.dev, bytes) != cudaSuccess)
+      rc = HQR_ERR_NOMEM;
+    else if (cudaEventCreateWithFlags(&t.uploaded, cudaEventDisableTiming) != cudaSuccess)
+      rc = HQR_ERR_CUDA;
+  }
+  if (rc == HQR_OK) rc = hqr::dag_workspace_reserve(&b->ws, (size_t)std::max(ids, ids_apply));
+  if (rc != HQR_OK) {
+    free_batch(b);
+    return rc;
+  }
+  b->T.resize(count);
+  size_t off = 0;
+  for (int i = 0; i < count; i++) {
+    b->T[i] = b->dT + off;
+    off += (size_t)M[i] * N[i];
+  }
+  *batch = b;
+  return HQR_OK;
+}
+
+int hqr_batch_destroy(hqr_batch_t* batch) {
+  if (!batch) return HQR_ERR_INVALID;
+  free_batch(batch);
+  return HQR_OK;
+}
+
+int hqr_batch_geqrf_async(hqr_batch_t* b, double* const* dA, double* const* dTAU, void* stream) {
+  if (!b || !dA || !dTAU) return HQR_ERR_INVALID;
+  for (int i = 0; i < b->count; i++)
+    if (!dA[i] || !dTAU[i]) return HQR_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  TRY(batch_table(b, false, dA, dTAU, dA, 0, s));
+  const hqr_batch::Table& t = b->tab[0];
+  return hqr::launch_batch(false, b->count, t.dev, t.n_ids, t.n_tasks, b->smem, &b->ws, g_timeout_ns, s);
+}
+
+int hqr_batch_geqrf(hqr_batch_t* b, double* const* dA, double* const* dTAU, void* stream) {
+  TRY(hqr_batch_geqrf_async(b, dA, dTAU, stream));
+  return hqr_batch_status(b, stream);
+}
+
+int hqr_batch_ormqr_t_async(hqr_batch_t* b, double* const* dA, double* const* dTAU, double* const* dC,
+                            int nrhs, void* stream) {
+  if (!b || !dA || !dTAU || !dC || nrhs <= 0 || nrhs > b->max_nrhs) return HQR_ERR_INVALID;
+  for (int i = 0; i < b->count; i++)
+    if (!dA[i] || !dTAU[i] || !dC[i]) return HQR_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  TRY(batch_table(b, true, dA, dTAU, dC, nrhs, s));
+  const hqr_batch::Table& t = b->tab[1];
+  return hqr::launch_batch(true, b->count, t.dev, t.n_ids, t.n_tasks, b->smem, &b->ws, g_timeout_ns, s);
+}
+
+int hqr_batch_ormqr_t(hqr_batch_t* b, double* const* dA, double* const* dTAU, double* const* dC, int nrhs,
+                      void* stream) {
+  TRY(hqr_batch_ormqr_t_async(b, dA, dTAU, dC, nrhs, stream));
+  return hqr_batch_status(b, stream);
+}
+
+int hqr_batch_status(hqr_batch_t* b, void* stream) {
+  if (!b) return HQR_ERR_INVALID;
+  return hqr::dag_status(&b->ws, (cudaStream_t)stream);
+}
+
+int hqr_batch_stats(hqr_batch_t* b, hqr_stats_t* out, void* stream) {
+  if (!b || !out) return HQR_ERR_INVALID;
+  unsigned long long v[14];
+  TRY(hqr::dag_stats(&b->ws, v, (cudaStream_t)stream));
+  for (int t = 0; t < 7; t++) {
+    out->count[t] = v[2 * t];
+    out->cycles[t] = v[2 * t + 1];
+  }
+  return HQR_OK;
 }
 
 }  // extern "C"

@@ -272,6 +272,128 @@ int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double
   return run_dag(p, ws, g, stream);
 }
 
+// --- batches of independent matrices (FP64) ---------------------------------------
+size_t mat_desc_bytes() { return sizeof(MatDesc); }
+
+// The per-matrix fields of a batch launch (factorization, or C <- Q^T C with
+// the T factors the factorization left), plus that matrix's id / task counts.
+// C <- Q^T C covers the first nrhs columns of C: ceil(nrhs / NB) tile
+// columns; fewer than NB right-hand sides take the narrowest column blocks
+// (a multiple of 8 dividing NB, at most the factorization's) that hold them.
+static DagParams batch_matrix_params(bool apply, const Geometry& g, int nrhs) {
+  DagParams p{};
+  p.mode = apply ? kModeApplyQt : kModeFactor;
+  p.MT = g.MT;
+  p.NT = g.NT;
+  p.NC = g.NC;
+  p.steps = g.steps;
+  p.CT = g.NT;
+  p.nblk = g.NB / g.w;
+  p.sh = shape_of(g);
+  if (apply) {
+    p.skip_panels = 1;
+    p.nblk = 1;
+    p.CT = (nrhs + g.NB - 1) / g.NB;
+    if (nrhs < g.NB) {
+      int cb = (nrhs + 7) / 8 * 8;
+      while (cb < g.CB && g.NB % cb != 0) cb += 8;
+      if (cb > g.CB) cb = g.CB;
+      p.sh.CB = cb;
+      p.NC = (nrhs + cb - 1) / cb;
+    }
+  }
+  p.J = p.CT;
+  p.sp = SmemPlan::make(p.sh);
+  return p;
+}
+static long long batch_matrix_tasks(bool apply, const DagParams& p) {
+  long long n = 0;
+  for (int i = 0; i < p.steps; i++) {
+    if (apply)
+      n += (long long)p.NC * p.CT * (p.MT - i);
+    else
+      n += (long long)(p.MT - i) * p.nblk + (long long)p.NC * (p.NT - 1 - i) * (p.MT - i);
+  }
+  return n;
+}
+
+long long batch_ids(bool apply, const Geometry& g, int nrhs) {
+  return id_end(batch_matrix_params(apply, g, nrhs));
+}
+
+int batch_describe(bool apply, int count, const Geometry* gs, double* const* A, double* const* T,
+                   double* const* TAU, double* const* C, int nrhs, void* desc, int* n_ids, int* n_tasks) {
+  MatDesc* d = static_cast<MatDesc*>(desc);
+  long long ids = 0, tasks = 0;
+  for (int b = 0; b < count; b++) {
+    const DagParams p = batch_matrix_params(apply, gs[b], nrhs);
+    MatDesc m{};
+    m.MT = p.MT;
+    m.NT = p.NT;
+    m.CT = p.CT;
+    m.NC = p.NC;
+    m.steps = p.steps;
+    m.J = p.J;
+    m.nblk = p.nblk;
+    m.sh = p.sh;
+    m.sp = p.sp;
+    m.A = A[b];
+    m.T = T[b];
+    m.TAU = TAU[b];
+    m.C = apply ? C[b] : A[b];
+    m.id_base = (int)ids;
+    ids += id_end(p);
+    tasks += batch_matrix_tasks(apply, p);
+    if (ids > 0x3fffffffLL) return HQR_ERR_UNSUPPORTED;
+    m.id_end = (int)ids;
+    d[b] = m;
+  }
+  *n_ids = (int)ids;
+  *n_tasks = (int)tasks;
+  return HQR_OK;
+}
+
+int launch_batch(bool apply, int count, const void* d_desc, int n_ids, int n_tasks, size_t smem,
+                 DagWorkspace* ws, long long timeout_ns, cudaStream_t stream) {
+  if (count <= 0 || n_tasks <= 0) return HQR_ERR_INVALID;
+  DagParams p{};
+  p.mode = apply ? kModeApplyQt : kModeFactor;
+  p.skip_panels = apply ? 1 : 0;
+  p.n_mats = count;
+  p.mats = static_cast<const MatDesc*>(d_desc);
+  p.n_ids = n_ids;
+  p.n_tasks = n_tasks;
+  p.timeout_ns = timeout_ns;
+  int rc = dag_workspace_reserve(ws, (size_t)n_ids);
+  if (rc != HQR_OK) return rc;
+  p.cnt = ws->cnt;
+  p.qhi = ws->qhi;
+  p.qlo = ws->qlo;
+  p.ctl = ws->ctl;
+  p.stats = ws->stats;
+  cudaError_t e = cudaMemsetAsync(ws->ctl, 0, kErr * sizeof(unsigned), stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ws->stats, 0, 2 * kNumStats * sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return record_cuda_error(e, "DAG workspace reset");
+  static std::mutex mu;
+  static size_t attr_bytes = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (smem > attr_bytes) {
+      e = cudaFuncSetAttribute(dag_exec_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem);
+      if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(dag_exec_kernel batch)");
+      attr_bytes = smem;
+    }
+  }
+  dag_init_batch_kernel<<<count, 256, 0, stream>>>(p);
+  dag_seed_batch_kernel<<<count, 256, 0, stream>>>(p);
+  const int grid = std::min(dag_sm_count(), std::max(1, n_tasks));
+  dag_exec_kernel<false, true><<<grid, kThreads, smem, stream>>>(p);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return record_cuda_error(e, "dag_exec_kernel batch launch");
+  return HQR_OK;
+}
+
 bool oz_supported(const Geometry& g) { return g.NB == oz::kK; }
 
 // The split path rebuilds every panel tile's full T from V and TAU, which do

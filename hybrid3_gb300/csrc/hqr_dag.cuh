@@ -63,6 +63,16 @@ constexpr int kStatSched = kNumTypes, kNumStats = kNumTypes + 1;
 // counters are touched once per task).
 enum Ctl : int { kHiHead = 0, kHiTail = 1, kLoHead = 2, kLoTail = 3, kDone = 4, kErr = 5, kCtlWords = 8 };
 
+// One matrix of a batch (batched DAG): its geometry, task-id range and arrays.
+struct MatDesc {
+  int MT, NT, CT, NC, steps, J, nblk;
+  TileShape sh;
+  SmemPlan sp;
+  double *A, *T, *TAU, *C;
+  int id_base;   // first global task id of this matrix
+  int id_end;    // one past its last (the next matrix's id_base)
+};
+
 struct DagParams {
   int mode;
   int MT, NT, CT, NC, steps, J;   // J = tile columns spanned by update ids
@@ -77,6 +87,12 @@ struct DagParams {
   double* TAU2;                    // TAU of each merge, compact: (i * dmax + d) * NB
   uint8_t* slices2;                // split: the merges' prepared operands, compact
   int* sexp2;
+  // Batch (n_mats > 0): the task ids of matrix m are [mats[m].id_base, + its
+  // count); counters and queues hold global ids, and every task runs with its
+  // matrix's fields copied over these (id_base included).
+  int id_base;
+  int n_mats;
+  const MatDesc* mats;
   TileShape sh;
   SmemPlan sp;
   double* A;        // factored matrix: R above, V below the diagonal
@@ -249,15 +265,18 @@ __device__ __forceinline__ bool is_high_priority(const DagParams& p, int id) {
 }
 
 // --- queues -------------------------------------------------------------------
-__device__ __forceinline__ void push_ready(const DagParams& p, int id) {
-  const bool hi = is_high_priority(p, id);
+// Queue global task id gid (queues hold global ids).
+__device__ __forceinline__ void push_queue(const DagParams& p, int gid, bool hi) {
   int* q = hi ? p.qhi : p.qlo;
   const unsigned slot = atomicAdd(p.ctl + (hi ? kHiTail : kLoTail), 1u);
   if ((int)slot < p.n_ids) {
-    atomicExch(q + slot, id);
+    atomicExch(q + slot, gid);
   } else {
     atomicOr((int*)(p.ctl + kErr), kErrBadTask);
   }
+}
+__device__ __forceinline__ void push_ready(const DagParams& p, int id) {
+  push_queue(p, p.id_base + id, is_high_priority(p, id));
 }
 
 // One input of task `id` is available (the releasing task's writes were fenced
@@ -265,9 +284,9 @@ __device__ __forceinline__ void push_ready(const DagParams& p, int id) {
 // still empty and the task is not on the high-priority queue, handed back to
 // the caller to run next (a continuation: no queue round trip).
 __device__ __forceinline__ void release(const DagParams& p, int id, int* keep = nullptr) {
-  if (atomicSub(p.cnt + id, 1) == 1) {
+  if (atomicSub(p.cnt + p.id_base + id, 1) == 1) {
     if (keep && *keep < 0 && !is_high_priority(p, id))
-      *keep = id;
+      *keep = p.id_base + id;
     else
       push_ready(p, id);
   }
@@ -282,14 +301,14 @@ __device__ __forceinline__ bool release_n(const DagParams& p, const int (&ids)[4
   int old[4];
 #pragma unroll
   for (int q = 0; q < 4; q++)
-    if (q < n) old[q] = atomicSub(p.cnt + ids[q], 1);
+    if (q < n) old[q] = atomicSub(p.cnt + p.id_base + ids[q], 1);
 #pragma unroll
   for (int q = 0; q < 4; q++) {
     if (q < n && old[q] == 1) {
       const bool h = is_high_priority(p, ids[q]);
       hi = hi || h;
       if (keep && *keep < 0 && !h)
-        *keep = ids[q];
+        *keep = p.id_base + ids[q];
       else
         push_ready(p, ids[q]);
     }
@@ -347,11 +366,7 @@ __device__ int pop_task(const DagParams& p) {
 }
 
 // --- dependency initialisation (one thread per id) --------------------------------
-__global__ void dag_init_kernel(DagParams p) {
-  const int id = blockIdx.x * blockDim.x + threadIdx.x;
-  if (id >= p.n_ids) return;
-  p.qhi[id] = -1;
-  p.qlo[id] = -1;
+__device__ int init_deps(const DagParams& p, int id) {
   int deps = kNever;
   const int P0 = panel_end(p);
   const int U0 = update_base(p);
@@ -404,13 +419,115 @@ __global__ void dag_init_kernel(DagParams p) {
     if (i < p.steps && d >= 1 && d < n_domains(p, i) && update_valid(p, i, j))
       deps = (p.skip_panels ? 0 : 1) + 2;
   }
-  p.cnt[id] = deps;
+  return deps;
+}
+
+__global__ void dag_init_kernel(DagParams p) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  if (id >= p.n_ids) return;
+  p.qhi[id] = -1;
+  p.qlo[id] = -1;
+  p.cnt[id] = init_deps(p, id);
 }
 
 __global__ void dag_seed_kernel(DagParams p) {
   const int id = blockIdx.x * blockDim.x + threadIdx.x;
   if (id >= p.n_ids) return;
   if (p.cnt[id] == 0) push_ready(p, id);
+}
+
+// --- batches ---------------------------------------------------------------------
+__device__ __forceinline__ void apply_mat(DagParams& q, const MatDesc& d) {
+  q.MT = d.MT;
+  q.NT = d.NT;
+  q.CT = d.CT;
+  q.NC = d.NC;
+  q.steps = d.steps;
+  q.J = d.J;
+  q.nblk = d.nblk;
+  q.sh = d.sh;
+  q.sp = d.sp;
+  q.A = d.A;
+  q.T = d.T;
+  q.TAU = d.TAU;
+  q.C = d.C;
+  q.id_base = d.id_base;
+}
+// Warp 0: the matrix that global task id g belongs to (ids are laid out by
+// matrix), a 32-way search: three dependent loads for 4096 matrices.
+__device__ __forceinline__ int find_mat_warp(const DagParams& p, int g) {
+  const int lane = threadIdx.x & 31;
+  int lo = 0, hi = p.n_mats;   // mats[lo].id_base <= g < mats[hi].id_base
+  while (hi - lo > 1) {
+    const int step = (hi - lo + 31) >> 5;
+    const int idx = lo + lane * step;
+    const bool le = idx < hi && __ldg(&p.mats[idx].id_base) <= g;
+    const unsigned b = __ballot_sync(0xffffffffu, le);
+    const int nlo = lo + (31 - __clz(b)) * step;
+    hi = min(hi, nlo + step);
+    lo = nlo;
+  }
+  return lo;
+}
+// Shared state of a batched executor CTA: the current task's matrix fields.
+template <bool BATCH> struct BatchLocal {
+  DagParams lp;
+  int end;   // one past lp's task ids (0: none loaded yet)
+};
+template <> struct BatchLocal<false> {};
+__device__ __forceinline__ const DagParams& local_params(const DagParams& p, BatchLocal<false>&) { return p; }
+__device__ __forceinline__ const DagParams& local_params(const DagParams&, BatchLocal<true>& b) { return b.lp; }
+__device__ __forceinline__ void init_local(BatchLocal<false>&) {}
+__device__ __forceinline__ void init_local(BatchLocal<true>& b) {
+  if (threadIdx.x == 0) {
+    b.lp.id_base = 0;
+    b.end = 0;
+  }
+}
+// All threads: make b.lp the fields of the matrix that owns gid.
+__device__ __forceinline__ void load_local(const DagParams& p, BatchLocal<false>&, int) {}
+__device__ __forceinline__ void load_local(const DagParams& p, BatchLocal<true>& b, int gid) {
+  if (threadIdx.x < 32) {
+    const bool have = gid >= b.lp.id_base && gid < b.end;
+    __syncwarp();
+    if (!have) {
+      const int m = find_mat_warp(p, gid);
+      if (threadIdx.x == 0) {
+        b.lp = p;
+        apply_mat(b.lp, p.mats[m]);
+        b.end = p.mats[m].id_end;
+      }
+    }
+  }
+  __syncthreads();
+}
+// One block per matrix: its ids' counters and queue slots, then (second
+// kernel) the ready ones pushed.
+__global__ void dag_init_batch_kernel(DagParams p) {
+  __shared__ DagParams q;
+  if (threadIdx.x == 0) {
+    q = p;
+    apply_mat(q, p.mats[blockIdx.x]);
+  }
+  __syncthreads();
+  const int end = (blockIdx.x + 1 < p.n_mats) ? p.mats[blockIdx.x + 1].id_base : p.n_ids;
+  for (int lid = threadIdx.x; q.id_base + lid < end; lid += blockDim.x) {
+    const int g = q.id_base + lid;
+    p.qhi[g] = -1;
+    p.qlo[g] = -1;
+    p.cnt[g] = init_deps(q, lid);
+  }
+}
+__global__ void dag_seed_batch_kernel(DagParams p) {
+  __shared__ DagParams q;
+  if (threadIdx.x == 0) {
+    q = p;
+    apply_mat(q, p.mats[blockIdx.x]);
+  }
+  __syncthreads();
+  const int end = (blockIdx.x + 1 < p.n_mats) ? p.mats[blockIdx.x + 1].id_base : p.n_ids;
+  for (int lid = threadIdx.x; q.id_base + lid < end; lid += blockDim.x)
+    if (p.cnt[q.id_base + lid] == 0) push_ready(q, lid);
 }
 
 // --- releases after a task ---------------------------------------------------------
@@ -515,13 +632,14 @@ __device__ void task_tbuild(const double* V, const double* tau_g, double* T, boo
 }
 
 // --- the persistent executor ---------------------------------------------------------
-template <bool OZ>
+// BATCH: the tasks of many matrices (FP64 tile kernels only); each task runs
+// with its matrix's fields (s_b.lp).
+template <bool OZ, bool BATCH = false>
 __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
   extern __shared__ __align__(1024) double smem[];
   __shared__ int s_id;
   __shared__ uint32_t s_tmem;
-  const int NB = p.sh.NB;
-  const size_t tsz = (size_t)NB * NB;
+  __shared__ BatchLocal<BATCH> s_b;
   unsigned long long local_cnt[kNumStats] = {0, 0, 0, 0, 0, 0, 0};
   unsigned long long local_cyc[kNumStats] = {0, 0, 0, 0, 0, 0, 0};
   if (OZ) {
@@ -531,6 +649,7 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
     __syncthreads();
     oz::tc_fence_after();
   }
+  init_local(s_b);
   int next = -1;   // thread 0: a continuation kept from the last release
   bool cont_ok = false;   // thread 0: no error and no high-priority task waiting (read before the releases)
   for (;;) {
@@ -542,16 +661,21 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
         fence_acq_rel_gpu();   // acquire: the other producers' tile writes are visible
         s_id = next;
       } else {
-        if (next >= 0) push_ready(p, next);
+        if (next >= 0) push_queue(p, next, false);   // a kept task is never high-priority
         s_id = pop_task(p);
       }
       next = -1;
     }
     __syncthreads();
-    const int id = s_id;
+    const int gid = s_id;
     __syncthreads();
-    if (id < 0) break;
-    const TaskDesc t = decode(p, id);
+    if (gid < 0) break;
+    load_local(p, s_b, gid);
+    const DagParams& q = local_params(p, s_b);
+    const int id = gid - q.id_base;
+    const int NB = q.sh.NB;
+    const size_t tsz = (size_t)NB * NB;
+    const TaskDesc t = decode(q, id);
     const long long c0 = clock64();
     if (threadIdx.x == 0) local_cyc[kStatSched] += (unsigned long long)(c0 - cp);
     // Each heavy task body has one call site (the split engine, the panel
@@ -569,99 +693,98 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
     bool ts_upper = false;
     switch (t.type) {
       case kGEQRT: {   // the diagonal tile or a domain's top tile
-        const size_t o = tile_off(t.k, t.i, p.MT, NB);
-        task_geqrt_blk(p.A + o, p.T + o, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.sh, smem, p.sp, t.c);
+        const size_t o = tile_off(t.k, t.i, q.MT, NB);
+        task_geqrt_blk(q.A + o, q.T + o, q.TAU + tau_off(t.k, t.i, q.MT, NB), q.sh, smem, q.sp, t.c);
         break;
       }
       case kTSQRT: {   // R of the domain's top tile over tile (k, i)
-        const int top = dom_top(p, t.i, dom_of(p, t.i, t.k));
-        const size_t o2 = tile_off(t.k, t.i, p.MT, NB);
-        ts_a1 = p.A + tile_off(top, t.i, p.MT, NB);
-        ts_a2 = p.A + o2;
-        ts_t = p.T + o2;
-        ts_tau = p.TAU + tau_off(t.k, t.i, p.MT, NB);
+        const int top = dom_top(q, t.i, dom_of(q, t.i, t.k));
+        const size_t o2 = tile_off(t.k, t.i, q.MT, NB);
+        ts_a1 = q.A + tile_off(top, t.i, q.MT, NB);
+        ts_a2 = q.A + o2;
+        ts_t = q.T + o2;
+        ts_tau = q.TAU + tau_off(t.k, t.i, q.MT, NB);
         break;
       }
       case kTTQRT: {   // merge of domain top t.k's R into R(i, i): FP64 on the panel path
-        const size_t slot = merge_slot(p, t.i, dom_of(p, t.i, t.k));
-        ts_a1 = p.A + tile_off(t.i, t.i, p.MT, NB);
-        ts_a2 = p.A + tile_off(t.k, t.i, p.MT, NB);
-        ts_t = p.T2 + slot * tsz;
-        ts_tau = p.TAU2 + slot * NB;
+        const size_t slot = merge_slot(q, t.i, dom_of(q, t.i, t.k));
+        ts_a1 = q.A + tile_off(t.i, t.i, q.MT, NB);
+        ts_a2 = q.A + tile_off(t.k, t.i, q.MT, NB);
+        ts_t = q.T2 + slot * tsz;
+        ts_tau = q.TAU2 + slot * NB;
         ts_upper = true;
         break;
       }
       case kTBUILD: {
-        const size_t o = tile_off(t.k, t.i, p.MT, NB);
-        task_tbuild(p.A + o, p.TAU + tau_off(t.k, t.i, p.MT, NB), p.T + o, t.k == t.i, p.sh, smem, p.sp);
+        const size_t o = tile_off(t.k, t.i, q.MT, NB);
+        task_tbuild(q.A + o, q.TAU + tau_off(t.k, t.i, q.MT, NB), q.T + o, t.k == t.i, q.sh, smem, q.sp);
         break;
       }
       case kOZPREP: {
-        const size_t o = tile_off(t.k, t.i, p.MT, NB);
-        const size_t slot = panel_slot(p.MT, t.i, t.k);
-        prep_v = p.A + o;
-        prep_tau = p.TAU + tau_off(t.k, t.i, p.MT, NB);
-        prep_g = p.T + o;
-        prep_kind = is_top(p, t.i, t.k) ? kVUnitLower : kVDense;
-        prep_slices = p.slices + slot * oz::panel_slice_bytes();
-        prep_exps = p.sexp + slot * 3 * NB;
+        const size_t o = tile_off(t.k, t.i, q.MT, NB);
+        const size_t slot = panel_slot(q.MT, t.i, t.k);
+        prep_v = q.A + o;
+        prep_tau = q.TAU + tau_off(t.k, t.i, q.MT, NB);
+        prep_g = q.T + o;
+        prep_kind = is_top(q, t.i, t.k) ? kVUnitLower : kVDense;
+        prep_slices = q.slices + slot * oz::panel_slice_bytes();
+        prep_exps = q.sexp + slot * 3 * NB;
         break;
       }
       case kTTPREP: {
-        const size_t slot = merge_slot(p, t.i, dom_of(p, t.i, t.k));
-        prep_v = p.A + tile_off(t.k, t.i, p.MT, NB);
-        prep_tau = p.TAU2 + slot * NB;
-        prep_g = p.T2 + slot * tsz;
+        const size_t slot = merge_slot(q, t.i, dom_of(q, t.i, t.k));
+        prep_v = q.A + tile_off(t.k, t.i, q.MT, NB);
+        prep_tau = q.TAU2 + slot * NB;
+        prep_g = q.T2 + slot * tsz;
         prep_kind = kVUpper;
-        prep_slices = p.slices2 + slot * oz::panel_slice_bytes();
-        prep_exps = p.sexp2 + slot * 3 * NB;
+        prep_slices = q.slices2 + slot * oz::panel_slice_bytes();
+        prep_exps = q.sexp2 + slot * 3 * NB;
         break;
       }
       case kLARFB: {   // tile row k = the diagonal or a domain top
-        const size_t ov = tile_off(t.k, t.i, p.MT, NB), oc = tile_off(t.k, t.j, p.MT, NB);
+        const size_t ov = tile_off(t.k, t.i, q.MT, NB), oc = tile_off(t.k, t.j, q.MT, NB);
         if (OZ) {
-          const size_t slot = panel_slot(p.MT, t.i, t.k);
-          oz_slices = p.slices + slot * oz::panel_slice_bytes();
-          oz_exps = p.sexp + slot * 3 * NB;
-          oz_bot = p.C + oc + (size_t)t.c * oz::kN * NB;
+          const size_t slot = panel_slot(q.MT, t.i, t.k);
+          oz_slices = q.slices + slot * oz::panel_slice_bytes();
+          oz_exps = q.sexp + slot * 3 * NB;
+          oz_bot = q.C + oc + (size_t)t.c * oz::kN * NB;
         } else {
-          task_larfb(p.A + ov, p.T + ov, p.C + oc, t.c * p.sh.CB, p.sh.CB, p.sh, smem, p.sp,
-                     p.mode == kModeBuildQ);
+          task_larfb(q.A + ov, q.T + ov, q.C + oc, t.c * q.sh.CB, q.sh.CB, q.sh, smem, q.sp,
+                     q.mode == kModeBuildQ);
         }
         break;
       }
       case kSSRFB:     // A1 = the domain top's tile row
       case kTTMQR: {   // the merge's reflectors on [row i; the domain top's row] of column j
         const bool tt = t.type == kTTMQR;
-        const int top = tt ? t.i : dom_top(p, t.i, dom_of(p, t.i, t.k));
-        const size_t ov = tile_off(t.k, t.i, p.MT, NB);
-        const size_t o1 = tile_off(top, t.j, p.MT, NB), o2 = tile_off(t.k, t.j, p.MT, NB);
-        const size_t slot = tt ? merge_slot(p, t.i, dom_of(p, t.i, t.k)) : panel_slot(p.MT, t.i, t.k);
+        const int top = tt ? t.i : dom_top(q, t.i, dom_of(q, t.i, t.k));
+        const size_t ov = tile_off(t.k, t.i, q.MT, NB);
+        const size_t o1 = tile_off(top, t.j, q.MT, NB), o2 = tile_off(t.k, t.j, q.MT, NB);
+        const size_t slot = tt ? merge_slot(q, t.i, dom_of(q, t.i, t.k)) : panel_slot(q.MT, t.i, t.k);
         if (OZ) {
           const size_t cofs = (size_t)t.c * oz::kN * NB;
-          oz_slices = (tt ? p.slices2 : p.slices) + slot * oz::panel_slice_bytes();
-          oz_exps = (tt ? p.sexp2 : p.sexp) + slot * 3 * NB;
-          oz_top = p.C + o1 + cofs;
-          oz_bot = p.C + o2 + cofs;
+          oz_slices = (tt ? q.slices2 : q.slices) + slot * oz::panel_slice_bytes();
+          oz_exps = (tt ? q.sexp2 : q.sexp) + slot * 3 * NB;
+          oz_top = q.C + o1 + cofs;
+          oz_bot = q.C + o2 + cofs;
         } else {
-          task_ssrfb(p.C + o1, p.C + o2, p.A + ov, tt ? p.T2 + slot * tsz : p.T + ov, t.c * p.sh.CB,
-                     p.sh.CB, p.sh, smem, p.sp, p.mode == kModeBuildQ, tt);
+          task_ssrfb(q.C + o1, q.C + o2, q.A + ov, tt ? q.T2 + slot * tsz : q.T + ov, t.c * q.sh.CB,
+                     q.sh.CB, q.sh, smem, q.sp, q.mode == kModeBuildQ, tt);
         }
         break;
       }
       default:
-        if (threadIdx.x == 0) atomicOr((int*)(p.ctl + kErr), kErrBadTask);
+        if (threadIdx.x == 0) atomicOr((int*)(q.ctl + kErr), kErrBadTask);
     }
-    if (ts_a1) task_tsqrt_blk(ts_a1, ts_a2, ts_t, ts_tau, p.sh, smem, p.sp, t.c, ts_upper);
+    if (ts_a1) task_tsqrt_blk(ts_a1, ts_a2, ts_t, ts_tau, q.sh, smem, q.sp, t.c, ts_upper);
     if (OZ && prep_v)
       task_ozprep(prep_v, prep_tau, prep_g, prep_kind, prep_slices, prep_exps, reinterpret_cast<uint8_t*>(smem),
-                  s_tmem, p.ctl + kErr, p.mode != kModeBuildQ);
+                  s_tmem, q.ctl + kErr, q.mode != kModeBuildQ);
     if (OZ && oz_bot) {
       oz::Ctx c;
-      oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, p.ctl + kErr);
+      oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, q.ctl + kErr);
       task_ozapply(c, oz_slices, oz_exps, oz_top, oz_bot);
     }
-    (void)tsz;
     fence_acq_rel_gpu();   // release: this task's writes before its dependents' counters
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -670,11 +793,11 @@ __global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
       local_cyc[stat_slot(t.type)] += (unsigned long long)(c1 - c0);
       // the control words are read before the releases so that their round
       // trips overlap the releases' atomics
-      volatile unsigned* ctl = p.ctl;
+      volatile unsigned* ctl = q.ctl;
       const unsigned err_now = ctl[kErr], hi_head = ctl[kHiHead], hi_tail = ctl[kHiTail];
-      const bool pushed_hi = release_dependents(p, t, &next);
+      const bool pushed_hi = release_dependents(q, t, &next);
       cont_ok = err_now == 0u && hi_head >= hi_tail && !pushed_hi;
-      atomicAdd(p.ctl + kDone, 1u);   // termination count only: no ordering needed
+      atomicAdd(q.ctl + kDone, 1u);   // termination count only: no ordering needed
       local_cnt[kStatSched]++;
       local_cyc[kStatSched] += (unsigned long long)(clock64() - c1);
     }

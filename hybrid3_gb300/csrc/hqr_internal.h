@@ -101,6 +101,16 @@ int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, doubl
 // accumulation, skipping the tile columns that are still unit vectors.
 int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT, const double* dTAU,
                    double* dQ, long long timeout_ns, cudaStream_t stream, const OzWorkspace* oz = nullptr);
+// Batches of independent FP64 factorizations in one persistent launch.
+// Descriptors (mat_desc_bytes() each) are written to host memory by
+// batch_describe and must be on the device (d_desc) for launch_batch.
+size_t mat_desc_bytes();
+// apply: C <- Q^T C on the first nrhs columns of each C (else the factorization).
+long long batch_ids(bool apply, const Geometry& g, int nrhs);
+int batch_describe(bool apply, int count, const Geometry* gs, double* const* A, double* const* T,
+                   double* const* TAU, double* const* C, int nrhs, void* desc, int* n_ids, int* n_tasks);
+int launch_batch(bool apply, int count, const void* d_desc, int n_ids, int n_tasks, size_t smem,
+                 DagWorkspace* ws, long long timeout_ns, cudaStream_t stream);
 // Scratch supplied by the caller instead of a DagWorkspace (no allocation).
 struct ExternalScratch {
   double* T;

@@ -137,6 +137,40 @@ int hqr_ormqr_t(hqr_plan_t *plan, const double *dRY, const double *dTAU, double 
 int hqr_lstsq(hqr_plan_t *plan, const double *dA, const double *dB, int ldb, int nrhs, double *dX,
               int ldx, int refine_steps, double *resid, void *stream);
 
+/* No counterpart in the reference (it factors one matrix per run).  A batch
+ * of independent FP64 tile QRs of uneven shapes, each run of the batch one
+ * persistent launch of the DAG executor over every matrix's tasks (a
+ * per-matrix task table: tile counts, tile order, arrays, first task id).
+ * Matrix b is M[b] x N[b] in the NB[b] x NB[b] tile layout of hqr_geqrf (M, N
+ * multiples of NB[b]; zero padding to such a shape leaves the leading block
+ * of R and the reflectors unchanged), inner blocks min(IB[b], 32).  max_nrhs:
+ * the largest nrhs that hqr_batch_ormqr_t will be given (its scheduler tables
+ * are reserved here, so a call can be captured into a CUDA graph).  The batch
+ * owns the T factors of every matrix. */
+typedef struct hqr_batch hqr_batch_t;
+int hqr_batch_create(hqr_batch_t **batch, int count, const long *M, const long *N, const int *NB,
+                     const int *IB, int max_nrhs);
+int hqr_batch_destroy(hqr_batch_t *batch);
+/* Factor every matrix in place: dA[b], dTAU[b] (MT*NT*NB doubles) are device
+ * pointers held in a host array.  The _async form only enqueues; the first
+ * call with a new set of pointers uploads the task table and may not be
+ * captured into a graph (HQR_ERR_UNSUPPORTED): later calls with the same
+ * pointers enqueue kernels and memsets only. */
+int hqr_batch_geqrf(hqr_batch_t *batch, double *const *dA, double *const *dTAU, void *stream);
+int hqr_batch_geqrf_async(hqr_batch_t *batch, double *const *dA, double *const *dTAU, void *stream);
+/* Hybrid_dormqr for every matrix: the first nrhs columns of dC[b] <- Q_b^T
+ * dC[b] for the last factorization of the batch (its T factors).  dC[b] is an
+ * MT x ceil(nrhs / NB[b]) tile grid of NB[b] tiles; its columns from nrhs on
+ * may or may not be transformed.  nrhs <= max_nrhs. */
+int hqr_batch_ormqr_t(hqr_batch_t *batch, double *const *dA, double *const *dTAU, double *const *dC,
+                      int nrhs, void *stream);
+int hqr_batch_ormqr_t_async(hqr_batch_t *batch, double *const *dA, double *const *dTAU,
+                            double *const *dC, int nrhs, void *stream);
+/* Synchronise `stream`, then read and clear the batch scheduler's error word. */
+int hqr_batch_status(hqr_batch_t *batch, void *stream);
+/* Task counts and SM cycles of the batch's last run (as hqr_plan_stats). */
+int hqr_batch_stats(hqr_batch_t *batch, hqr_stats_t *out, void *stream);
+
 /* Tile-wise C = A^T B of square tiled matrices (Hybrid_dgemm). */
 int hqr_dgemm_tn(long N, int NB, const double *dA, const double *dB, double *dC, void *stream);
 /* Identity in tile layout (Hybrid_make_I). */
