@@ -524,17 +524,19 @@ def run_batched(H, torch, L, args):
     t0 = time.perf_counter()
     if args.batch_nb:
         nb_ib = tuple(int(x) for x in args.batch_nb.split("/"))
-        table = {c: {"nb": nb_ib[0], "ib": nb_ib[1], "n_range": list(r), "fixed": True}
-                 for c, r in enumerate(AT.CLASSES)}
+        table = AT.fixed_table(nb_ib[0], nb_ib[1], args.batch_ctas or 1)
     else:
         table = AT.tune_batch(H, torch, m, n, nrhs)
     tune_s = time.perf_counter() - t0
-    nb = [AT.choose(table, x)[0] for x in n]
-    ib = [AT.choose(table, x)[1] for x in n]
+    pick = [AT.choose(table, a, b, nrhs) for a, b in zip(m, n)]
+    nb = [p[0] for p in pick]
+    ib = [p[1] for p in pick]
+    from collections import Counter
+    nb_use = {f"{k[0]}/{k[1]}": v for k, v in sorted(Counter(pick).items())}
     stream = torch.cuda.Stream()
     s = stream.cuda_stream
     d = AT.BatchData(H, torch, m, n, nb, ib, nrhs, 20151130, stream)
-    bt = d.batch(H)
+    bt = d.batch(H, table["ctas"])
     ev = lambda: torch.cuda.Event(enable_timing=True)
 
     def step(rec=None):
@@ -569,7 +571,17 @@ def run_batched(H, torch, L, args):
     elapsed = t_start.elapsed_time(t_end) / 1e3 / args.steps
     fact = float(np.mean([r[0].elapsed_time(r[1]) for r in recs])) / 1e3
     appl = float(np.mean([r[1].elapsed_time(r[2]) for r in recs])) / 1e3
-    stats = bt.stats(s)
+    stats = bt.stats(s)   # of the last Q^T C launch
+    # per-type task counts and SM time of one more factorization (untimed)
+    with torch.cuda.stream(stream):
+        d.restore()
+    bt.geqrf(d.pa, d.pt, stream=s)
+    fstats = bt.stats(s)
+    bt.ormqr_t(d.pa, d.pt, d.pc, nrhs, stream=s)   # A and C as after a whole step again
+    tot = sum(fstats["cycles"]) or 1
+    types = ["geqrt", "tsqrt", "larfb", "ssrfb", "tbuild", "ozprep", "sched"]
+    geqrf_tasks = {t: {"count": c, "sm_share": round(y / tot, 4)}
+                   for t, c, y in zip(types, fstats["count"], fstats["cycles"]) if c}
 
     # accuracy on a sample (check only): R^T R against A^T A, and the
     # least-squares solution R \ (Q^T c)(1:n) against an FP64 solver's
@@ -652,7 +664,7 @@ def run_batched(H, torch, L, args):
                                f"n uniform in {{32..m}} step 32, entries uniform[-1,1) seeded per matrix; "
                                f"factorization + dormqr on {nrhs} right-hand sides each",
                    "count": count, "nrhs": nrhs,
-                   "nb_ib_per_class": {str(k): v for k, v in table.items()}, "tune_s": round(tune_s, 2),
+                   "autotune": AT.describe(table), "tune_s": round(tune_s, 2), "nb_ib_use": nb_use,
                    "l2": f"inputs ({8 * d.A0.numel() / 2**30:.1f} GiB) exceed the 129 MB L2; no flush",
                    "parallelism": "one GPU"},
         "phases_ms": {"geqrf": round(1e3 * fact, 3), "ormqr": round(1e3 * appl, 3)},
@@ -663,7 +675,7 @@ def run_batched(H, torch, L, args):
                      "padded_flops_frac": round(padded_flops / d.flops, 4),
                      "peak_source": "FP64 FMA issue rate measured in this run (hqr_fp64_peak_tflops)",
                      "traffic": None},
-        "task_counts": stats["count"],
+        "task_counts": {"geqrf": geqrf_tasks, "ormqr": stats["count"]},
         "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": 2 * 3 * args.steps,
         "clocks": clk,
@@ -701,6 +713,8 @@ def main():
     ap.add_argument("--batch", type=int, default=4096, help="matrices in the --batched workload")
     ap.add_argument("--batch-nrhs", type=int, default=4, help="right-hand sides per matrix for --batched")
     ap.add_argument("--batch-nb", default=None, help="fixed NB/IB for --batched (default: autotuned)")
+    ap.add_argument("--batch-ctas", type=int, default=0,
+                    help="executor CTAs per SM (1 or 2) for --batched with --batch-nb")
     ap.add_argument("--tree", type=int, default=0,
                     help="domain tree of this many tiles for the TS reduction (0: the flat tree)")
     args = ap.parse_args()

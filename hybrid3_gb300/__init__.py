@@ -110,7 +110,7 @@ SIGNATURES = {
     "hqr_colmajor_to_tiles_padded": (_I, [_L, _L, _L, _I, _vp, _vp, _vp]),
     "hqr_tiles_to_colmajor_padded": (_I, [_L, _L, _L, _I, _vp, _vp, _vp]),
     "hqr_batch_create": (_I, [ctypes.POINTER(_vp), _I, ctypes.POINTER(_L), ctypes.POINTER(_L),
-                              ctypes.POINTER(_I), ctypes.POINTER(_I), _I]),
+                              ctypes.POINTER(_I), ctypes.POINTER(_I), _I, _I]),
     "hqr_batch_destroy": (_I, [_vp]),
     "hqr_batch_geqrf": (_I, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), _vp]),
     "hqr_batch_geqrf_async": (_I, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), _vp]),
@@ -118,6 +118,7 @@ SIGNATURES = {
     "hqr_batch_ormqr_t_async": (_I, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp), _I,
                                      _vp]),
     "hqr_batch_status": (_I, [_vp, _vp]),
+    "hqr_batch_ctas_per_sm": (_I, [_vp]),
     "hqr_batch_stats": (_I, [_vp, ctypes.POINTER(HqrStats), _vp]),
     "hqr_dgemm_tn": (_I, [_L, _I, _vp, _vp, _vp, _vp]),
     "hqr_make_identity": (_I, [_L, _L, _I, _vp, _vp]),
@@ -227,11 +228,11 @@ class Batch:
     """Owns an hqr_batch_t: independent FP64 tile QRs of uneven shapes, each
     call one persistent launch over every matrix's tasks."""
 
-    def __init__(self, M, N, NB, IB, max_nrhs: int = 1):
+    def __init__(self, M, N, NB, IB, max_nrhs: int = 1, ctas_per_sm: int = 0):
         n = len(M)
         h = _vp()
         check(lib().hqr_batch_create(ctypes.byref(h), n, (_L * n)(*M), (_L * n)(*N), (_I * n)(*NB),
-                                     (_I * n)(*IB), max_nrhs), "hqr_batch_create")
+                                     (_I * n)(*IB), max_nrhs, ctas_per_sm), "hqr_batch_create")
         self.h = h
         self.count = n
         self._keep = []
@@ -258,6 +259,9 @@ class Batch:
         a, t, c = _ptrs(dA), _ptrs(dTAU), _ptrs(dC)
         fn = lib().hqr_batch_ormqr_t if wait else lib().hqr_batch_ormqr_t_async
         check(fn(self.h, a, t, c, nrhs, stream), "hqr_batch_ormqr_t")
+
+    def ctas_per_sm(self) -> int:
+        return lib().hqr_batch_ctas_per_sm(self.h)
 
     def status(self, stream=None):
         check(lib().hqr_batch_status(self.h, stream), "hqr_batch_status")

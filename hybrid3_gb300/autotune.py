@@ -4,11 +4,14 @@ QR (hqr_batch_*), measured on the device.
 The reference fixes NB and IB per run (main.c takes them from the command
 line).  A batch of uneven shapes has no single best pair: small matrices want
 small tiles (more tasks per matrix, less zero padding), large ones large tiles
-(fewer scheduling passes per flop).  The tuner splits the workload's shapes
-into size classes by their column count n, and for each class times every
-candidate (NB, IB) on a sample of the workload's own shapes in that class --
-the matrices zero-padded to NB multiples, as the batch runs them -- and keeps
-the fastest by algorithmic (unpadded) flops per second.
+(fewer scheduling passes per flop, faster update kernels).  The tuner splits
+the workload's shapes into size classes by their column count n, and for each
+class times every candidate (NB, IB) on a sample of the workload's own shapes
+in that class, zero-padded to NB multiples as the batch runs them: the rate of
+a candidate is the padded flops it executes per second.  Each matrix then
+takes the candidate with the least predicted time, its own padded flops at
+NB divided by its class's rate for that candidate -- so a 96 x 96 matrix can
+take NB 96 where the class's other shapes take 128.
 """
 from __future__ import annotations
 
@@ -18,7 +21,7 @@ import numpy as np
 
 # column-count classes (inclusive bounds) and the candidates tried in each
 CLASSES = ((1, 160), (161, 448), (449, 1024), (1025, 1 << 30))
-CANDIDATES = ((32, 32), (64, 32), (64, 16), (128, 32))
+CANDIDATES = ((64, 16), (96, 16), (96, 32), (128, 16), (128, 32), (192, 32), (256, 32))
 
 
 def class_of(n: int) -> int:
@@ -83,17 +86,26 @@ class BatchData:
         self.A.copy_(self.A0, non_blocking=True)
         self.C.copy_(self.C0, non_blocking=True)
 
-    def batch(self, H):
-        return H.Batch(self.Mp, self.Np, self.nb, self.ib, max_nrhs=self.nrhs)
+    def batch(self, H, ctas_per_sm: int = 0):
+        return H.Batch(self.Mp, self.Np, self.nb, self.ib, max_nrhs=self.nrhs, ctas_per_sm=ctas_per_sm)
+
+
+def padded_flops(m: int, n: int, nb: int, nrhs: int) -> float:
+    mp, np_ = padded(m, nb), padded(n, nb)
+    return qr_flops(mp, np_) + ormqr_flops(mp, np_, nrhs)
 
 
 def tune_batch(H, torch, m, n, nrhs: int, candidates=CANDIDATES, sample_flops: float = 1.5e11,
                max_sample: int = 600, seed: int = 7):
-    """(NB, IB) per size class for a workload of shapes (m[b], n[b]): a dict
-    class index -> {"nb", "ib", "n_range", "tflops": {candidate: measured}}."""
+    """Measured rates (padded TFLOP/s) of every candidate (NB, IB) per size
+    class, with one and, where the tiles fit, two executor CTAs per SM, for a
+    workload of shapes (m[b], n[b]); then the CTAs-per-SM setting (the same
+    for the whole batch) whose best per-matrix choices predict the least
+    total time.  Returns {"ctas": k, "classes": {class: {"n_range", "sample",
+    "rates": {k: {(NB, IB): rate}}}}}."""
     rng = np.random.default_rng(seed)
     m, n = np.asarray(m), np.asarray(n)
-    table = {}
+    classes = {}
     stream = torch.cuda.Stream()
     for c, (lo, hi) in enumerate(CLASSES):
         idx = np.nonzero((n >= lo) & (n <= hi))[0]
@@ -107,32 +119,70 @@ def tune_batch(H, torch, m, n, nrhs: int, candidates=CANDIDATES, sample_flops: f
             if acc >= sample_flops or len(take) >= max_sample:
                 break
         sm, sn = m[take].tolist(), n[take].tolist()
-        res = {}
+        rates = {1: {}, 2: {}}
         for nb, ib in candidates:
             d = BatchData(H, torch, sm, sn, [nb] * len(sm), [ib] * len(sm), nrhs, 1000 + c, stream)
-            bt = d.batch(H)
-            try:
-                times = []
-                for rep in range(2):   # the first run uploads the task tables
-                    with torch.cuda.stream(stream):
-                        d.restore()
-                    torch.cuda.synchronize()
-                    t0 = time.perf_counter()
-                    bt.geqrf(d.pa, d.pt, stream=stream.cuda_stream)
-                    bt.ormqr_t(d.pa, d.pt, d.pc, nrhs, stream=stream.cuda_stream)
-                    times.append(time.perf_counter() - t0)
-                res[(nb, ib)] = d.flops / times[-1] / 1e12
-            finally:
-                bt.close()
-                del d
-                torch.cuda.empty_cache()
-        best = max(res, key=res.get)
-        table[c] = {"nb": best[0], "ib": best[1], "n_range": [lo, hi], "sample": len(sm),
-                    "tflops": {f"{k[0]}/{k[1]}": round(v, 4) for k, v in res.items()}}
+            pf = sum(padded_flops(a, b, nb, nrhs) for a, b in zip(sm, sn))
+            for ctas in (1, 2):
+                try:
+                    bt = d.batch(H, ctas)
+                except RuntimeError:   # the tiles do not fit two CTAs per SM
+                    continue
+                try:
+                    times = []
+                    for rep in range(2):   # the first run uploads the task tables
+                        with torch.cuda.stream(stream):
+                            d.restore()
+                        torch.cuda.synchronize()
+                        t0 = time.perf_counter()
+                        bt.geqrf(d.pa, d.pt, stream=stream.cuda_stream)
+                        bt.ormqr_t(d.pa, d.pt, d.pc, nrhs, stream=stream.cuda_stream)
+                        times.append(time.perf_counter() - t0)
+                    rates[ctas][(nb, ib)] = pf / times[-1] / 1e12
+                finally:
+                    bt.close()
+            del d
+            torch.cuda.empty_cache()
+        classes[c] = {"rates": rates, "n_range": [lo, hi], "sample": len(sm)}
+    table = {"ctas": 1, "classes": classes}
+    best = None
+    for ctas in (1, 2):
+        if not all(e["rates"][ctas] for e in classes.values()):
+            continue
+        table["ctas"] = ctas
+        t = sum(predicted_time(table, int(a), int(b), nrhs) for a, b in zip(m, n))
+        if best is None or t < best[0]:
+            best = (t, ctas)
+    table["ctas"] = best[1]
     return table
 
 
-def choose(table, n: int, default=(64, 32)):
-    """(NB, IB) for a matrix with n columns from a tune_batch table."""
-    e = table.get(class_of(n))
-    return (e["nb"], e["ib"]) if e else default
+def fixed_table(nb: int, ib: int, ctas: int = 1):
+    """A table that picks (nb, ib) for every shape."""
+    return {"ctas": ctas, "classes": {c: {"rates": {ctas: {(nb, ib): 1.0}}, "n_range": list(r), "sample": 0}
+                                      for c, r in enumerate(CLASSES)}}
+
+
+def _best(table, m: int, n: int, nrhs: int):
+    rates = table["classes"][class_of(n)]["rates"][table["ctas"]]
+    k = min(rates, key=lambda k: padded_flops(m, n, k[0], nrhs) / rates[k])
+    return k, padded_flops(m, n, k[0], nrhs) / rates[k]
+
+
+def predicted_time(table, m: int, n: int, nrhs: int) -> float:
+    return _best(table, m, n, nrhs)[1]
+
+
+def choose(table, m: int, n: int, nrhs: int):
+    """(NB, IB) for an m x n matrix: the least predicted time over its class's
+    measured candidates at the table's CTAs per SM."""
+    return _best(table, m, n, nrhs)[0]
+
+
+def describe(table):
+    """A JSON-able summary of a tune_batch table."""
+    return {"ctas_per_sm": table["ctas"],
+            "classes": {str(c): {"n_range": e["n_range"], "sample": e["sample"],
+                                 "padded_tflops": {f"{k[0]}/{k[1]}/{ctas}": round(v, 4)
+                                                   for ctas, r in e["rates"].items() for k, v in r.items()}}
+                        for c, e in table["classes"].items()}}

@@ -605,6 +605,7 @@ struct hqr_batch {
   hqr::DagWorkspace ws;
   size_t smem = 0;
   int max_nrhs = 0;
+  int ctas_per_sm = 1;   // executor CTAs per SM
   struct Table {
     std::vector<unsigned char> host;   // the descriptors last uploaded
     unsigned char* pinned = nullptr;
@@ -656,18 +657,31 @@ int batch_table(hqr_batch* b, bool apply, double* const* dA, double* const* dTAU
 extern "C" {
 
 int hqr_batch_create(hqr_batch_t** batch, int count, const long* M, const long* N, const int* NB,
-                     const int* IB, int max_nrhs) {
+                     const int* IB, int max_nrhs, int ctas_per_sm) {
   if (!batch) return HQR_ERR_INVALID;
   *batch = nullptr;
-  if (count <= 0 || !M || !N || !NB || !IB || max_nrhs < 0) return HQR_ERR_INVALID;
+  if (count <= 0 || !M || !N || !NB || !IB || max_nrhs < 0 || ctas_per_sm < 0 || ctas_per_sm > 2)
+    return HQR_ERR_INVALID;
   hqr_batch* b = new hqr_batch();
   b->count = count;
   b->max_nrhs = max_nrhs;
   b->g.resize(count);
   size_t t_elems = 0;
   long long ids = 0, ids_apply = 0;
+  // two CTAs per SM when every matrix's tiles fit half an SM's shared memory
+  // (asked for, or by default when they all do)
+  bool two = ctas_per_sm != 1;
+  for (int i = 0; i < count && two; i++) {
+    hqr::Geometry g;
+    two = hqr::make_geometry(M[i], N[i], NB[i], IB[i], &g, hqr::batch_two_cta_smem()) == HQR_OK;
+  }
+  if (ctas_per_sm == 2 && !two) {
+    free_batch(b);
+    return HQR_ERR_UNSUPPORTED;
+  }
+  b->ctas_per_sm = two ? 2 : 1;
   for (int i = 0; i < count; i++) {
-    const int rc = hqr::make_geometry(M[i], N[i], NB[i], IB[i], &b->g[i]);
+    const int rc = hqr::make_geometry(M[i], N[i], NB[i], IB[i], &b->g[i], two ? hqr::batch_two_cta_smem() : 0);
     if (rc != HQR_OK) {
       free_batch(b);
       return rc;
@@ -719,7 +733,7 @@ int hqr_batch_geqrf_async(hqr_batch_t* b, double* const* dA, double* const* dTAU
   cudaStream_t s = (cudaStream_t)stream;
   TRY(batch_table(b, false, dA, dTAU, dA, 0, s));
   const hqr_batch::Table& t = b->tab[0];
-  return hqr::launch_batch(false, b->count, t.dev, t.n_ids, t.n_tasks, b->smem, &b->ws, g_timeout_ns, s);
+  return hqr::launch_batch(false, b->count, t.dev, t.n_ids, t.n_tasks, b->smem, b->ctas_per_sm, &b->ws, g_timeout_ns, s);
 }
 
 int hqr_batch_geqrf(hqr_batch_t* b, double* const* dA, double* const* dTAU, void* stream) {
@@ -735,7 +749,7 @@ int hqr_batch_ormqr_t_async(hqr_batch_t* b, double* const* dA, double* const* dT
   cudaStream_t s = (cudaStream_t)stream;
   TRY(batch_table(b, true, dA, dTAU, dC, nrhs, s));
   const hqr_batch::Table& t = b->tab[1];
-  return hqr::launch_batch(true, b->count, t.dev, t.n_ids, t.n_tasks, b->smem, &b->ws, g_timeout_ns, s);
+  return hqr::launch_batch(true, b->count, t.dev, t.n_ids, t.n_tasks, b->smem, b->ctas_per_sm, &b->ws, g_timeout_ns, s);
 }
 
 int hqr_batch_ormqr_t(hqr_batch_t* b, double* const* dA, double* const* dTAU, double* const* dC, int nrhs,
@@ -743,6 +757,8 @@ int hqr_batch_ormqr_t(hqr_batch_t* b, double* const* dA, double* const* dTAU, do
   TRY(hqr_batch_ormqr_t_async(b, dA, dTAU, dC, nrhs, stream));
   return hqr_batch_status(b, stream);
 }
+
+int hqr_batch_ctas_per_sm(hqr_batch_t* b) { return b ? b->ctas_per_sm : 0; }
 
 int hqr_batch_status(hqr_batch_t* b, void* stream) {
   if (!b) return HQR_ERR_INVALID;

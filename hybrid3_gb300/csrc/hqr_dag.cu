@@ -9,7 +9,7 @@
 
 namespace hqr {
 
-int make_geometry(long M, long N, int NB, int IB, Geometry* g) {
+int make_geometry(long M, long N, int NB, int IB, Geometry* g, size_t smem_limit) {
   if (NB < 16 || NB > kMaxNB || NB % 16 != 0) return HQR_ERR_UNSUPPORTED;
   if (M <= 0 || N <= 0 || M % NB != 0 || N % NB != 0) return HQR_ERR_INVALID;
   if (IB <= 0 || IB > NB) return HQR_ERR_INVALID;
@@ -28,7 +28,7 @@ int make_geometry(long M, long N, int NB, int IB, Geometry* g) {
   g->w = w;
   // column block of the update tasks: the widest multiple of 8 dividing NB,
   // at most 64 and at most NB*CB*8 <= 64 KiB, whose shared-memory plan fits
-  const size_t smem_cap = 227 * 1024 - 256;   // leave room for static shared memory
+  const size_t smem_cap = smem_limit ? smem_limit : 227 * 1024 - 256;   // room for static shared memory
   int cb = (8192 / NB) > 64 ? 64 : 8192 / NB;
   if (cb > NB) cb = NB;
   cb -= cb % 8;
@@ -353,8 +353,23 @@ int batch_describe(bool apply, int count, const Geometry* gs, double* const* A, 
   return HQR_OK;
 }
 
+size_t batch_two_cta_smem() {
+  static size_t v = 0;
+  if (v == 0) {
+    int dev = 0, per_sm = 0;
+    cudaFuncAttributes fa{};
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaFuncGetAttributes(&fa, dag_exec_kernel<false, true>);
+    // per CTA: the dynamic part, the kernel's static part and 1 KiB the system reserves
+    const long long b = (long long)per_sm / 2 - (long long)fa.sharedSizeBytes - 1024;
+    v = b > 0 ? (size_t)b : 1;
+  }
+  return v;
+}
+
 int launch_batch(bool apply, int count, const void* d_desc, int n_ids, int n_tasks, size_t smem,
-                 DagWorkspace* ws, long long timeout_ns, cudaStream_t stream) {
+                 int ctas_per_sm, DagWorkspace* ws, long long timeout_ns, cudaStream_t stream) {
   if (count <= 0 || n_tasks <= 0) return HQR_ERR_INVALID;
   DagParams p{};
   p.mode = apply ? kModeApplyQt : kModeFactor;
@@ -376,18 +391,26 @@ int launch_batch(bool apply, int count, const void* d_desc, int n_ids, int n_tas
   if (e != cudaSuccess) return record_cuda_error(e, "DAG workspace reset");
   static std::mutex mu;
   static size_t attr_bytes = 0;
+  int occ = 1;
   {
     std::lock_guard<std::mutex> lk(mu);
     if (smem > attr_bytes) {
       e = cudaFuncSetAttribute(dag_exec_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(dag_exec_kernel<false, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
       if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(dag_exec_kernel batch)");
       attr_bytes = smem;
     }
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dag_exec_kernel<false, true>, kThreads, smem);
+    if (e != cudaSuccess) return record_cuda_error(e, "occupancy of dag_exec_kernel batch");
   }
+  if (occ < 1) return HQR_ERR_UNSUPPORTED;
+  if (ctas_per_sm > 0) occ = std::min(occ, ctas_per_sm);
   dag_init_batch_kernel<<<count, 256, 0, stream>>>(p);
   dag_seed_batch_kernel<<<count, 256, 0, stream>>>(p);
-  const int grid = std::min(dag_sm_count(), std::max(1, n_tasks));
+  const int grid = std::min(occ * dag_sm_count(), std::max(1, n_tasks));
   dag_exec_kernel<false, true><<<grid, kThreads, smem, stream>>>(p);
   e = cudaGetLastError();
   if (e != cudaSuccess) return record_cuda_error(e, "dag_exec_kernel batch launch");

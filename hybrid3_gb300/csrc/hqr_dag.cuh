@@ -633,9 +633,11 @@ __device__ void task_tbuild(const double* V, const double* tau_g, double* T, boo
 
 // --- the persistent executor ---------------------------------------------------------
 // BATCH: the tasks of many matrices (FP64 tile kernels only); each task runs
-// with its matrix's fields (s_b.lp).
+// with its matrix's fields (s_b.lp).  Up to two CTAs per SM (at most 128
+// registers per thread): while one runs a latency-bound panel column loop,
+// the other's update keeps the FP64 pipe busy.
 template <bool OZ, bool BATCH = false>
-__global__ void __launch_bounds__(kThreads, 1) dag_exec_kernel(DagParams p) {
+__global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagParams p) {
   extern __shared__ __align__(1024) double smem[];
   __shared__ int s_id;
   __shared__ uint32_t s_tmem;

@@ -19,7 +19,9 @@ struct Geometry {
   size_t smem_bytes;
 };
 
-int make_geometry(long M, long N, int NB, int IB, Geometry* g);
+// smem_limit: bytes of dynamic shared memory the executor may use (0: one CTA
+// per SM); the update tasks' column block narrows to fit.
+int make_geometry(long M, long N, int NB, int IB, Geometry* g, size_t smem_limit = 0);
 
 // Remember the text of a failed CUDA call (reported by hqr_last_cuda_error)
 // and return HQR_ERR_CUDA.
@@ -109,8 +111,11 @@ size_t mat_desc_bytes();
 long long batch_ids(bool apply, const Geometry& g, int nrhs);
 int batch_describe(bool apply, int count, const Geometry* gs, double* const* A, double* const* T,
                    double* const* TAU, double* const* C, int nrhs, void* desc, int* n_ids, int* n_tasks);
+// Dynamic shared memory per executor CTA that lets two CTAs share an SM.
+size_t batch_two_cta_smem();
+// ctas_per_sm: executor CTAs per SM (0: as many as fit, at most 2).
 int launch_batch(bool apply, int count, const void* d_desc, int n_ids, int n_tasks, size_t smem,
-                 DagWorkspace* ws, long long timeout_ns, cudaStream_t stream);
+                 int ctas_per_sm, DagWorkspace* ws, long long timeout_ns, cudaStream_t stream);
 // Scratch supplied by the caller instead of a DagWorkspace (no allocation).
 struct ExternalScratch {
   double* T;

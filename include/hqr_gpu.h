@@ -145,11 +145,17 @@ int hqr_lstsq(hqr_plan_t *plan, const double *dA, const double *dB, int ldb, int
  * multiples of NB[b]; zero padding to such a shape leaves the leading block
  * of R and the reflectors unchanged), inner blocks min(IB[b], 32).  max_nrhs:
  * the largest nrhs that hqr_batch_ormqr_t will be given (its scheduler tables
- * are reserved here, so a call can be captured into a CUDA graph).  The batch
+ * are reserved here, so a call can be captured into a CUDA graph).
+ * ctas_per_sm: executor CTAs per SM.  2 runs two on each SM (while one is in
+ * a latency-bound panel column loop the other's update keeps the FP64 pipe
+ * busy); every matrix's tile plan must then fit half an SM's shared memory
+ * (the update tasks' column blocks narrow to fit; NB <= 128 with inner blocks
+ * of 16, NB <= 64 with 32), else HQR_ERR_UNSUPPORTED.  1: one per SM, the
+ * widest column blocks.  0: 2 when every matrix fits, else 1.  The batch
  * owns the T factors of every matrix. */
 typedef struct hqr_batch hqr_batch_t;
 int hqr_batch_create(hqr_batch_t **batch, int count, const long *M, const long *N, const int *NB,
-                     const int *IB, int max_nrhs);
+                     const int *IB, int max_nrhs, int ctas_per_sm);
 int hqr_batch_destroy(hqr_batch_t *batch);
 /* Factor every matrix in place: dA[b], dTAU[b] (MT*NT*NB doubles) are device
  * pointers held in a host array.  The _async form only enqueues; the first
@@ -166,6 +172,8 @@ int hqr_batch_ormqr_t(hqr_batch_t *batch, double *const *dA, double *const *dTAU
                       int nrhs, void *stream);
 int hqr_batch_ormqr_t_async(hqr_batch_t *batch, double *const *dA, double *const *dTAU,
                             double *const *dC, int nrhs, void *stream);
+/* Executor CTAs per SM of the batch's launches (1 or 2). */
+int hqr_batch_ctas_per_sm(hqr_batch_t *batch);
 /* Synchronise `stream`, then read and clear the batch scheduler's error word. */
 int hqr_batch_status(hqr_batch_t *batch, void *stream);
 /* Task counts and SM cycles of the batch's last run (as hqr_plan_stats). */

@@ -30,7 +30,8 @@ def tol(A2d):
 # M, N, NB, IB: tall, square, wide, one tile, mixed tile orders in one batch
 SHAPES = [(64, 32, 32, 8), (256, 128, 64, 16), (384, 384, 128, 32), (128, 128, 32, 32),
           (512, 128, 128, 32), (96, 96, 32, 16), (640, 192, 64, 32), (32, 32, 32, 8),
-          (256, 512, 64, 16), (1024, 256, 128, 32), (192, 64, 64, 16), (448, 448, 64, 32)]
+          (256, 512, 64, 16), (1024, 256, 128, 32), (192, 64, 64, 16), (448, 448, 64, 32),
+          (288, 192, 96, 32), (384, 384, 192, 32), (192, 96, 96, 16), (512, 256, 256, 32)]
 
 
 def rhs_tiles(C2d, NB):
@@ -99,6 +100,23 @@ def test_batch_matches_oracle_per_matrix(env, nrhs):
         want = [w + v for w, v in zip(want, c[:6])]
     assert st["count"][:6] == want
     assert st["count"][6] == sum(want)   # one scheduling pass per task
+
+
+@pytest.mark.parametrize("ctas", [1, 2])
+def test_batch_ctas_per_sm(env, ctas):
+    """Small tiles run with one or two executor CTAs per SM: same results."""
+    H, torch = env
+    shapes = [s for s in SHAPES if s[2] <= 64 or (s[2] == 128 and s[3] == 16)] + [(512, 384, 128, 16)]
+    A, C, dA, dT, dC = make_batch(H, torch, shapes, 620, 4)
+    bt = H.Batch([s[0] for s in shapes], [s[1] for s in shapes], [s[2] for s in shapes],
+                 [s[3] for s in shapes], max_nrhs=4, ctas_per_sm=ctas)
+    try:
+        assert bt.ctas_per_sm() == ctas
+        bt.geqrf([x.data_ptr() for x in dA], [x.data_ptr() for x in dT])
+        bt.ormqr_t([x.data_ptr() for x in dA], [x.data_ptr() for x in dT], [x.data_ptr() for x in dC], 4)
+    finally:
+        bt.close()
+    check_against_oracle(shapes, A, C, dA, dT, dC, 4)
 
 
 def test_batch_many_small_uneven(env):
@@ -198,8 +216,11 @@ def test_batch_invalid_arguments(env):
     Ls, Is = ctypes.c_long, ctypes.c_int
     # M not a multiple of NB
     assert L.hqr_batch_create(ctypes.byref(h), 1, (Ls * 1)(100), (Ls * 1)(64), (Is * 1)(64), (Is * 1)(16),
-                              1) == H.HQR_ERR_INVALID
-    assert L.hqr_batch_create(ctypes.byref(h), 0, None, None, None, None, 1) == H.HQR_ERR_INVALID
+                              1, 0) == H.HQR_ERR_INVALID
+    assert L.hqr_batch_create(ctypes.byref(h), 0, None, None, None, None, 1, 0) == H.HQR_ERR_INVALID
+    # NB 256 tiles do not fit two executor CTAs per SM
+    assert L.hqr_batch_create(ctypes.byref(h), 1, (Ls * 1)(256), (Ls * 1)(256), (Is * 1)(256), (Is * 1)(32),
+                              1, 2) == H.HQR_ERR_UNSUPPORTED
     bt = H.Batch([128], [128], [64], [16], max_nrhs=4)
     dA = torch.zeros(128 * 128, dtype=torch.float64, device="cuda")
     dT = torch.zeros(2 * 2 * 64, dtype=torch.float64, device="cuda")
