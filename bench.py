@@ -583,33 +583,32 @@ def run_batched(H, torch, L, args):
     geqrf_tasks = {t: {"count": c, "sm_share": round(y / tot, 4)}
                    for t, c, y in zip(types, fstats["count"], fstats["cycles"]) if c}
 
-    # accuracy on a sample (check only): R^T R against A^T A, and the
-    # least-squares solution R \ (Q^T c)(1:n) against an FP64 solver's
+    # accuracy on a sample (check only, on the host): R^T R against A^T A, and
+    # the least-squares solution R \\ (Q^T c)(1:n) against numpy's FP64 solver
     acc = {"gram_rel_max": 0.0, "lstsq_rel_max": 0.0, "sample": 0}
     f64 = torch.float64
-    for b in range(0, count, max(1, count // 24)):
+    import scipy.linalg as sla
+    for b in (range(0, count, max(1, count // 16)) if not args.no_check else []):
         mm, nn, NB = m[b], n[b], nb[b]
         Mp, Np = d.Mp[b], d.Np[b]
-        cmA = torch.empty(Np * Mp, dtype=f64, device="cuda")
-        cmA0 = torch.empty_like(cmA)
         Cw = -(-nrhs // NB) * NB
-        cmC = torch.empty(Cw * Mp, dtype=f64, device="cuda")
-        cmC0 = torch.empty_like(cmC)
-        for src, dst, cols, off in ((d.A, cmA, Np, d.a_off), (d.A0, cmA0, Np, d.a_off),
-                                    (d.C, cmC, Cw, d.c_off), (d.C0, cmC0, Cw, d.c_off)):
+        out = {}
+        for key, src, cols, off in (("A", d.A, Np, d.a_off), ("A0", d.A0, Np, d.a_off),
+                                    ("C", d.C, Cw, d.c_off), ("C0", d.C0, Cw, d.c_off)):
+            dst = torch.empty(cols * Mp, dtype=f64, device="cuda")
             H.check(L.hqr_tiles_to_colmajor_padded(Mp, cols, Mp, NB, src.data_ptr() + 8 * int(off[b]),
                                                    dst.data_ptr(), None), "from tiles")
-        A0 = cmA0.view(Np, Mp).T[:mm, :nn]
-        R = torch.triu(cmA.view(Np, Mp).T[:nn, :nn])
-        QtC = cmC.view(Cw, Mp).T[:nn, :nrhs]
-        C0 = cmC0.view(Cw, Mp).T[:mm, :nrhs]
+            out[key] = dst.cpu().numpy().reshape(cols, Mp).T
+        A0 = out["A0"][:mm, :nn]
+        R = np.triu(out["A"][:nn, :nn])
+        QtC = out["C"][:nn, :nrhs]
+        C0 = out["C0"][:mm, :nrhs]
         G = A0.T @ A0
-        acc["gram_rel_max"] = max(acc["gram_rel_max"], float(torch.linalg.norm(R.T @ R - G) / torch.linalg.norm(G)))
-        x = torch.linalg.solve_triangular(R, QtC, upper=True)
-        xr = torch.linalg.lstsq(A0, C0).solution
-        acc["lstsq_rel_max"] = max(acc["lstsq_rel_max"], float(torch.linalg.norm(x - xr) / torch.linalg.norm(xr)))
+        acc["gram_rel_max"] = max(acc["gram_rel_max"], float(np.linalg.norm(R.T @ R - G) / np.linalg.norm(G)))
+        x = sla.solve_triangular(R, QtC)
+        xr = np.linalg.lstsq(A0, C0, rcond=None)[0]
+        acc["lstsq_rel_max"] = max(acc["lstsq_rel_max"], float(np.linalg.norm(x - xr) / np.linalg.norm(xr)))
         acc["sample"] += 1
-    torch.cuda.synchronize()
 
     # end to end: pinned host arrays in, R + reflectors, TAU and Q^T C out
     e2e = None
