@@ -232,10 +232,12 @@ def graded_tiles(H, torch, L, n: int, NBs, kappa: float, seed: int):
 
 
 def measure(H, torch, L, args, precision: str, n: int, NB: int, IB: int, steps: int, warmup: int,
-            dist, world: int, clocks_too: bool, check: bool, init=None):
-    """Time `steps` device-resident steps (factorization + make_Q).  init: the
-    input in tile layout (device), else the seeded uniform matrix."""
-    M = N = n
+            dist, world: int, clocks_too: bool, check: bool, init=None, rows=None):
+    """Time `steps` device-resident steps (factorization + make_Q) of an
+    rows x n matrix (square when rows is None).  init: the input in tile
+    layout (device), else the seeded uniform matrix."""
+    N = n
+    M = rows or n
     ntau = (M // NB) * (N // NB) * NB
     prec = H.HQR_PREC_OZAKI if precision == "split" else H.HQR_PREC_FP64
     stream = torch.cuda.Stream()
@@ -250,6 +252,8 @@ def measure(H, torch, L, args, precision: str, n: int, NB: int, IB: int, steps: 
     else:
         dA0.copy_(init)
     plan = H.Plan(M, N, NB, IB, prec)
+    if args.tree:
+        plan.set_tree(args.tree)
     ev = lambda: torch.cuda.Event(enable_timing=True)
 
     def step(rec=None):
@@ -299,7 +303,25 @@ def measure(H, torch, L, args, precision: str, n: int, NB: int, IB: int, steps: 
     mq_s = [r[2].elapsed_time(r[3]) / 1e3 for r in recs]
     stats_mq = plan.stats(s)
     acc = {}
-    if check:
+    if check and M != N:
+        # tall: Q^T I_{M x N} has orthonormal columns, and R^T R = A^T A
+        f64 = torch.float64
+        cm = torch.empty(M * N, dtype=f64, device="cuda")
+        H.check(L.hqr_tiles_to_colmajor(M, N, NB, dQ.data_ptr(), cm.data_ptr(), s), "from tiles")
+        torch.cuda.synchronize()
+        X = cm.view(N, M).T
+        acc["orth_fro"] = float(torch.linalg.norm(X.T @ X - torch.eye(N, dtype=f64, device="cuda")))
+        torch.cuda.synchronize()
+        H.check(L.hqr_tiles_to_colmajor(M, N, NB, dA0.data_ptr(), cm.data_ptr(), s), "from tiles")
+        torch.cuda.synchronize()
+        G = X.T @ X   # X now views A0
+        Rt = torch.empty(M * N, dtype=f64, device="cuda")
+        H.check(L.hqr_tiles_to_colmajor(M, N, NB, dA.data_ptr(), Rt.data_ptr(), s), "from tiles")
+        torch.cuda.synchronize()
+        R = torch.triu(Rt.view(N, M).T[:N])
+        acc["gram_rel"] = float(torch.linalg.norm(R.T @ R - G) / torch.linalg.norm(G))
+        del cm, X, G, Rt, R
+    elif check:
         # ||A - Q R||_F / ||A||_F and ||I - Q Q^T||_F from the Q^T array of the last
         # step, on the device in FP64 (the checks of main.c:201-258)
         dW = torch.empty_like(dA0)
@@ -707,6 +729,8 @@ def main():
     ap.add_argument("--m", type=int, default=32768, help="rows of A for --lstsq")
     ap.add_argument("--nrhs", type=int, default=16, help="right-hand sides for --lstsq")
     ap.add_argument("--refine", type=int, default=1, help="FP64 refinement steps for --lstsq")
+    ap.add_argument("--rows", type=int, default=None,
+                    help="rows of A for the QR + make_Q workload (default: square, --n)")
     ap.add_argument("--batched", action="store_true",
                     help="batched uneven QR + dormqr workload through hqr_batch_*")
     ap.add_argument("--batch", type=int, default=4096, help="matrices in the --batched workload")
@@ -760,19 +784,23 @@ def main():
                          args.kappa, 1000 + rank)
         init = t[NB]
         init64 = t.get(args.fp64_nb)
+    rows = args.rows if args.rows and args.rows != n else None
+    M = rows or n
+    if rows and args.kappa is not None:
+        raise SystemExit("--kappa inputs are square")
     main_run = measure(H, torch, L, args, args.precision, n, NB, IB, args.steps, args.warmup, dist,
-                       world, True, not args.no_check, init)
+                       world, True, not args.no_check, init, rows)
     value = main_run["flops"] / main_run["elapsed"] / 1e12
 
     e2e = None
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else args.steps
-    if e2e_steps > 0:
+    if e2e_steps > 0 and rows is None:
         e2e = measure_e2e(H, torch, L, args.precision, n, NB, IB, e2e_steps, dist, world)
 
     compare = None
     if args.precision == "split" and not args.no_compare:
         fp = measure(H, torch, L, args, "fp64", n, args.fp64_nb, IB, 1, 1, dist, world, False,
-                     not args.no_check, init64)
+                     not args.no_check, init64, rows)
         fv = fp["flops"] / fp["elapsed"] / 1e12
         compare = {"value": round(fv, 6), "unit": "TFLOP/s", "NB": args.fp64_nb, "IB": IB,
                    "steps": 1, "warmup": 1, "ms_per_step": round(1e3 * fp["elapsed"], 3),
@@ -788,7 +816,7 @@ def main():
                "sample": f"one {args.cpu_n}x{args.cpu_n} factorization + make_Q (NB=256, IB={IB})"}
 
     fact_mean = float(np.mean(main_run["fact_s"]))
-    achieved = qr_flops(n, n) / fact_mean / 1e12
+    achieved = qr_flops(M, n) / fact_mean / 1e12
     peaks = measured_peaks()
     if args.precision == "split":
         bf16 = peaks.get("bf16_tflops_sustained") or 1700.0
@@ -800,7 +828,7 @@ def main():
                     "peak_source": f"emulated FP64 peak = MEASURED_PEAKS.json bf16_tflops_sustained "
                                    f"({bf16}) / {prods} slice products (of measured)",
                     "traffic": load_traffic(n, NB, "split"),
-                    "algorithmic_flops_per_launch": qr_flops(n, n)}
+                    "algorithmic_flops_per_launch": qr_flops(M, n)}
     else:
         roofline = {"kernel": "dag_exec_kernel<fp64> (factorization launch)", "bound": "fp64",
                     "achieved": round(achieved, 4), "peak": round(peak_fp64, 4), "unit": "TFLOP/s",
@@ -808,7 +836,7 @@ def main():
                     "peak_source": "FP64 FMA issue rate measured in this run (hqr_fp64_peak_tflops); "
                                    "MEASURED_PEAKS.json holds no FP64 figure",
                     "traffic": load_traffic(n, NB, "fp64"),
-                    "algorithmic_flops_per_launch": qr_flops(n, n)}
+                    "algorithmic_flops_per_launch": qr_flops(M, n)}
     launches_per_step = 3 + 5
     line = {
         "metric": METRIC, "value": round(value, 6), "unit": "TFLOP/s", "n_gpus": world,
@@ -816,13 +844,14 @@ def main():
         "ms_per_step": round(1e3 * main_run["elapsed"] / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"tiled QR + Q generation (make_Q), n={n} square, NB={NB}, IB={IB}, " +
+        "config": {"workload": f"tiled QR + Q generation (make_Q), " +
+                               (f"n={n} square" if rows is None else f"{M}x{n} tall") + f", NB={NB}, IB={IB}, " +
                                ("uniform[-1,1) seed 20151130" if args.kappa is None else
                                 f"graded A = U diag(sigma) V^T, U, V Haar, kappa={args.kappa:g}"),
-                   "n": n, "NB": NB, "IB": IB,
+                   "n": n, "rows": M, "NB": NB, "IB": IB, "tree_domain_tiles": args.tree,
                    "precision": ("split (Ozaki BF16 slices on tcgen05, FP64 panels)"
                                  if args.precision == "split" else "fp64 (plain)"),
-                   "l2": "inputs (2 GiB per matrix) exceed the 129 MB L2; no flush",
+                   "l2": f"inputs ({8 * M * n / 2**30:.0f} GiB per matrix) exceed the 129 MB L2; no flush",
                    "parallelism": f"replicas x{world}"},
         "phases_ms": {"factor": round(1e3 * fact_mean, 3),
                       "make_q": round(1e3 * float(np.mean(main_run["mq_s"])), 3)},
