@@ -39,6 +39,15 @@ METRIC = "tile-QR TFLOP/s at FP64-level backward error: split-precision vs plain
 DP = ctypes.POINTER(ctypes.c_double)
 
 
+PRECISION_TEXT = {"split": "split (Ozaki BF16 slices on tcgen05, FP64 panels)",
+                  "fast": "reduced split (the 10 slice products of weight <= 3 on tcgen05, FP64 panels)",
+                  "fp64": "fp64 (plain)"}
+
+
+def prec_code(H, precision: str) -> int:
+    return {"split": H.HQR_PREC_OZAKI, "fast": H.HQR_PREC_OZAKI_FAST}.get(precision, H.HQR_PREC_FP64)
+
+
 def qr_flops(m: int, n: int) -> float:
     return 2.0 * m * n * n - 2.0 * n ** 3 / 3.0
 
@@ -239,7 +248,7 @@ def measure(H, torch, L, args, precision: str, n: int, NB: int, IB: int, steps: 
     N = n
     M = rows or n
     ntau = (M // NB) * (N // NB) * NB
-    prec = H.HQR_PREC_OZAKI if precision == "split" else H.HQR_PREC_FP64
+    prec = prec_code(H, precision)
     stream = torch.cuda.Stream()
     s = stream.cuda_stream
     f64 = torch.float64
@@ -349,7 +358,7 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
     """The same workload through the drop-in C entry points with pinned host arrays:
     Hybrid_tile_QR then Hybrid_make_Q, host<->device copies inside the timed region."""
     M = N = n
-    L.hqr_set_default_precision(H.HQR_PREC_OZAKI if precision == "split" else H.HQR_PREC_FP64)
+    L.hqr_set_default_precision(prec_code(H, precision))
     f64 = torch.float64
     gen = torch.empty(M * N, dtype=f64, device="cuda")
     H.check(L.hqr_fill_uniform(M, N, NB, 20151130, gen.data_ptr(), None), "fill")
@@ -421,7 +430,7 @@ def run_lstsq(H, torch, L, args):
     (torch.linalg.lstsq, check only) and against x_true."""
     m, n, nrhs, NB, IB = args.m, args.n, args.nrhs, args.nb, args.ib
     kappa = args.kappa if args.kappa is not None else 1e3
-    prec = H.HQR_PREC_OZAKI if args.precision == "split" else H.HQR_PREC_FP64
+    prec = prec_code(H, args.precision)
     f64 = torch.float64
     gen = torch.Generator(device="cuda")
     gen.manual_seed(20151130)
@@ -476,8 +485,7 @@ def run_lstsq(H, torch, L, args):
                                f"b = A x_true + 1e-8 noise",
                    "m": m, "n": n, "nrhs": nrhs, "kappa": kappa, "NB": NB, "IB": IB,
                    "refine_steps": args.refine, "tree_domain_tiles": args.tree,
-                   "precision": ("split (Ozaki BF16 slices on tcgen05, FP64 panels)"
-                                 if args.precision == "split" else "fp64 (plain)")},
+                   "precision": PRECISION_TEXT[args.precision]},
         "accuracy": {"forward_error_vs_fp64_lstsq": rel(x, x_ref),
                      "forward_error_vs_x_true": rel(x, x_true),
                      "fp64_lstsq_error_vs_x_true": rel(x_ref, x_true),
@@ -712,7 +720,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=None, help="order (default 16384; 8192 columns with --lstsq)")
-    ap.add_argument("--precision", default="split", choices=["split", "fp64"])
+    ap.add_argument("--precision", default="split", choices=["split", "fast", "fp64"])
     ap.add_argument("--nb", type=int, default=None, help="tile order (default 128 split, 256 fp64)")
     ap.add_argument("--ib", type=int, default=32)
     ap.add_argument("--fp64-nb", type=int, default=256, help="tile order of the plain-FP64 comparison")
@@ -744,7 +752,7 @@ def main():
     if args.n is None:
         args.n = 8192 if args.lstsq else 16384
     if args.nb is None:
-        args.nb = 128 if args.precision == "split" else 256
+        args.nb = 128 if args.precision in ("split", "fast") else 256
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -779,7 +787,7 @@ def main():
     peak_fp64 = L.hqr_fp64_peak_tflops(None)
     init = init64 = None
     if args.kappa is not None:
-        compare_too = args.precision == "split" and not args.no_compare
+        compare_too = args.precision in ("split", "fast") and not args.no_compare
         t = graded_tiles(H, torch, L, n, sorted({NB, args.fp64_nb} if compare_too else {NB}),
                          args.kappa, 1000 + rank)
         init = t[NB]
@@ -798,7 +806,7 @@ def main():
         e2e = measure_e2e(H, torch, L, args.precision, n, NB, IB, e2e_steps, dist, world)
 
     compare = None
-    if args.precision == "split" and not args.no_compare:
+    if args.precision in ("split", "fast") and not args.no_compare:
         fp = measure(H, torch, L, args, "fp64", n, args.fp64_nb, IB, 1, 1, dist, world, False,
                      not args.no_check, init64, rows)
         fv = fp["flops"] / fp["elapsed"] / 1e12
@@ -818,9 +826,9 @@ def main():
     fact_mean = float(np.mean(main_run["fact_s"]))
     achieved = qr_flops(M, n) / fact_mean / 1e12
     peaks = measured_peaks()
-    if args.precision == "split":
+    if args.precision in ("split", "fast"):
         bf16 = peaks.get("bf16_tflops_sustained") or 1700.0
-        prods = split_products(NB)
+        prods = split_products(NB) if args.precision == "split" else 10
         peak = bf16 / prods
         roofline = {"kernel": "dag_exec_kernel<split> (factorization launch)", "bound": "tensor",
                     "achieved": round(achieved, 4), "peak": round(peak, 4), "unit": "TFLOP/s",
@@ -849,8 +857,7 @@ def main():
                                ("uniform[-1,1) seed 20151130" if args.kappa is None else
                                 f"graded A = U diag(sigma) V^T, U, V Haar, kappa={args.kappa:g}"),
                    "n": n, "rows": M, "NB": NB, "IB": IB, "tree_domain_tiles": args.tree,
-                   "precision": ("split (Ozaki BF16 slices on tcgen05, FP64 panels)"
-                                 if args.precision == "split" else "fp64 (plain)"),
+                   "precision": PRECISION_TEXT[args.precision],
                    "l2": f"inputs ({8 * M * n / 2**30:.0f} GiB per matrix) exceed the 129 MB L2; no flush",
                    "parallelism": f"replicas x{world}"},
         "phases_ms": {"factor": round(1e3 * fact_mean, 3),

@@ -21,7 +21,7 @@ struct hqr_plan {
   int precision;
   double* dT;
   hqr::DagWorkspace ws;
-  hqr::OzWorkspace oz;   // allocated for HQR_PREC_OZAKI only
+  hqr::OzWorkspace oz;   // allocated for the split precisions only
   hqr::TreeWorkspace tree;   // domain tree (hqr_plan_set_tree); S = 0: flat
 };
 
@@ -107,6 +107,8 @@ int check_status(const mat_stat_t* st, int my_rank, int Proc_num) {
 
 size_t tau_len(const hqr::Geometry& g) { return (size_t)g.MT * g.NT * g.NB; }
 
+bool split_precision(int precision) { return precision == HQR_PREC_OZAKI || precision == HQR_PREC_OZAKI_FAST; }
+
 #define TRY(x)                      \
   do {                              \
     int _rc = (x);                  \
@@ -178,13 +180,14 @@ void hqr_set_error_mode(int mode) { g_error_mode = mode; }
 int hqr_get_default_precision(void) {
   if (g_default_precision < 0) {
     const char* e = getenv("HQR_PRECISION");
-    g_default_precision =
-        (e && (!strcmp(e, "ozaki") || !strcmp(e, "split"))) ? HQR_PREC_OZAKI : HQR_PREC_FP64;
+    g_default_precision = (e && (!strcmp(e, "ozaki") || !strcmp(e, "split")))  ? HQR_PREC_OZAKI
+                          : (e && !strcmp(e, "fast"))                             ? HQR_PREC_OZAKI_FAST
+                                                                                  : HQR_PREC_FP64;
   }
   return g_default_precision;
 }
 void hqr_set_default_precision(int precision) {
-  g_default_precision = (precision == HQR_PREC_OZAKI) ? HQR_PREC_OZAKI : HQR_PREC_FP64;
+  g_default_precision = split_precision(precision) ? precision : HQR_PREC_FP64;
 }
 int hqr_last_error(void) { return g_last_error; }
 const char* hqr_last_cuda_error(void) { return g_cuda_msg; }
@@ -193,11 +196,11 @@ void hqr_set_timeout_ms(long long ms) { g_timeout_ns = (ms > 0 ? ms : 1) * 10000
 int hqr_plan_create(hqr_plan_t** plan, long M, long N, int NB, int IB, int precision) {
   if (!plan) return HQR_ERR_INVALID;
   *plan = nullptr;
-  if (precision != HQR_PREC_FP64 && precision != HQR_PREC_OZAKI) return HQR_ERR_INVALID;
+  if (precision != HQR_PREC_FP64 && !split_precision(precision)) return HQR_ERR_INVALID;
   hqr::Geometry g;
   TRY(hqr::make_geometry(M, N, NB, IB, &g));
-  if (precision == HQR_PREC_OZAKI && !hqr::oz_supported(g)) return HQR_ERR_UNSUPPORTED;
-  if (precision == HQR_PREC_OZAKI) TRY(hqr::narrow_panels(&g));
+  if (split_precision(precision) && !hqr::oz_supported(g)) return HQR_ERR_UNSUPPORTED;
+  if (split_precision(precision)) TRY(hqr::narrow_panels(&g));
   hqr_plan* p = new hqr_plan();
   p->g = g;
   p->precision = precision;
@@ -207,7 +210,8 @@ int hqr_plan_create(hqr_plan_t** plan, long M, long N, int NB, int IB, int preci
     return HQR_ERR_NOMEM;
   }
   cudaMemset(p->dT, 0, (size_t)M * N * sizeof(double));
-  if (precision == HQR_PREC_OZAKI) {
+  if (split_precision(precision)) {
+    p->oz.groups = precision == HQR_PREC_OZAKI_FAST ? 4 : 8;
     if (cudaMalloc(&p->oz.slices, hqr::oz_slice_bytes(g)) != cudaSuccess ||
         cudaMalloc(&p->oz.sexp, hqr::oz_exp_bytes(g)) != cudaSuccess) {
       hqr_plan_destroy(p);
@@ -243,7 +247,7 @@ int hqr_plan_set_tree(hqr_plan_t* plan, int domain_tiles) {
   const size_t nb = (size_t)g.NB;
   bool ok = cudaMalloc(&t.T2, slots * nb * nb * sizeof(double)) == cudaSuccess &&
             cudaMalloc(&t.TAU2, slots * nb * sizeof(double)) == cudaSuccess;
-  if (ok && plan->precision == HQR_PREC_OZAKI)
+  if (ok && split_precision(plan->precision))
     ok = cudaMalloc(&t.slices2, slots * hqr::oz_panel_bytes()) == cudaSuccess &&
          cudaMalloc(&t.sexp2, slots * 3 * nb * sizeof(int)) == cudaSuccess;
   if (!ok) {

@@ -109,6 +109,7 @@ struct DagParams {
   unsigned long long* stats;   // [type][0] = count, [type][1] = SM cycles
   // split precision
   int oz;           // 1: OZPREP/OZAPPLY tasks (NC = NB / 64)
+  int oz_groups;    // t-groups of the split updates (8 or 4; host side: picks the kernel)
   int prep;         // 1: separate OZPREP ids after the panel ids (factorization)
   uint8_t* slices;  // sliced left operands, one block per panel tile
   int* sexp;        // their row exponents (3 * NB ints per panel tile)
@@ -636,7 +637,8 @@ __device__ void task_tbuild(const double* V, const double* tau_g, double* T, boo
 // with its matrix's fields (s_b.lp).  Up to two CTAs per SM (at most 128
 // registers per thread): while one runs a latency-bound panel column loop,
 // the other's update keeps the FP64 pipe busy.
-template <bool OZ, bool BATCH = false>
+// OZG: t-groups of the split updates (8: FP64-level; 4: the reduced form).
+template <bool OZ, bool BATCH = false, int OZG = 8>
 __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagParams p) {
   extern __shared__ __align__(1024) double smem[];
   __shared__ int s_id;
@@ -785,7 +787,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
     if (OZ && oz_bot) {
       oz::Ctx c;
       oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, q.ctl + kErr);
-      task_ozapply(c, oz_slices, oz_exps, oz_top, oz_bot);
+      task_ozapply<OZG>(c, oz_slices, oz_exps, oz_top, oz_bot);
     }
     fence_acq_rel_gpu();   // release: this task's writes before its dependents' counters
     __syncthreads();

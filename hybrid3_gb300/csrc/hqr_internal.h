@@ -63,6 +63,7 @@ void dag_workspace_free(DagWorkspace* ws);
 struct OzWorkspace {
   uint8_t* slices = nullptr;   // sliced V^T, T^T, V of every panel tile
   int* sexp = nullptr;         // their row exponents
+  int groups = 8;              // t-groups of the updates: 8 (FP64-level) or 4 (reduced)
 };
 // Bytes of the split-precision workspace for a geometry (NB = 128).
 size_t oz_slice_bytes(const Geometry& g);

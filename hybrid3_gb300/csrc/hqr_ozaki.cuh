@@ -208,6 +208,28 @@ __device__ __forceinline__ void tmem_ld_groups(uint32_t taddr, uint32_t (&r)[8][
       : "memory");
 }
 
+// The first four t-group accumulators only (the products of weight t <= 3).
+__device__ __forceinline__ void tmem_ld_groups4(uint32_t taddr, uint32_t (&r)[8][8]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%32];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%33];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%16,%17,%18,%19,%20,%21,%22,%23}, [%34];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%24,%25,%26,%27,%28,%29,%30,%31}, [%35];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=&r"(r[0][0]), "=&r"(r[0][1]), "=&r"(r[0][2]), "=&r"(r[0][3]), "=&r"(r[0][4]), "=&r"(r[0][5]),
+        "=&r"(r[0][6]), "=&r"(r[0][7]), "=&r"(r[1][0]), "=&r"(r[1][1]), "=&r"(r[1][2]), "=&r"(r[1][3]),
+        "=&r"(r[1][4]), "=&r"(r[1][5]), "=&r"(r[1][6]), "=&r"(r[1][7]), "=&r"(r[2][0]), "=&r"(r[2][1]),
+        "=&r"(r[2][2]), "=&r"(r[2][3]), "=&r"(r[2][4]), "=&r"(r[2][5]), "=&r"(r[2][6]), "=&r"(r[2][7]),
+        "=&r"(r[3][0]), "=&r"(r[3][1]), "=&r"(r[3][2]), "=&r"(r[3][3]), "=&r"(r[3][4]), "=&r"(r[3][5]),
+        "=&r"(r[3][6]), "=&r"(r[3][7])
+      : "r"(taddr), "r"(taddr + 1 * kN), "r"(taddr + 2 * kN), "r"(taddr + 3 * kN)
+      : "memory");
+#pragma unroll
+  for (int t = 4; t < 8; t++)
+#pragma unroll
+    for (int i = 0; i < 8; i++) r[t][i] = 0u;   // FP32 zero: the dropped groups
+}
+
 // ---------------------------------------------------------------------------
 // Slicing
 // ---------------------------------------------------------------------------
@@ -348,7 +370,8 @@ __device__ __forceinline__ void stage_y(Ctx& c, const double* Y, int ldy, int co
 }
 
 // Slice quad g (column g / 4 of 64, rows k0 + 4 (g % 4) .. +3) of the staged
-// right operand into B stage `s`.
+// right operand into B stage `s` (digit planes 0..G-1).
+template <int G = kGroups>
 __device__ __forceinline__ void slice_b_quad(Ctx& c, uint8_t* stage, int g, int k0) {
   const int col = g >> 2, q = g & 3;
   const int E = c.sEb[c.yb * kN + col];
@@ -362,7 +385,7 @@ __device__ __forceinline__ void slice_b_quad(Ctx& c, uint8_t* stage, int g, int 
   digits(fixed_of(y23.y, E), d[3]);
   const int off = core_off(col, 4 * q);
 #pragma unroll
-  for (int p = 0; p < kS; p++) {
+  for (int p = 0; p < G; p++) {
     uint2 w;
     w.x = bf16x2(d[0][p], d[1][p]);
     w.y = bf16x2(d[2][p], d[3][p]);
@@ -377,18 +400,22 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
 __device__ __forceinline__ bool wait_chunk(const Ctx& c, int base, int stages, int n) {
   return mbar_wait(c.bar + base + n % stages, (uint32_t)((n / stages) & 1), c.err);
 }
+// Chunk `chunk` of X into A stage n: its digit planes 0..G-1 (the first G x 4
+// KiB of the chunk).
+template <int G = kGroups>
 __device__ __forceinline__ void issue_a(Ctx& c, const uint8_t* X, int chunk, int n) {
   uint64_t* b = c.bar + kBarAFull + n % kAStages;
-  mbar_expect_tx(b, kAChunkBytes);
-  tma_load_1d(c.sA + (n % kAStages) * kAChunkBytes, X + (size_t)chunk * kAChunkBytes, kAChunkBytes, b);
+  mbar_expect_tx(b, G * kSliceABytes);
+  tma_load_1d(c.sA + (n % kAStages) * kAChunkBytes, X + (size_t)chunk * kAChunkBytes, G * kSliceABytes, b);
 }
 
 // Issue the bulk copies of the first chunks of the next product's left
 // operand X (thread 0), e.g. before the right operand is staged.
+template <int G = kGroups>
 __device__ __forceinline__ void prefetch(Ctx& c, const uint8_t* X) {
   if (threadIdx.x == 0) {
     fence_proxy_async_global();
-    for (; c.na < c.n + kAStages; c.na++) issue_a(c, X, c.na - c.n, c.na);
+    for (; c.na < c.n + kAStages; c.na++) issue_a<G>(c, X, c.na - c.n, c.na);
   }
 }
 
@@ -397,8 +424,11 @@ __device__ __forceinline__ void prefetch(Ctx& c, const uint8_t* X) {
 // first chunks are fetched as soon as their stages are free.  Warp 0, one
 // thread: bulk copies of A and the MMAs; warps 1..7: slicing of B, up to
 // kBStages chunks ahead of the MMAs.  On return (true) the accumulators are
-// final in TMEM.
+// final in TMEM.  G < 8: only the pairs of weight p + q < G (accumulators
+// 0..G-1; the others are left as they are).
+template <int G = kGroups>
 inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
+  static_assert(G >= 1 && G <= kGroups, "t-groups");
   const int n0 = c.n;
   bool ok = true;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -409,7 +439,7 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
       const uint64_t dB0 = sdesc(smem_u32(c.sB), 128, 256);
       fence_proxy_async_global();
       // chunks of this product not prefetched yet (stages free: every earlier MMA is done)
-      for (; c.na < n0 + kAStages; c.na++) issue_a(c, X, c.na - n0, c.na);
+      for (; c.na < n0 + kAStages; c.na++) issue_a<G>(c, X, c.na - n0, c.na);
       for (int j = 0; j < kChunks && ok; j++) {
         const int n = n0 + j;
         if (!wait_chunk(c, kBarAFull, kAStages, n) || !wait_chunk(c, kBarBFull, kBStages, n)) {
@@ -419,12 +449,12 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
         tc_fence_after();
         const uint64_t dA = dA0 + (uint64_t)(((n % kAStages) * kAChunkBytes) >> 4);
         const uint64_t dB = dB0 + (uint64_t)(((n % kBStages) * kBChunkBytes) >> 4);
-        // pairs (p, q) with p + q <= kGroups - 1 into t-group p + q; the first
+        // pairs (p, q) with p + q <= G - 1 into t-group p + q; the first
         // product into each group in chunk 0 overwrites it
 #pragma unroll
-        for (int p = 0; p < kS; p++) {
+        for (int p = 0; p < kS && p < G; p++) {
 #pragma unroll
-          for (int q = 0; q < kS && p + q < kGroups; q++) {
+          for (int q = 0; q < kS && p + q < G; q++) {
             const int first_p = (p + q) - (kS - 1) > 0 ? (p + q) - (kS - 1) : 0;
             const uint32_t acc = (j > 0 || p > first_p) ? 1u : 0u;
             mma_bf16(c.tmem + (uint32_t)((p + q) * kN), dA + (uint64_t)((p * kSliceABytes) >> 4),
@@ -438,7 +468,7 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
             ok = false;
             break;
           }
-          issue_a(c, X, j + kAStages - 1, n + kAStages - 1);
+          issue_a<G>(c, X, j + kAStages - 1, n + kAStages - 1);
           c.na = n + kAStages;
         }
       }
@@ -449,7 +479,7 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
             ok = false;
             break;
           }
-          issue_a(c, Xnext, j, n0 + kChunks + j);
+          issue_a<G>(c, Xnext, j, n0 + kChunks + j);
         }
         if (ok) c.na = n0 + kChunks + kAStages;
       }
@@ -467,7 +497,7 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
         break;
       }
       uint8_t* stage = c.sB + (n % kBStages) * kBChunkBytes;
-      for (; g < (j + 1) * 256; g += kStride) slice_b_quad(c, stage, g & 255, j * kKC);
+      for (; g < (j + 1) * 256; g += kStride) slice_b_quad<G>(c, stage, g & 255, j * kKC);
       fence_proxy_async();
       __syncwarp();
       if (lane == 0) mbar_arrive(c.bar + kBarBFull + n % kBStages);
@@ -548,9 +578,12 @@ enum Epi : int {
 
 // Recombine the 8 t-group accumulators into FP64 and apply the epilogue.
 // Warp w handles TMEM lanes (rows) 32*(w%4).. and kColsPerWarp columns from
-// kColsPerWarp*(w/4).  Ea: row exponents of X (global).
+// kColsPerWarp*(w/4).  Ea: row exponents of X (global).  G = 4: groups 4..7
+// are taken as zero.
+template <int G = kGroups>
 inline __device__ void drain(Ctx& c, const int* Ea, int mode, double* g, int ldg, double* gm,
                              int ldm) {
+  static_assert(G == 8 || G == 4, "epilogue loads");
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   constexpr int kColsPerWarp = kN / (kWarps / 4);
   static_assert(kColsPerWarp % kDC == 0, "epilogue passes");
@@ -575,7 +608,10 @@ inline __device__ void drain(Ctx& c, const int* Ea, int mode, double* g, int ldg
 #pragma unroll
     for (int i = 0; i < kDC; i++) mem[i] = msrc ? ldg_cg(msrc + row + (size_t)(c0 + i) * mld) : 0.0;
     uint32_t acc[kGroups][kDC];
-    tmem_ld_groups(lane_addr + (uint32_t)c0, acc);
+    if (G == 8)
+      tmem_ld_groups(lane_addr + (uint32_t)c0, acc);
+    else
+      tmem_ld_groups4(lane_addr + (uint32_t)c0, acc);
 #pragma unroll
     for (int i = 0; i < kDC; i++) {
       const int col = c0 + i;
@@ -607,11 +643,14 @@ inline __device__ void drain(Ctx& c, const int* Ea, int mode, double* g, int ldg
 }
 
 // One product: X (prepared, row exponents Ea) times the staged right operand;
-// Xnext: the next product's left operand (prefetched) or nullptr.
+// Xnext: the next product's left operand (prefetched) or nullptr.  G: the
+// t-groups kept (8: every product of weight <= 7, FP64-level; 4: weight <= 3,
+// about 2^-30 of rowmax * colmax * K).
+template <int G = kGroups>
 inline __device__ bool product(Ctx& c, const uint8_t* Xprep, const uint8_t* Xnext, const int* Ea,
                                int mode, double* g, int ldg, double* gm, int ldm) {
-  if (!gemm(c, Xprep, Xnext)) return false;
-  drain(c, Ea, mode, g, ldg, gm, ldm);
+  if (!gemm<G>(c, Xprep, Xnext)) return false;
+  drain<G>(c, Ea, mode, g, ldg, gm, ldm);
   return true;
 }
 

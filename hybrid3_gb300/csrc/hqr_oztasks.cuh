@@ -148,20 +148,22 @@ inline __device__ bool task_ozprep(const double* V, const double* tau, double* G
 
 // One 64-column block of the update.  Ctop: A1 block (SSRFB) or nullptr
 // (LARFB); Cbot: A2 block (SSRFB) or the C block (LARFB); ld NB.  Returns
-// false on a device time-out (error word already set).
+// false on a device time-out (error word already set).  G: t-groups of the
+// three products (8: FP64-level; 4: the reduced form, see oz::product).
+template <int G = oz::kGroups>
 inline __device__ bool task_ozapply(oz::Ctx& c, const uint8_t* slices, const int* exps, double* Ctop,
                                     double* Cbot) {
   using namespace oz;
   constexpr size_t ob = operand_bytes();
-  prefetch(c, slices + kOzVT * ob);
+  prefetch<G>(c, slices + kOzVT * ob);
   stage_y(c, Cbot, kK, -1);
-  if (!product(c, slices + kOzVT * ob, slices + kOzTT * ob, exps + kOzVT * kK, kEpiToY, nullptr, 0, Ctop,
-               kK))
+  if (!product<G>(c, slices + kOzVT * ob, slices + kOzTT * ob, exps + kOzVT * kK, kEpiToY, nullptr, 0, Ctop,
+                  kK))
     return false;
-  if (!product(c, slices + kOzTT * ob, slices + kOzV * ob, exps + kOzTT * kK, kEpiToYSubTop, nullptr, 0,
-               Ctop, kK))
+  if (!product<G>(c, slices + kOzTT * ob, slices + kOzV * ob, exps + kOzTT * kK, kEpiToYSubTop, nullptr, 0,
+                  Ctop, kK))
     return false;
-  if (!product(c, slices + kOzV * ob, nullptr, exps + kOzV * kK, kEpiSubInto, Cbot, kK, nullptr, 0))
+  if (!product<G>(c, slices + kOzV * ob, nullptr, exps + kOzV * kK, kEpiSubInto, Cbot, kK, nullptr, 0))
     return false;
   ctx_release(c);
   return true;

@@ -34,6 +34,11 @@ extern "C" {
 #define HQR_PREC_FP64 0    /* FP64 on CUDA cores */
 #define HQR_PREC_OZAKI 1   /* split-precision slices on the tensor cores, FP64 recombination;
                               NB = 128 only (HQR_ERR_UNSUPPORTED otherwise) */
+#define HQR_PREC_OZAKI_FAST 2 /* the same updates with only the slice products of weight <= 3
+                              (10 of 36): each product to about 2^-30 of its operands' row and
+                              column maxima, an FP32-class factorization for least squares with
+                              FP64 iterative refinement (hqr_lstsq, refine_steps >= 2); FP64
+                              panels, NB = 128 only */
 
 /* Error behaviour of the drop-in (Hybrid_*, tile_*) entry points. */
 #define HQR_ERRORS_ABORT 0   /* print to stderr and exit(1) (the reference's MPI_Abort) */
@@ -57,7 +62,8 @@ const char *hqr_status_string(int status);
 void hqr_set_error_mode(int mode);
 /* Arithmetic of the trailing updates used by the drop-in entry points
  * (default: HQR_PREC_FP64, or HQR_PREC_OZAKI when the environment variable
- * HQR_PRECISION is "ozaki" or "split" at first use). */
+ * HQR_PRECISION is "ozaki" or "split" at first use, HQR_PREC_OZAKI_FAST when
+ * it is "fast"). */
 void hqr_set_default_precision(int precision);
 int hqr_get_default_precision(void);
 int hqr_last_error(void);
