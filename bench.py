@@ -565,7 +565,7 @@ def run_batched(H, torch, L, args):
     nb_use = {f"{k[0]}/{k[1]}": v for k, v in sorted(Counter(pick).items())}
     stream = torch.cuda.Stream()
     s = stream.cuda_stream
-    d = AT.BatchData(H, torch, m, n, nb, ib, nrhs, 20151130, stream)
+    d = AT.BatchData(H, torch, m, n, nb, ib, nrhs, 20151130)
     bt = d.batch(H, table["ctas"])
     ev = lambda: torch.cuda.Event(enable_timing=True)
 
@@ -640,10 +640,21 @@ def run_batched(H, torch, L, args):
         acc["lstsq_rel_max"] = max(acc["lstsq_rel_max"], float(np.linalg.norm(x - xr) / np.linalg.norm(xr)))
         acc["sample"] += 1
 
-    # end to end: pinned host arrays in, R + reflectors, TAU and Q^T C out
+    # end to end: pinned host arrays in, R + reflectors, TAU and Q^T C out.
+    # The matrices are cut into P groups of about equal work, each its own
+    # batch: group g + 1's inputs are copied in and group g - 1's results out
+    # while group g is factored (one stream per direction).
+    bt.close()
     e2e = None
     if args.e2e_steps is None or args.e2e_steps > 0:
         ks = args.e2e_steps if args.e2e_steps is not None else args.steps
+        P = max(1, min(args.batch_groups, count))
+        work = np.cumsum([AT.padded_flops(a, b, k, nrhs) for a, b, k in zip(m, n, nb)])
+        cuts = [0] + [int(np.searchsorted(work, work[-1] * (g + 1) / P)) + 1 for g in range(P - 1)] + [count]
+        cuts = sorted(set(min(max(c, 0), count) for c in cuts))
+        groups = [(cuts[i], cuts[i + 1]) for i in range(len(cuts) - 1) if cuts[i + 1] > cuts[i]]
+        bts = [H.Batch(d.Mp[g0:g1], d.Np[g0:g1], nb[g0:g1], ib[g0:g1], max_nrhs=nrhs, ctas_per_sm=table["ctas"])
+               for g0, g1 in groups]
         hA0 = torch.empty(d.A0.numel(), dtype=f64).pin_memory()
         hC0 = torch.empty(d.C0.numel(), dtype=f64).pin_memory()
         hA0.copy_(d.A0.cpu())
@@ -651,27 +662,44 @@ def run_batched(H, torch, L, args):
         hA = torch.empty_like(hA0).pin_memory()
         hC = torch.empty_like(hC0).pin_memory()
         hT = torch.empty(d.TAU.numel(), dtype=f64).pin_memory()
+        s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+        ev_in = [torch.cuda.Event() for _ in groups]
+        ev_out = [torch.cuda.Event() for _ in groups]
+        rng = lambda o, g0, g1: slice(int(o[g0]), int(o[g1]))
         times = []
         for it in range(1 + ks):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            with torch.cuda.stream(stream):
-                d.A.copy_(hA0, non_blocking=True)
-                d.C.copy_(hC0, non_blocking=True)
-            bt.geqrf(d.pa, d.pt, stream=s, wait=False)
-            bt.ormqr_t(d.pa, d.pt, d.pc, nrhs, stream=s, wait=False)
-            with torch.cuda.stream(stream):
-                hA.copy_(d.A, non_blocking=True)
-                hT.copy_(d.TAU, non_blocking=True)
-                hC.copy_(d.C, non_blocking=True)
-            bt.status(s)
+            with torch.cuda.stream(s_in):
+                for gi, (g0, g1) in enumerate(groups):
+                    a, c = rng(d.a_off, g0, g1), rng(d.c_off, g0, g1)
+                    d.A[a].copy_(hA0[a], non_blocking=True)
+                    d.C[c].copy_(hC0[c], non_blocking=True)
+                    ev_in[gi].record(s_in)
+            for gi, (g0, g1) in enumerate(groups):
+                stream.wait_event(ev_in[gi])
+                bts[gi].geqrf(d.pa[g0:g1], d.pt[g0:g1], stream=s, wait=False)
+                bts[gi].ormqr_t(d.pa[g0:g1], d.pt[g0:g1], d.pc[g0:g1], nrhs, stream=s, wait=False)
+                ev_out[gi].record(stream)
+                with torch.cuda.stream(s_out):
+                    s_out.wait_event(ev_out[gi])
+                    a, c, t = rng(d.a_off, g0, g1), rng(d.c_off, g0, g1), rng(d.t_off, g0, g1)
+                    hA[a].copy_(d.A[a], non_blocking=True)
+                    hT[t].copy_(d.TAU[t], non_blocking=True)
+                    hC[c].copy_(d.C[c], non_blocking=True)
+            torch.cuda.synchronize()
+            for b_ in bts:
+                b_.status(s)
             if it > 0:
                 times.append(time.perf_counter() - t0)
         e2e = {"value": round(d.flops / float(np.mean(times)) / 1e12, 6), "unit": "TFLOP/s",
                "h2d_bytes_per_step": 8 * (d.A0.numel() + d.C0.numel()),
                "d2h_bytes_per_step": 8 * (d.A0.numel() + d.TAU.numel() + d.C0.numel()),
-               "steps": ks, "warmup": 1,
-               "api": "hqr_batch_geqrf_async + hqr_batch_ormqr_t_async, pinned host arrays"}
+               "steps": ks, "warmup": 1, "groups": len(groups),
+               "api": "hqr_batch_geqrf_async + hqr_batch_ormqr_t_async per group, pinned host arrays, "
+                      "copies of the next / previous group overlapped on two copy streams"}
+        for b_ in bts:
+            b_.close()
         del hA0, hC0, hA, hC, hT
 
     cpu = None
@@ -709,7 +737,6 @@ def run_batched(H, torch, L, args):
         "gpu_launches": 2 * 3 * args.steps,
         "clocks": clk,
     }
-    bt.close()
     print(json.dumps(line), flush=True)
 
 
@@ -744,6 +771,8 @@ def main():
     ap.add_argument("--batch", type=int, default=4096, help="matrices in the --batched workload")
     ap.add_argument("--batch-nrhs", type=int, default=4, help="right-hand sides per matrix for --batched")
     ap.add_argument("--batch-nb", default=None, help="fixed NB/IB for --batched (default: autotuned)")
+    ap.add_argument("--batch-groups", type=int, default=4,
+                    help="batches the --batched end-to-end run is cut into (copies overlap compute)")
     ap.add_argument("--batch-ctas", type=int, default=0,
                     help="executor CTAs per SM (1 or 2) for --batched with --batch-nb")
     ap.add_argument("--tree", type=int, default=0,

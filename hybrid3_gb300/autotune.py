@@ -49,7 +49,7 @@ class BatchData:
     ceil(m/NB) x ceil(n/NB) tiles of NB), TAU, right-hand sides (ceil(m/NB)
     x ceil(nrhs/NB) tiles), with pristine copies of A and C, contiguous."""
 
-    def __init__(self, H, torch, m, n, nb, ib, nrhs: int, seed: int, stream=None):
+    def __init__(self, H, torch, m, n, nb, ib, nrhs: int, seed: int):
         f64 = torch.float64
         self.m, self.n, self.nb, self.ib, self.nrhs = list(m), list(n), list(nb), list(ib), nrhs
         cnt = len(self.m)
@@ -66,7 +66,10 @@ class BatchData:
         self.C0 = torch.zeros(int(self.c_off[-1]), dtype=f64, device="cuda")
         self.C = torch.empty_like(self.C0)
         L = H.lib()
-        s = stream.cuda_stream if stream is not None else None
+        # the conversions run on torch's current stream: the generated
+        # temporaries are freed to torch's allocator on that stream, so a
+        # conversion on another stream could read reused memory
+        s = torch.cuda.current_stream().cuda_stream
         g = torch.Generator(device="cuda")
         for b in range(cnt):
             # entries uniform[-1, 1), seeded per matrix; column-major m x n and m x nrhs
@@ -121,7 +124,7 @@ def tune_batch(H, torch, m, n, nrhs: int, candidates=CANDIDATES, sample_flops: f
         sm, sn = m[take].tolist(), n[take].tolist()
         rates = {1: {}, 2: {}}
         for nb, ib in candidates:
-            d = BatchData(H, torch, sm, sn, [nb] * len(sm), [ib] * len(sm), nrhs, 1000 + c, stream)
+            d = BatchData(H, torch, sm, sn, [nb] * len(sm), [ib] * len(sm), nrhs, 1000 + c)
             pf = sum(padded_flops(a, b, nb, nrhs) for a, b in zip(sm, sn))
             for ctas in (1, 2):
                 try:

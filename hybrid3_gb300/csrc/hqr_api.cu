@@ -605,6 +605,9 @@ struct hqr_batch {
   int count = 0;
   std::vector<hqr::Geometry> g;
   std::vector<double*> T;    // per matrix, into dT
+  // table order: the largest factorizations (longest task chains) first, so
+  // that their first tasks are queued first and the launch ends with small ones
+  std::vector<int> order;
   double* dT = nullptr;
   hqr::DagWorkspace ws;
   size_t smem = 0;
@@ -639,8 +642,8 @@ int batch_table(hqr_batch* b, bool apply, double* const* dA, double* const* dTAU
   const size_t bytes = (size_t)b->count * hqr::mat_desc_bytes();
   std::vector<unsigned char> desc(bytes);
   int n_ids = 0, n_tasks = 0;
-  TRY(hqr::batch_describe(apply, b->count, b->g.data(), dA, b->T.data(), dTAU, dC, nrhs, desc.data(), &n_ids,
-                          &n_tasks));
+  TRY(hqr::batch_describe(apply, b->count, b->g.data(), b->order.data(), dA, b->T.data(), dTAU, dC, nrhs,
+                          desc.data(), &n_ids, &n_tasks));
   if (t.valid && t.nrhs == nrhs && desc == t.host) return HQR_OK;   // the device copy is current
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   TRY(cuda_rc(cudaStreamIsCapturing(s, &cs)));
@@ -714,6 +717,13 @@ int hqr_batch_create(hqr_batch_t** batch, int count, const long* M, const long* 
     free_batch(b);
     return rc;
   }
+  b->order.resize(count);
+  for (int i = 0; i < count; i++) b->order[i] = i;
+  auto work = [&](int i) {
+    const hqr::Geometry& g = b->g[i];
+    return (double)g.M * g.N * g.N - (double)g.N * g.N * g.N / 3.0;
+  };
+  std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) { return work(x) > work(y); });
   b->T.resize(count);
   size_t off = 0;
   for (int i = 0; i < count; i++) {

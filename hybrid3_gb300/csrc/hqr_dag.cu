@@ -323,11 +323,13 @@ long long batch_ids(bool apply, const Geometry& g, int nrhs) {
   return id_end(batch_matrix_params(apply, g, nrhs));
 }
 
-int batch_describe(bool apply, int count, const Geometry* gs, double* const* A, double* const* T,
-                   double* const* TAU, double* const* C, int nrhs, void* desc, int* n_ids, int* n_tasks) {
+int batch_describe(bool apply, int count, const Geometry* gs, const int* order, double* const* A,
+                   double* const* T, double* const* TAU, double* const* C, int nrhs, void* desc, int* n_ids,
+                   int* n_tasks) {
   MatDesc* d = static_cast<MatDesc*>(desc);
   long long ids = 0, tasks = 0;
-  for (int b = 0; b < count; b++) {
+  for (int i = 0; i < count; i++) {
+    const int b = order ? order[i] : i;
     const DagParams p = batch_matrix_params(apply, gs[b], nrhs);
     MatDesc m{};
     m.MT = p.MT;
@@ -348,7 +350,7 @@ int batch_describe(bool apply, int count, const Geometry* gs, double* const* A, 
     tasks += batch_matrix_tasks(apply, p);
     if (ids > 0x3fffffffLL) return HQR_ERR_UNSUPPORTED;
     m.id_end = (int)ids;
-    d[b] = m;
+    d[i] = m;
   }
   *n_ids = (int)ids;
   *n_tasks = (int)tasks;

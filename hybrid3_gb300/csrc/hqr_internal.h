@@ -110,8 +110,11 @@ int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double
 size_t mat_desc_bytes();
 // apply: C <- Q^T C on the first nrhs columns of each C (else the factorization).
 long long batch_ids(bool apply, const Geometry& g, int nrhs);
-int batch_describe(bool apply, int count, const Geometry* gs, double* const* A, double* const* T,
-                   double* const* TAU, double* const* C, int nrhs, void* desc, int* n_ids, int* n_tasks);
+// order (or null): the matrices in the order of the table (and of the first
+// tasks queued: the init and seed kernels run one block per table entry).
+int batch_describe(bool apply, int count, const Geometry* gs, const int* order, double* const* A,
+                   double* const* T, double* const* TAU, double* const* C, int nrhs, void* desc, int* n_ids,
+                   int* n_tasks);
 // Dynamic shared memory per executor CTA that lets two CTAs share an SM.
 size_t batch_two_cta_smem();
 // ctas_per_sm: executor CTAs per SM (0: as many as fit, at most 2).
