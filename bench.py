@@ -354,9 +354,12 @@ def measure(H, torch, L, args, precision: str, n: int, NB: int, IB: int, steps: 
             "stats_mq": stats_mq, "flops": step_flops(M, N) * steps * world}
 
 
-def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: int, dist, world: int):
+def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: int, dist, world: int,
+                sample_clocks: bool = False):
     """The same workload through the drop-in C entry points with pinned host arrays:
-    Hybrid_tile_QR then Hybrid_make_Q, host<->device copies inside the timed region."""
+    Hybrid_tile_QR then Hybrid_make_Q, host<->device copies inside the timed region.
+    This region is timed on the host, so by default nvidia-smi does not poll
+    during it (sample_clocks: it does, as during the device-timed region)."""
     M = N = n
     L.hqr_set_default_precision(prec_code(H, precision))
     f64 = torch.float64
@@ -375,9 +378,9 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
     pq = ctypes.cast(hQ.data_ptr(), DP)
     pt = ctypes.cast(hTAU.data_ptr(), DP)
     times, t_qr, t_mq = [], [], []
-    clocks = ClockSampler(torch.cuda.current_device())
+    clocks = ClockSampler(torch.cuda.current_device()) if sample_clocks else None
     for it in range(1 + steps):
-        if it == 1:
+        if it == 1 and clocks:
             clocks.start()
         hA.copy_(hA0)
         hQ.zero_()
@@ -392,7 +395,7 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
             times.append(t2 - t0)
             t_qr.append(t1 - t0)
             t_mq.append(t2 - t1)
-    clk = clocks.stop()
+    clk = clocks.stop() if clocks else "not sampled (host-timed region)"
     L.hqr_set_default_precision(H.HQR_PREC_FP64)
     t_e2e = sum(times)
     if dist:
@@ -755,6 +758,8 @@ def main():
     ap.add_argument("--cpu-n", type=int, default=4096, help="CPU sample order")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--e2e-clocks", action="store_true",
+                    help="poll nvidia-smi during the host-timed end-to-end region too")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--kappa", type=float, default=None,
                     help="graded input A = U diag(sigma) V^T with condition number kappa "
@@ -832,7 +837,7 @@ def main():
     e2e = None
     e2e_steps = args.e2e_steps if args.e2e_steps is not None else args.steps
     if e2e_steps > 0 and rows is None:
-        e2e = measure_e2e(H, torch, L, args.precision, n, NB, IB, e2e_steps, dist, world)
+        e2e = measure_e2e(H, torch, L, args.precision, n, NB, IB, e2e_steps, dist, world, args.e2e_clocks)
 
     compare = None
     if args.precision in ("split", "fast") and not args.no_compare:
