@@ -48,6 +48,24 @@ def prec_code(H, precision: str) -> int:
     return {"split": H.HQR_PREC_OZAKI, "fast": H.HQR_PREC_OZAKI_FAST}.get(precision, H.HQR_PREC_FP64)
 
 
+def max_over_ranks(x: float, dist, device: str = "cuda") -> float:
+    """The largest x over the ranks (x itself without a process group): the
+    job's time is that of its slowest replica."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: float, seconds: float, dist, device: str = "cuda") -> float:
+    """Whole-job throughput of independent replicas: every rank's units over
+    the slowest rank's time."""
+    world = dist.get_world_size() if dist else 1
+    return world * units_per_rank / max_over_ranks(seconds, dist, device)
+
+
 def qr_flops(m: int, n: int) -> float:
     return 2.0 * m * n * n - 2.0 * n ** 3 / 3.0
 
@@ -303,11 +321,7 @@ def measure(H, torch, L, args, precision: str, n: int, NB: int, IB: int, steps: 
         dist.barrier()
     clk = clocks.stop() if clocks else None
     H.check(L.hqr_plan_status(plan.h, s), "timed run")
-    elapsed = t_start.elapsed_time(t_end) / 1e3
-    if dist:
-        t = torch.tensor([elapsed], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(t_start.elapsed_time(t_end) / 1e3, dist)
     fact_s = [r[0].elapsed_time(r[1]) / 1e3 for r in recs]
     mq_s = [r[2].elapsed_time(r[3]) / 1e3 for r in recs]
     stats_mq = plan.stats(s)
@@ -397,14 +411,10 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
             t_mq.append(t2 - t1)
     clk = clocks.stop() if clocks else "not sampled (host-timed region)"
     L.hqr_set_default_precision(H.HQR_PREC_FP64)
-    t_e2e = sum(times)
-    if dist:
-        t = torch.tensor([t_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    rate = job_rate(steps * step_flops(M, N), sum(times), dist)
     nbytes = M * N * 8
     tau_b = (M // NB) * (N // NB) * NB * 8
-    return {"value": round(world * steps * step_flops(M, N) / t_e2e / 1e12, 6), "unit": "TFLOP/s",
+    return {"value": round(rate / 1e12, 6), "unit": "TFLOP/s",
             # Hybrid_tile_QR: A, TAU in and out; Hybrid_make_Q: Q, RY, TAU in, Q, RY out
             "h2d_bytes_per_step": nbytes + tau_b + 2 * nbytes + tau_b,
             "d2h_bytes_per_step": nbytes + tau_b + 2 * nbytes,
