@@ -415,8 +415,9 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
     nbytes = M * N * 8
     tau_b = (M // NB) * (N // NB) * NB * 8
     return {"value": round(rate / 1e12, 6), "unit": "TFLOP/s",
-            # Hybrid_tile_QR: A, TAU in and out; Hybrid_make_Q: Q, RY, TAU in, Q, RY out
-            "h2d_bytes_per_step": nbytes + tau_b + 2 * nbytes + tau_b,
+            # Hybrid_tile_QR: A, TAU in and out; Hybrid_make_Q: RY, TAU in (a square
+            # Q is written whole on the device, not copied in), Q, RY out
+            "h2d_bytes_per_step": 2 * nbytes + 2 * tau_b,
             "d2h_bytes_per_step": nbytes + tau_b + 2 * nbytes,
             "steps": steps, "warmup": 1, "precision": precision,
             "phases_ms": {"Hybrid_tile_QR": round(1e3 * float(np.mean(t_qr)), 3),
