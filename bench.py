@@ -890,7 +890,9 @@ def main():
                                    "MEASURED_PEAKS.json holds no FP64 figure",
                     "traffic": load_traffic(n, NB, "fp64"),
                     "algorithmic_flops_per_launch": qr_flops(M, n)}
-    launches_per_step = 3 + 5
+    # this library's kernels per step: factorization (init, seed, executor);
+    # make_Q (identity, init, seed, executor, tile transpose, zero reflectors)
+    launches_per_step = 3 + 6
     line = {
         "metric": METRIC, "value": round(value, 6), "unit": "TFLOP/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup,
