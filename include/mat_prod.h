@@ -28,7 +28,10 @@ typedef struct mstatus {
     unsigned int my_tile_N;      /* tile columns held by this rank */
 } mat_stat_t;
 
-/* mat_init (mat_prod.c:15-37): M and N are truncated to multiples of NB. */
+/* mat_init (mat_prod.c:15-37): tile counts mat / tile (truncating); rank
+ * my_rank of proc_num holds every tile row and tile columns g with
+ * g % proc_num == my_rank, so my_mat_N = tile_n * (its tile columns) while
+ * my_mat_M = mat_m as given, as in the reference. */
 void mat_init(mat_stat_t *status, long int mat_m, long int mat_n, int tile_m, int tile_n,
               int my_rank, int proc_num);
 
