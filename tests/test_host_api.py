@@ -105,3 +105,61 @@ def test_mat_comp3_is_the_one_norm_and_propagates_nan(H):
     assert got == pytest.approx(np.abs(E.reshape(128, 256)).sum(axis=1).max(), rel=1e-14)
     E[300] = np.nan
     assert math.isnan(H.lib().mat_comp3(ctypes.byref(st), E.ctypes.data_as(P), 0, 1))
+
+
+def test_mat_dprint_is_tile_to_column_major(H):
+    import oracle as O
+    M, N, NB = 192, 128, 64
+    st = H.status(M, N, NB)
+    A2d = np.arange(M * N, dtype=np.float64).reshape(N, M).T   # column-major values 0..
+    T = np.ascontiguousarray(O.to_tiles(A2d, NB))
+    out = np.zeros(M * N)
+    P = ctypes.POINTER(ctypes.c_double)
+    H.lib().mat_dprint(ctypes.byref(st), out.ctypes.data_as(P), T.ctypes.data_as(P))
+    assert np.array_equal(out, np.arange(M * N, dtype=np.float64))
+
+
+def test_mat_remv_undoes_mat_make(H):
+    st = H.status(128, 128, 32)
+    A = np.zeros(128 * 128)
+    P = ctypes.POINTER(ctypes.c_double)
+    H.lib().mat_make(ctypes.byref(st), A.ctypes.data_as(P), 77, 0)
+    assert A.min() >= 0.0 and A.max() <= 1.0 and A.std() > 0.2
+    H.lib().mat_remv(ctypes.byref(st), A.ctypes.data_as(P), 77, 0)
+    assert np.abs(A).max() == 0.0
+
+
+def test_status_strings(H):
+    L = H.lib()
+    codes = [H.HQR_OK, H.HQR_ERR_INVALID, H.HQR_ERR_CUDA, H.HQR_ERR_TIMEOUT, H.HQR_ERR_NOMEM,
+             H.HQR_ERR_UNSUPPORTED, H.HQR_ERR_DEVICE]
+    texts = [L.hqr_status_string(c).decode() for c in codes]
+    assert all(texts) and len(set(texts)) == len(texts)
+
+
+def test_drop_in_rejects_bad_status_before_any_device_work(H):
+    """The drop-in entry points validate mat_stat_t first (one rank, square
+    tiles, whole tiles), so these calls never reach the device."""
+    L = H.lib()
+    L.hqr_set_error_mode(H.HQR_ERRORS_RETURN)
+    P = ctypes.POINTER(ctypes.c_double)
+    A = np.zeros(256 * 256)
+    tau = np.zeros(128 * 128)
+    bad = []
+    st = H.MatStat()
+    L.mat_init(ctypes.byref(st), 256, 256, 128, 128, 0, 2)      # two ranks
+    bad.append((st, 0, 2))
+    st = H.MatStat()
+    L.mat_init(ctypes.byref(st), 256, 256, 128, 64, 0, 1)       # non-square tiles
+    bad.append((st, 0, 1))
+    st = H.MatStat()
+    L.mat_init(ctypes.byref(st), 250, 256, 128, 128, 0, 1)      # rows not whole tiles
+    bad.append((st, 0, 1))
+    for st, rank, procs in bad:
+        L.Hybrid_tile_QR(ctypes.byref(st), A.ctypes.data_as(P), tau.ctypes.data_as(P), rank, procs, 32)
+        assert L.hqr_last_error() == H.HQR_ERR_INVALID
+        L.Hybrid_make_Q(ctypes.byref(st), A.ctypes.data_as(P), A.ctypes.data_as(P), tau.ctypes.data_as(P),
+                        rank, procs, 32)
+        assert L.hqr_last_error() == H.HQR_ERR_INVALID
+    L.Hybrid_tile_QR(None, A.ctypes.data_as(P), tau.ctypes.data_as(P), 0, 1, 32)
+    assert L.hqr_last_error() == H.HQR_ERR_INVALID
