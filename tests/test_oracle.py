@@ -235,7 +235,8 @@ def _flat_tree_scipy(A2d, NB, IB):
     return np.block(A)
 
 
-@pytest.mark.parametrize("M,N,NB,IB", [(192, 64, 32, 8), (256, 128, 64, 16), (96, 96, 32, 32)])
+@pytest.mark.parametrize("M,N,NB,IB", [(192, 64, 32, 8), (256, 128, 64, 16), (96, 96, 32, 32),
+                                       (288, 192, 96, 32), (192, 96, 96, 16), (384, 192, 192, 32)])
 def test_tall_and_square_flat_tree_against_lapack(M, N, NB, IB):
     A = O.uniform_matrix(M, N, 11)
     ref = _flat_tree_scipy(A, NB, IB)
