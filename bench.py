@@ -580,8 +580,12 @@ def run_batched(H, torch, L, args):
     if args.batch_nb:
         nb_ib = tuple(int(x) for x in args.batch_nb.split("/"))
         table = AT.fixed_table(nb_ib[0], nb_ib[1], args.batch_ctas or 1)
+    elif args.batch_tune_file and os.path.exists(args.batch_tune_file):
+        table = AT.load(args.batch_tune_file)
     else:
         table = AT.tune_batch(H, torch, m, n, nrhs)
+        if args.batch_tune_file:
+            AT.save(table, args.batch_tune_file)
     tune_s = time.perf_counter() - t0
     pick = [AT.choose(table, a, b, nrhs) for a, b in zip(m, n)]
     nb = [p[0] for p in pick]
@@ -799,6 +803,8 @@ def main():
     ap.add_argument("--batch", type=int, default=4096, help="matrices in the --batched workload")
     ap.add_argument("--batch-nrhs", type=int, default=4, help="right-hand sides per matrix for --batched")
     ap.add_argument("--batch-nb", default=None, help="fixed NB/IB for --batched (default: autotuned)")
+    ap.add_argument("--batch-tune-file", default=None,
+                    help="autotuner table for --batched: read if it exists, else measured and written")
     ap.add_argument("--batch-groups", type=int, default=4,
                     help="batches the --batched end-to-end run is cut into (copies overlap compute)")
     ap.add_argument("--batch-ctas", type=int, default=0,

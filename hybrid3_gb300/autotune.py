@@ -182,6 +182,31 @@ def choose(table, m: int, n: int, nrhs: int):
     return _best(table, m, n, nrhs)[0]
 
 
+def save(table, path: str) -> None:
+    """Write a tune_batch table as JSON (to reuse it for the same shapes and
+    device without measuring again)."""
+    import json
+    enc = {"ctas": table["ctas"],
+           "classes": {str(c): {"n_range": e["n_range"], "sample": e["sample"],
+                                "rates": {str(k): [[nb, ib, r] for (nb, ib), r in rs.items()]
+                                          for k, rs in e["rates"].items()}}
+                       for c, e in table["classes"].items()}}
+    with open(path, "w") as f:
+        json.dump(enc, f, indent=1)
+
+
+def load(path: str):
+    """A table written by save()."""
+    import json
+    with open(path) as f:
+        enc = json.load(f)
+    return {"ctas": int(enc["ctas"]),
+            "classes": {int(c): {"n_range": e["n_range"], "sample": e["sample"],
+                                 "rates": {int(k): {(int(nb), int(ib)): float(r) for nb, ib, r in rs}
+                                           for k, rs in e["rates"].items()}}
+                        for c, e in enc["classes"].items()}}
+
+
 def describe(table):
     """A JSON-able summary of a tune_batch table."""
     return {"ctas_per_sm": table["ctas"],

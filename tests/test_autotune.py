@@ -77,3 +77,13 @@ def test_batched_workload_shapes():
     assert m.min() == 64 and m.max() == 2048 and n.min() == 32
     m2, n2 = bench.batch_shapes(4096, 20151130)
     assert np.array_equal(m, m2) and np.array_equal(n, n2)
+
+
+def test_table_save_and_load_round_trip(tmp_path):
+    t = table({(96, 16): 0.5, (128, 32): 0.6}, {(128, 16): 0.9}, ctas=2)
+    path = tmp_path / "tune.json"
+    AT.save(t, str(path))
+    u = AT.load(str(path))
+    assert u == t
+    for m, n in ((192, 192), (2048, 1024), (64, 32)):
+        assert AT.choose(u, m, n, 4) == AT.choose(t, m, n, 4)
