@@ -566,6 +566,44 @@ def batch_cpu_sample(m, n, nrhs: int, threads: int, budget_s: float = 15.0):
     return flops / (time.perf_counter() - t_start), done
 
 
+def run_batched_reference(args, rank: int):
+    """The reference arm of the batched workload: the reference's algorithm
+    (the oracle's restatement of Hybrid_tile_QR + Hybrid_dormqr) on the
+    host cores, one matrix per thread, each step a bounded sample (about 10 s)
+    of the same shapes.  The reference has no batched mode; this is what
+    running its CPU path over the matrices would do."""
+    if rank != 0:
+        return
+    thr = os.cpu_count() or 1
+    m, n = batch_shapes(args.batch, 20151130)
+    for _ in range(min(args.warmup, 1)):
+        batch_cpu_sample(m, n, args.batch_nrhs, thr, 2.0)
+    rates, done, walls = [], 0, []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r, k = batch_cpu_sample(m, n, args.batch_nrhs, thr, 10.0)
+        walls.append(time.perf_counter() - t0)
+        rates.append(r)
+        done += k
+    value = float(np.mean(rates)) / 1e12
+    line = {
+        "impl": "reference", "metric": BATCH_METRIC, "value": round(value, 6), "unit": "TFLOP/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * float(np.mean(walls)), 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.batch} independent FP64 matrices (m uniform in {{64..2048}} step 32, "
+                               f"n uniform in {{32..m}} step 32), factorization + dormqr on "
+                               f"{args.batch_nrhs} right-hand sides; bounded samples of these shapes",
+                   "count": args.batch, "nrhs": args.batch_nrhs},
+        "cpu_baseline": {"value": round(value, 6), "unit": "TFLOP/s", "cores": thr, "kind": "port",
+                         "sample": f"{done} matrices over {args.steps} steps of about 10 s"},
+        "e2e": {"value": round(value, 6), "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_batched(H, torch, L, args):
     """4096 independent FP64 QRs of uneven shapes plus dormqr on nrhs
     right-hand sides each, every step two persistent launches over all the
@@ -822,7 +860,10 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
 
     if args.impl == "reference":
-        run_reference(args, rank)
+        if args.batched:
+            run_batched_reference(args, rank)
+        else:
+            run_reference(args, rank)
         return
 
     import torch
