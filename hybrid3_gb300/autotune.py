@@ -44,6 +44,21 @@ def ormqr_flops(m: int, n: int, nrhs: int) -> float:
     return 2.0 * nrhs * n * (2.0 * m - n)
 
 
+def layout(m, n, nb, nrhs: int):
+    """Padded shapes and element offsets of a batch stored contiguously:
+    matrix b is Mp[b] x Np[b] (m, n rounded up to nb[b]) at a_off[b], its TAU
+    (MT * NT * NB) at t_off[b] and its right-hand sides (Mp[b] x
+    ceil(nrhs / NB) * NB) at c_off[b]; each offset array has one more entry,
+    the total."""
+    Mp = [padded(a, b) for a, b in zip(m, nb)]
+    Np = [padded(a, b) for a, b in zip(n, nb)]
+    a_len = [mp * np_ for mp, np_ in zip(Mp, Np)]
+    t_len = [(mp // b) * (np_ // b) * b for mp, np_, b in zip(Mp, Np, nb)]
+    c_len = [mp * padded(nrhs, b) for mp, b in zip(Mp, nb)]
+    off = lambda L: np.concatenate([[0], np.cumsum(L)]).astype(np.int64)
+    return Mp, Np, off(a_len), off(t_len), off(c_len)
+
+
 class BatchData:
     """Device buffers of one batch: matrices (zero-padded tile layout, each
     ceil(m/NB) x ceil(n/NB) tiles of NB), TAU, right-hand sides (ceil(m/NB)
@@ -53,13 +68,7 @@ class BatchData:
         f64 = torch.float64
         self.m, self.n, self.nb, self.ib, self.nrhs = list(m), list(n), list(nb), list(ib), nrhs
         cnt = len(self.m)
-        self.Mp = [padded(a, b) for a, b in zip(self.m, self.nb)]
-        self.Np = [padded(a, b) for a, b in zip(self.n, self.nb)]
-        a_len = [mp * np_ for mp, np_ in zip(self.Mp, self.Np)]
-        t_len = [(mp // b) * (np_ // b) * b for mp, np_, b in zip(self.Mp, self.Np, self.nb)]
-        c_len = [mp * padded(nrhs, b) for mp, b in zip(self.Mp, self.nb)]
-        off = lambda L: np.concatenate([[0], np.cumsum(L)]).astype(np.int64)
-        self.a_off, self.t_off, self.c_off = off(a_len), off(t_len), off(c_len)
+        self.Mp, self.Np, self.a_off, self.t_off, self.c_off = layout(self.m, self.n, self.nb, nrhs)
         self.A0 = torch.zeros(int(self.a_off[-1]), dtype=f64, device="cuda")
         self.A = torch.empty_like(self.A0)
         self.TAU = torch.zeros(int(self.t_off[-1]), dtype=f64, device="cuda")

@@ -87,3 +87,15 @@ def test_table_save_and_load_round_trip(tmp_path):
     assert u == t
     for m, n in ((192, 192), (2048, 1024), (64, 32)):
         assert AT.choose(u, m, n, 4) == AT.choose(t, m, n, 4)
+
+
+def test_batch_layout():
+    m, n, nb = [96, 64, 2048], [32, 64, 1000], [64, 32, 128]
+    Mp, Np, a_off, t_off, c_off = AT.layout(m, n, nb, 4)
+    assert Mp == [128, 64, 2048] and Np == [64, 64, 1024]
+    assert list(a_off) == [0, 128 * 64, 128 * 64 + 64 * 64, 128 * 64 + 64 * 64 + 2048 * 1024]
+    assert list(t_off) == [0, 2 * 1 * 64, 128 + 2 * 2 * 32, 128 + 128 + 16 * 8 * 128]
+    # 4 right-hand sides take one tile column of NB
+    assert list(c_off) == [0, 128 * 64, 128 * 64 + 64 * 32, 128 * 64 + 64 * 32 + 2048 * 128]
+    # every offset is a whole number of 8-byte elements, tiles start on 16-byte boundaries
+    assert all(int(x) % 2 == 0 for x in a_off)
