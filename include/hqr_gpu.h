@@ -36,9 +36,10 @@ extern "C" {
                               NB = 128 only (HQR_ERR_UNSUPPORTED otherwise) */
 #define HQR_PREC_OZAKI_FAST 2 /* the same updates with only the slice products of weight <= 3
                               (10 of 36): each product to about 2^-30 of its operands' row and
-                              column maxima, an FP32-class factorization for least squares with
-                              FP64 iterative refinement (hqr_lstsq, refine_steps >= 2); FP64
-                              panels, NB = 128 only */
+                              column maxima, an FP32-class factorization (FP64 panels, NB = 128
+                              only).  For least squares with FP64 iterative refinement
+                              (hqr_lstsq, refine_steps >= 2) on well-conditioned problems: the
+                              refinement ends near kappa^2 * 5e-9 * ||r|| / (||A|| ||x||) */
 
 /* Error behaviour of the drop-in (Hybrid_*, tile_*) entry points. */
 #define HQR_ERRORS_ABORT 0   /* print to stderr and exit(1) (the reference's MPI_Abort) */
