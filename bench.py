@@ -403,6 +403,8 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
     pq = ctypes.cast(hQ.data_ptr(), DP)
     pt = ctypes.cast(hTAU.data_ptr(), DP)
     times, t_qr, t_mq = [], [], []
+    ph_qr, ph_mq = [], []   # per call: [h2d, DAG, idle, d2h, device total, host] ms
+    ph = (ctypes.c_double * 6)()
     clocks = ClockSampler(torch.cuda.current_device()) if sample_clocks else None
     for it in range(1 + steps):
         if it == 1 and clocks:
@@ -413,10 +415,15 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
         L.Hybrid_tile_QR(ctypes.byref(st), pa, pt, 0, 1, IB)
         H.check(L.hqr_last_error(), "Hybrid_tile_QR")
         t1 = time.perf_counter()
+        L.hqr_dropin_phase_ms(ph)
+        p_qr = list(ph)
         L.Hybrid_make_Q(ctypes.byref(st), pq, pa, pt, 0, 1, IB)
         H.check(L.hqr_last_error(), "Hybrid_make_Q")
+        t2 = time.perf_counter()
+        L.hqr_dropin_phase_ms(ph)
         if it > 0:
-            t2 = time.perf_counter()
+            ph_qr.append(p_qr)
+            ph_mq.append(list(ph))
             times.append(t2 - t0)
             t_qr.append(t1 - t0)
             t_mq.append(t2 - t1)
@@ -433,6 +440,11 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
             "steps": steps, "warmup": 1, "precision": precision,
             "phases_ms": {"Hybrid_tile_QR": round(1e3 * float(np.mean(t_qr)), 3),
                           "Hybrid_make_Q": round(1e3 * float(np.mean(t_mq)), 3)},
+            # inside each call, from CUDA events on its stream (means over the steps)
+            "device_phases_ms": {
+                name: dict(zip(("h2d", "dag", "idle_status", "d2h", "device_total", "host_wall"),
+                               (round(float(v), 3) for v in np.mean(np.array(rows), axis=0))))
+                for name, rows in (("Hybrid_tile_QR", ph_qr), ("Hybrid_make_Q", ph_mq))},
             "clocks": clk,
             "api": "Hybrid_tile_QR + Hybrid_make_Q (pinned host arrays)"}
 
@@ -776,7 +788,8 @@ def run_batched(H, torch, L, args):
         cpu = {"value": round(v / 1e12, 6), "unit": "TFLOP/s", "cores": thr, "kind": "port",
                "sample": f"{done} matrices of the workload (oracle Hybrid_tile_QR + Hybrid_dormqr, NB 32, "
                          f"one matrix per thread)"}
-    peak = L.hqr_fp64_peak_tflops(None)
+    peak = max(L.hqr_fp64_peak_tflops(None), L.hqr_fp64_mma_peak_tflops(0, None),
+               L.hqr_fp64_mma_peak_tflops(1, None))
     value = d.flops / elapsed / 1e12
     padded_flops = sum(AT.qr_flops(a, b) + AT.ormqr_flops(a, b, nrhs) for a, b in zip(d.Mp, d.Np))
     line = {
@@ -797,7 +810,8 @@ def run_batched(H, torch, L, args):
                      "achieved": round(d.flops / elapsed / 1e12, 4), "peak": round(peak, 4),
                      "unit": "TFLOP/s", "frac": round(value / peak, 4) if peak > 0 else None,
                      "padded_flops_frac": round(padded_flops / d.flops, 4),
-                     "peak_source": "FP64 FMA issue rate measured in this run (hqr_fp64_peak_tflops)",
+                     "peak_source": "the larger of the FP64 FMA and DMMA issue rates measured in this "
+                                    "run (hqr_fp64_peak_tflops, hqr_fp64_mma_peak_tflops)",
                      "traffic": load_batch_traffic(sum(AT.qr_flops(a, b) for a, b in zip(m, n))),
                      "traffic_note": "factorization launch; the 128-matrix capture scaled by flops"},
         "task_counts": {"geqrf": geqrf_tasks, "ormqr": stats["count"]},
@@ -820,6 +834,7 @@ def main():
     ap.add_argument("--ib", type=int, default=32)
     ap.add_argument("--fp64-nb", type=int, default=256, help="tile order of the plain-FP64 comparison")
     ap.add_argument("--no-compare", action="store_true", help="skip the plain-FP64 comparison run")
+    ap.add_argument("--fp64-steps", type=int, default=3, help="timed steps of the plain-FP64 comparison")
     ap.add_argument("--cpu-n", type=int, default=4096, help="CPU sample order")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-check", action="store_true")
@@ -860,6 +875,10 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
 
     if args.impl == "reference":
+        # The reference's driver opens two nested parallel regions and only
+        # terminates with one thread in the outer one (Hybrid_tile_QR.c:399-405):
+        # its build runs with "1,<cores>", set before any OpenMP runtime loads.
+        os.environ.setdefault("OMP_NUM_THREADS", f"1,{os.cpu_count() or 1}")
         if args.batched:
             run_batched_reference(args, rank)
         else:
@@ -888,7 +907,12 @@ def main():
         return
     n, NB, IB = args.n, args.nb, args.ib
 
-    peak_fp64 = L.hqr_fp64_peak_tflops(None)
+    # FP64 rates of this GPU: FMA on the CUDA cores and the FP64 tensor cores
+    # (DMMA), each an issue-rate probe; the FP64 roofline takes the larger
+    fp64_rates = {"ffma": L.hqr_fp64_peak_tflops(None),
+                  "dmma_m8n8k4": L.hqr_fp64_mma_peak_tflops(0, None),
+                  "dmma_m16n8k16": L.hqr_fp64_mma_peak_tflops(1, None)}
+    peak_fp64 = max(fp64_rates.values())
     init = init64 = None
     if args.kappa is not None:
         compare_too = args.precision in ("split", "fast") and not args.no_compare
@@ -911,13 +935,15 @@ def main():
 
     compare = None
     if args.precision in ("split", "fast") and not args.no_compare:
-        fp = measure(H, torch, L, args, "fp64", n, args.fp64_nb, IB, 1, 1, dist, world, False,
+        fp = measure(H, torch, L, args, "fp64", n, args.fp64_nb, IB, args.fp64_steps, 1, dist, world, False,
                      not args.no_check, init64, rows)
         fv = fp["flops"] / fp["elapsed"] / 1e12
         compare = {"value": round(fv, 6), "unit": "TFLOP/s", "NB": args.fp64_nb, "IB": IB,
-                   "steps": 1, "warmup": 1, "ms_per_step": round(1e3 * fp["elapsed"], 3),
-                   "phases_ms": {"factor": round(1e3 * fp["fact_s"][0], 3),
-                                 "make_q": round(1e3 * fp["mq_s"][0], 3)},
+                   "steps": args.fp64_steps, "warmup": 1,
+                   "ms_per_step": round(1e3 * fp["elapsed"] / args.fp64_steps, 3),
+                   "phases_ms": {"factor": round(1e3 * float(np.mean(fp["fact_s"])), 3),
+                                 "make_q": round(1e3 * float(np.mean(fp["mq_s"])), 3)},
+                   "fp64_roofline_frac": round(fv / peak_fp64, 4),
                    "accuracy": fp["acc"], "split_over_fp64": round(value / fv, 3)}
 
     cpu = None
@@ -945,8 +971,9 @@ def main():
         roofline = {"kernel": "dag_exec_kernel<fp64> (factorization launch)", "bound": "fp64",
                     "achieved": round(achieved, 4), "peak": round(peak_fp64, 4), "unit": "TFLOP/s",
                     "frac": round(achieved / peak_fp64, 4) if peak_fp64 > 0 else None,
-                    "peak_source": "FP64 FMA issue rate measured in this run (hqr_fp64_peak_tflops); "
-                                   "MEASURED_PEAKS.json holds no FP64 figure",
+                    "peak_source": "the larger of the FP64 FMA and DMMA issue rates measured in this run "
+                                   "(hqr_fp64_peak_tflops, hqr_fp64_mma_peak_tflops); MEASURED_PEAKS.json "
+                                   "holds no FP64 figure",
                     "traffic": load_traffic(n, NB, "fp64"),
                     "algorithmic_flops_per_launch": qr_flops(M, n)}
     # this library's kernels per step: factorization (init, seed, executor);
@@ -972,6 +999,7 @@ def main():
         "plain_fp64": compare,
         "roofline": roofline,
         "fp64_peak_measured_tflops": round(peak_fp64, 4),
+        "fp64_rates_tflops": {k: round(v, 4) for k, v in fp64_rates.items()},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": launches_per_step * args.steps,

@@ -6,6 +6,7 @@
 // friends call MPI_Abort): each call stages its operands in device buffers
 // owned by the library, runs the tile DAG on the GPU and copies results back.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -23,6 +24,9 @@ struct hqr_plan {
   hqr::DagWorkspace ws;
   hqr::OzWorkspace oz;   // allocated for the split precisions only
   hqr::TreeWorkspace tree;   // domain tree (hqr_plan_set_tree); S = 0: flat
+  // 1 while dT / oz hold the T factors / prepared operands of the last
+  // factorization on this plan (a rebuild from other reflectors replaces them)
+  int factors_valid = 0;
 };
 
 namespace {
@@ -121,6 +125,8 @@ bool split_precision(int precision) { return precision == HQR_PREC_OZAKI || prec
 // tile columns that are still unit vectors (2/3 of the forward updates), then
 // transposed in place; the identity is written whole, so the result does not
 // depend on dQ's prior contents.  Other shapes: the forward application.
+// rebuild_t: rebuild the T factors / prepared operands from dRY, dTAU (they
+// then replace the factorization's in the plan); else use the factorization's.
 int build_qt(hqr_plan* plan, double* dQ, const double* dRY, const double* dTAU, bool rebuild_t,
              cudaStream_t s) {
   const hqr::Geometry& g = plan->g;
@@ -130,15 +136,56 @@ int build_qt(hqr_plan* plan, double* dQ, const double* dRY, const double* dTAU, 
     return hqr::launch_apply_qt_tree(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g.NT, g_timeout_ns, s,
                                      &plan->oz, &plan->tree);
   }
+  if (rebuild_t) plan->factors_valid = 0;
   if (g.M == g.N && g.NB % 32 == 0) {
     hqr::make_identity(dQ, g.M, g.N, g.NB, true, s);
-    TRY(hqr::launch_build_q(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g_timeout_ns, s, &plan->oz));
+    TRY(hqr::launch_build_q(g, &plan->ws, dRY, plan->dT, dTAU, dQ, rebuild_t, g_timeout_ns, s, &plan->oz));
     hqr::transpose_tiles(dQ, g.N, g.NB, s);
     return cuda_rc(cudaGetLastError());
   }
   hqr::make_identity(dQ, g.M, g.N, g.NB, false, s);
   return hqr::launch_apply_qt(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g.NT, rebuild_t, g_timeout_ns, s,
                               &plan->oz);
+}
+
+// Whether a Q application must rebuild its T factors: always unless the
+// caller vouches for the plan's (use_plan_t) and nothing has replaced them.
+bool must_rebuild(const hqr_plan* plan, int use_plan_t) { return !use_plan_t || !plan->factors_valid; }
+
+// Phases of the last drop-in call, from CUDA events on the staging stream:
+// marks 0..4 = before the host-to-device copies, after them, after the DAG
+// launch(es) were enqueued, after the host read the scheduler's status, after
+// the device-to-host copies.
+struct PhaseTimes {
+  cudaEvent_t ev[5] = {};
+  bool ready = false;
+  double ms[6] = {};
+  std::chrono::steady_clock::time_point t0;
+};
+PhaseTimes g_phase;
+
+void phase_begin(cudaStream_t s) {
+  if (!g_phase.ready) {
+    g_phase.ready = true;
+    for (auto& e : g_phase.ev)
+      if (cudaEventCreate(&e) != cudaSuccess) g_phase.ready = false;
+  }
+  g_phase.t0 = std::chrono::steady_clock::now();
+  if (g_phase.ready) cudaEventRecord(g_phase.ev[0], s);
+}
+void phase_mark(int i, cudaStream_t s) {
+  if (g_phase.ready) cudaEventRecord(g_phase.ev[i], s);
+}
+// After the final synchronisation: [h2d, DAG, idle while the host checked the
+// status, d2h, device total, host wall time] in milliseconds.
+void phase_end() {
+  const double host = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - g_phase.t0).count();
+  if (!g_phase.ready) return;
+  float f[5] = {0, 0, 0, 0, 0};
+  for (int i = 0; i < 4; i++) cudaEventElapsedTime(&f[i], g_phase.ev[i], g_phase.ev[i + 1]);
+  cudaEventElapsedTime(&f[4], g_phase.ev[0], g_phase.ev[4]);
+  for (int i = 0; i < 5; i++) g_phase.ms[i] = f[i];
+  g_phase.ms[5] = host;
 }
 
 int h2d(double* d, const double* h, size_t n, cudaStream_t s) {
@@ -249,7 +296,7 @@ int hqr_plan_set_tree(hqr_plan_t* plan, int domain_tiles) {
             cudaMalloc(&t.TAU2, slots * nb * sizeof(double)) == cudaSuccess;
   if (ok && split_precision(plan->precision))
     ok = cudaMalloc(&t.slices2, slots * hqr::oz_panel_bytes()) == cudaSuccess &&
-         cudaMalloc(&t.sexp2, slots * 3 * nb * sizeof(int)) == cudaSuccess;
+         cudaMalloc(&t.sexp2, slots * hqr::oz_exp_bytes_per_panel((int)nb)) == cudaSuccess;
   if (!ok) {
     free_tree(&t);
     return HQR_ERR_NOMEM;
@@ -274,8 +321,11 @@ double* hqr_plan_t_factors(hqr_plan_t* plan) { return plan ? plan->dT : nullptr;
 
 int hqr_geqrf_async(hqr_plan_t* plan, double* dA, double* dTAU, void* stream) {
   if (!plan || !dA || !dTAU) return HQR_ERR_INVALID;
-  return hqr::launch_factor(plan->g, &plan->ws, dA, plan->dT, dTAU, g_timeout_ns,
-                            (cudaStream_t)stream, &plan->oz, &plan->tree);
+  plan->factors_valid = 0;
+  TRY(hqr::launch_factor(plan->g, &plan->ws, dA, plan->dT, dTAU, g_timeout_ns, (cudaStream_t)stream, &plan->oz,
+                         &plan->tree));
+  plan->factors_valid = 1;
+  return HQR_OK;
 }
 
 int hqr_plan_status(hqr_plan_t* plan, void* stream) {
@@ -305,7 +355,7 @@ int hqr_make_q_async(hqr_plan_t* plan, double* dQ, double* dRY, const double* dT
   if (!plan || !dQ || !dRY || !dTAU) return HQR_ERR_INVALID;
   const hqr::Geometry& g = plan->g;
   cudaStream_t s = (cudaStream_t)stream;
-  TRY(build_qt(plan, dQ, dRY, dTAU, !use_plan_t, s));
+  TRY(build_qt(plan, dQ, dRY, dTAU, plan->tree.S > 0 ? !use_plan_t : must_rebuild(plan, use_plan_t), s));
   hqr::zero_reflectors(dRY, g.M, g.N, g.NB, s);
   return cuda_rc(cudaGetLastError());
 }
@@ -324,8 +374,10 @@ int hqr_ormqr_t(hqr_plan_t* plan, const double* dRY, const double* dTAU, double*
     TRY(hqr::launch_apply_qt_tree(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, g_timeout_ns,
                                   (cudaStream_t)stream, &plan->oz, &plan->tree));
   } else {
-    TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, !use_plan_t,
-                             g_timeout_ns, (cudaStream_t)stream, &plan->oz));
+    const bool rebuild = must_rebuild(plan, use_plan_t);
+    if (rebuild) plan->factors_valid = 0;
+    TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, rebuild, g_timeout_ns,
+                             (cudaStream_t)stream, &plan->oz));
   }
   return hqr_plan_status(plan, stream);
 }
@@ -451,6 +503,17 @@ double hqr_fp64_peak_tflops(void* stream) {
   return hqr::measure_fp64_peak_tflops((cudaStream_t)stream);
 }
 
+int hqr_dropin_phase_ms(double* out) {
+  if (!out) return HQR_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (int i = 0; i < 6; i++) out[i] = g_phase.ms[i];
+  return HQR_OK;
+}
+
+double hqr_fp64_mma_peak_tflops(int shape, void* stream) {
+  return hqr::measure_fp64_mma_peak_tflops(shape, (cudaStream_t)stream);
+}
+
 int hqr_zero_reflectors(long M, long N, int NB, double* dA, void* stream) {
   if (!dA || NB <= 0 || M % NB || N % NB) return HQR_ERR_INVALID;
   hqr::zero_reflectors(dA, M, N, NB, (cudaStream_t)stream);
@@ -473,12 +536,20 @@ static int do_tile_qr(mat_stat_t* st, double* A, double* TAU, int rank, int P, i
   double *dA, *dTAU;
   TRY(stage_reserve(0, (size_t)M * N, &dA));
   TRY(stage_reserve(1, tau_len(plan->g), &dTAU));
+  phase_begin(s);
   TRY(h2d(dA, A, (size_t)M * N, s));
   TRY(h2d(dTAU, TAU, tau_len(plan->g), s));
-  TRY(hqr_geqrf(plan, dA, dTAU, s));
+  phase_mark(1, s);
+  TRY(hqr_geqrf_async(plan, dA, dTAU, s));
+  phase_mark(2, s);
+  TRY(hqr_plan_status(plan, s));
+  phase_mark(3, s);
   TRY(d2h(A, dA, (size_t)M * N, s));
   TRY(d2h(TAU, dTAU, tau_len(plan->g), s));
-  return cuda_rc(cudaStreamSynchronize(s));
+  phase_mark(4, s);
+  TRY(cuda_rc(cudaStreamSynchronize(s)));
+  phase_end();
+  return HQR_OK;
 }
 
 void Hybrid_tile_QR(mat_stat_t* status, double* A, double* TAU, int my_rank, int Proc_num, int ib) {
@@ -508,26 +579,33 @@ static int do_apply(mat_stat_t* st, double* Q, double* RY, double* TAU, int rank
   TRY(stage_reserve(0, (size_t)M * N, &dRY));
   TRY(stage_reserve(1, tau_len(plan->g), &dTAU));
   TRY(stage_reserve(2, (size_t)M * N, &dQ));
+  phase_begin(s);
   TRY(h2d(dRY, RY, (size_t)M * N, s));
   TRY(h2d(dTAU, TAU, tau_len(plan->g), s));
+  if (mode == 2 || (mode == 0 && plan->g.M != plan->g.N)) TRY(h2d(dQ, Q, (size_t)M * N, s));
+  phase_mark(1, s);
   if (mode == 2) {
-    TRY(h2d(dQ, Q, (size_t)M * N, s));
+    plan->factors_valid = 0;
     TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dQ, plan->g.NT, true,
                              g_timeout_ns, s, &plan->oz));
   } else {
     // make_Q (caller-zeroed Q, Hybrid_make_Q.c:91-95) and dorgqr (Q := I,
     // Hybrid_dorgqr.c:56) both produce Q^T of the factorization
-    if (mode == 0 && plan->g.M != plan->g.N) TRY(h2d(dQ, Q, (size_t)M * N, s));
     if (mode == 1) hqr::make_identity(dQ, M, N, NB, true, s);
     TRY(build_qt(plan, dQ, dRY, dTAU, true, s));
   }
+  phase_mark(2, s);
   TRY(hqr_plan_status(plan, s));
+  phase_mark(3, s);
   if (mode == 0) {
     hqr::zero_reflectors(dRY, M, N, NB, s);
     TRY(d2h(RY, dRY, (size_t)M * N, s));
   }
   TRY(d2h(Q, dQ, (size_t)M * N, s));
-  return cuda_rc(cudaStreamSynchronize(s));
+  phase_mark(4, s);
+  TRY(cuda_rc(cudaStreamSynchronize(s)));
+  phase_end();
+  return HQR_OK;
 }
 
 void Hybrid_make_Q(mat_stat_t* status, double* Q, double* RY, double* TAU, int my_rank,

@@ -215,10 +215,13 @@ int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, doubl
   set_oz(p, g, ozw);
   p.prep = 0;
   p.nblk = 1;
+  // rebuild_t: panel tasks rebuild each panel tile's T (FP64: its diagonal
+  // blocks) or prepared operands (split) from V and TAU; else the updates use
+  // those the factorization left in dT / the slice store
+  p.skip_panels = rebuild_t ? 0 : 1;
   long long n = 0;
-  for (int i = 0; i < g.steps; i++) n += (g.MT - i) + (long long)p.NC * CT * (g.MT - i);
+  for (int i = 0; i < g.steps; i++) n += (rebuild_t ? (g.MT - i) : 0) + (long long)p.NC * CT * (g.MT - i);
   p.n_tasks = (int)n;
-  (void)rebuild_t;   // panel tasks always rebuild T: O(NB^2 w) (FP64) or O(NB^3) (split) per tile
   return run_dag(p, ws, g, stream);
 }
 
@@ -250,7 +253,7 @@ int launch_apply_qt_tree(const Geometry& g, DagWorkspace* ws, const double* dA, 
 }
 
 int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT, const double* dTAU,
-                   double* dQ, long long timeout_ns, cudaStream_t stream, const OzWorkspace* ozw) {
+                   double* dQ, bool rebuild_t, long long timeout_ns, cudaStream_t stream, const OzWorkspace* ozw) {
   if (g.M != g.N) return HQR_ERR_INVALID;
   DagParams p{};
   p.mode = kModeBuildQ;
@@ -267,9 +270,11 @@ int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double
   set_oz(p, g, ozw);
   p.prep = 0;
   p.nblk = 1;
-  // per step i: MT - i panel tasks and NC (NT - i) (MT - i) updates
+  p.skip_panels = rebuild_t ? 0 : 1;   // as in launch_apply_qt (split: T from its own slot)
+  // per step i: MT - i panel tasks (when rebuilding) and NC (NT - i) (MT - i) updates
   long long n = 0;
-  for (int i = 0; i < g.steps; i++) n += (g.MT - i) + (long long)p.NC * (g.NT - i) * (g.MT - i);
+  for (int i = 0; i < g.steps; i++)
+    n += (rebuild_t ? (g.MT - i) : 0) + (long long)p.NC * (g.NT - i) * (g.MT - i);
   p.n_tasks = (int)n;
   return run_dag(p, ws, g, stream);
 }
@@ -440,7 +445,8 @@ static size_t panel_tiles(const Geometry& g) {
 }
 size_t oz_slice_bytes(const Geometry& g) { return panel_tiles(g) * oz::panel_slice_bytes(); }
 size_t oz_panel_bytes() { return oz::panel_slice_bytes(); }
-size_t oz_exp_bytes(const Geometry& g) { return panel_tiles(g) * 3 * (size_t)g.NB * sizeof(int); }
+size_t oz_exp_bytes(const Geometry& g) { return panel_tiles(g) * oz::kSlots * (size_t)g.NB * sizeof(int); }
+size_t oz_exp_bytes_per_panel(int NB) { return (size_t)oz::kSlots * NB * sizeof(int); }
 
 size_t tree_slots(const Geometry& g, int S) {
   if (S <= 0 || S >= g.MT) return 0;

@@ -112,7 +112,7 @@ struct DagParams {
   int oz_groups;    // t-groups of the split updates (8 or 4; host side: picks the kernel)
   int prep;         // 1: separate OZPREP ids after the panel ids (factorization)
   uint8_t* slices;  // sliced left operands, one block per panel tile
-  int* sexp;        // their row exponents (3 * NB ints per panel tile)
+  int* sexp;        // their row exponents (oz::kSlots * NB ints per panel tile)
 };
 
 constexpr int kNever = 0x3fffffff;
@@ -394,8 +394,8 @@ __device__ int init_deps(const DagParams& p, int id) {
     const int j = u % p.J;
     const int i = u / p.J;
     if (k >= i && i < p.steps && update_valid(p, i, j)) {
-      if (p.mode == kModeBuildQ)   // panel + chain from the tile below + step i+1's write of (k, j)
-        deps = 1 + (k < p.MT - 1 ? 1 : 0) + ((k > i && j > i && i + 1 < p.steps) ? 1 : 0);
+      if (p.mode == kModeBuildQ)   // panel (unless given) + chain from the tile below + step i+1's write of (k, j)
+        deps = (p.skip_panels ? 0 : 1) + (k < p.MT - 1 ? 1 : 0) + ((k > i && j > i && i + 1 < p.steps) ? 1 : 0);
       else   // panel (unless given) + the chain above in the domain + the previous step's write
         deps = (p.skip_panels ? 0 : 1) + (is_top(p, i, k) ? 0 : 1) + (i > 0 ? 1 : 0);
     }
@@ -732,7 +732,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
         prep_g = q.T + o;
         prep_kind = is_top(q, t.i, t.k) ? kVUnitLower : kVDense;
         prep_slices = q.slices + slot * oz::panel_slice_bytes();
-        prep_exps = q.sexp + slot * 3 * NB;
+        prep_exps = q.sexp + slot * oz::kSlots * NB;
         break;
       }
       case kTTPREP: {
@@ -742,7 +742,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
         prep_g = q.T2 + slot * tsz;
         prep_kind = kVUpper;
         prep_slices = q.slices2 + slot * oz::panel_slice_bytes();
-        prep_exps = q.sexp2 + slot * 3 * NB;
+        prep_exps = q.sexp2 + slot * oz::kSlots * NB;
         break;
       }
       case kLARFB: {   // tile row k = the diagonal or a domain top
@@ -750,7 +750,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
         if (OZ) {
           const size_t slot = panel_slot(q.MT, t.i, t.k);
           oz_slices = q.slices + slot * oz::panel_slice_bytes();
-          oz_exps = q.sexp + slot * 3 * NB;
+          oz_exps = q.sexp + slot * oz::kSlots * NB;
           oz_bot = q.C + oc + (size_t)t.c * oz::kN * NB;
         } else {
           task_larfb(q.A + ov, q.T + ov, q.C + oc, t.c * q.sh.CB, q.sh.CB, q.sh, smem, q.sp,
@@ -768,7 +768,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
         if (OZ) {
           const size_t cofs = (size_t)t.c * oz::kN * NB;
           oz_slices = (tt ? q.slices2 : q.slices) + slot * oz::panel_slice_bytes();
-          oz_exps = (tt ? q.sexp2 : q.sexp) + slot * 3 * NB;
+          oz_exps = (tt ? q.sexp2 : q.sexp) + slot * oz::kSlots * NB;
           oz_top = q.C + o1 + cofs;
           oz_bot = q.C + o2 + cofs;
         } else {
@@ -781,13 +781,16 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
         if (threadIdx.x == 0) atomicOr((int*)(q.ctl + kErr), kErrBadTask);
     }
     if (ts_a1) task_tsqrt_blk(ts_a1, ts_a2, ts_t, ts_tau, q.sh, smem, q.sp, t.c, ts_upper);
+    // the factorization's preparations also keep T for Q generation
     if (OZ && prep_v)
       task_ozprep(prep_v, prep_tau, prep_g, prep_kind, prep_slices, prep_exps, reinterpret_cast<uint8_t*>(smem),
-                  s_tmem, q.ctl + kErr, q.mode != kModeBuildQ);
+                  s_tmem, q.ctl + kErr, q.mode != kModeBuildQ, q.mode == kModeFactor && t.type == kOZPREP);
     if (OZ && oz_bot) {
       oz::Ctx c;
       oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, q.ctl + kErr);
-      task_ozapply<OZG>(c, oz_slices, oz_exps, oz_top, oz_bot);
+      // Q generation on the factorization's slices takes T from its own slot
+      task_ozapply<OZG>(c, oz_slices, oz_exps, oz_top, oz_bot,
+                        (q.mode == kModeBuildQ && q.skip_panels) ? (int)kOzT : (int)kOzTT);
     }
     fence_acq_rel_gpu();   // release: this task's writes before its dependents' counters
     __syncthreads();

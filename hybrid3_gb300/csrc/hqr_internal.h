@@ -61,13 +61,14 @@ void dag_workspace_free(DagWorkspace* ws);
 
 // Workspace of the split-precision updates (null slices: FP64 updates).
 struct OzWorkspace {
-  uint8_t* slices = nullptr;   // sliced V^T, T^T, V of every panel tile
+  uint8_t* slices = nullptr;   // sliced V^T, T^T, V, T of every panel tile
   int* sexp = nullptr;         // their row exponents
   int groups = 8;              // t-groups of the updates: 8 (FP64-level) or 4 (reduced)
 };
 // Bytes of the split-precision workspace for a geometry (NB = 128).
 size_t oz_slice_bytes(const Geometry& g);
 size_t oz_exp_bytes(const Geometry& g);
+size_t oz_exp_bytes_per_panel(int NB);   // row exponents of one panel tile's operands
 size_t oz_panel_bytes();   // prepared operands of one panel tile
 bool oz_supported(const Geometry& g);
 // Inner block width of the FP64 panels for the split path (see hqr_dag.cu).
@@ -102,8 +103,10 @@ int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, doubl
                     cudaStream_t stream, const OzWorkspace* oz = nullptr);
 // Q = H_0 H_1 ... H_{steps-1} dQ for dQ = I (square matrices): backward
 // accumulation, skipping the tile columns that are still unit vectors.
+// rebuild_t false: the T factors / prepared operands of the factorization.
 int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT, const double* dTAU,
-                   double* dQ, long long timeout_ns, cudaStream_t stream, const OzWorkspace* oz = nullptr);
+                   double* dQ, bool rebuild_t, long long timeout_ns, cudaStream_t stream,
+                   const OzWorkspace* oz = nullptr);
 // Batches of independent FP64 factorizations in one persistent launch.
 // Descriptors (mat_desc_bytes() each) are written to host memory by
 // batch_describe and must be on the device (d_desc) for launch_batch.
@@ -159,5 +162,6 @@ void tiles_to_colmajor(const double* dT, double* dOut, long M, long N, int NB, c
 void colmajor_to_tiles(const double* dIn, double* dT, long M, long N, int NB, cudaStream_t s);
 void max_col_abs_sum(const double* dColMajor, long M, long N, double* d_out, cudaStream_t s);
 double measure_fp64_peak_tflops(cudaStream_t s);
+double measure_fp64_mma_peak_tflops(int shape, cudaStream_t s);
 
 }  // namespace hqr

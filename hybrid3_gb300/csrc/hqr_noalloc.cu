@@ -5,11 +5,11 @@
 // DAG's dependency counters and ready queues, the scheduler's control words)
 // lives in one fixed-size array in device global memory, reserved when the
 // library's device code is loaded.  It exists for callers that may not call
-// cudaMalloc: code that runs while a CUDA graph is being captured, processes
-// whose device memory is entirely owned by their own pool allocator, and
-// latency-bound paths that cannot afford the device-wide synchronisation an
-// allocation can cause.  They pass device pointers to A and TAU and nothing
-// else.
+// cudaMalloc: processes whose device memory is entirely owned by their own
+// pool allocator, and latency-bound paths that cannot afford the device-wide
+// synchronisation an allocation can cause.  They pass device pointers to A and
+// TAU and nothing else.  Each call ends by synchronising its stream and
+// reading the scheduler's error word.
 //
 // Limits and sharing:
 //   * the array holds kNoAllocScratchBytes (64 MiB) on every GPU that loads

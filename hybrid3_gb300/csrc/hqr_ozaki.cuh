@@ -60,9 +60,11 @@ constexpr int kAChunkBytes = kS * kSliceABytes;         // 32 KiB: all slices of
 constexpr int kBChunkBytes = kS * kSliceBBytes;         // 16 KiB
 constexpr long long kWaitIters = 1LL << 26;             // bounded mbarrier waits
 
-// Bytes of one prepared left operand and of the three of a panel tile.
+// Bytes of one prepared left operand and of the kSlots of a panel tile
+// (V^T, T^T, V, and T for applying the reflector itself).
+constexpr int kSlots = 4;
 __host__ __device__ constexpr size_t operand_bytes() { return (size_t)kK * kK * kS * 2; }
-__host__ __device__ constexpr size_t panel_slice_bytes() { return 3 * operand_bytes(); }
+__host__ __device__ constexpr size_t panel_slice_bytes() { return kSlots * operand_bytes(); }
 
 // Pipeline depth: A chunks (bulk TMA) and sliced B chunks in flight.
 constexpr int kAStages = 3;

@@ -14,8 +14,11 @@
 
 namespace hqr {
 
-// Offsets of a panel tile's three prepared operands and their row exponents.
-constexpr size_t kOzVT = 0, kOzTT = 1, kOzV = 2;
+// Slots of a panel tile's prepared operands (and of their row exponents):
+// V^T, the middle operand (T^T, or T where the preparation applies H itself),
+// V, and -- written by the factorization's preparation only -- T, so that Q
+// generation (which applies H, not H^T) can reuse the factorization's slices.
+constexpr size_t kOzVT = 0, kOzTT = 1, kOzV = 2, kOzT = 3;
 
 // T upper triangular, packed by columns in shared memory: T(a, b) (a <= b)
 // at b (b + 1) / 2 + a.  As a left operand: X = T^T (transposed) or X = T.
@@ -91,12 +94,12 @@ enum VKind : int {
 
 // OZPREP of panel tile V (global, NB x NB, of shape vkind) with TAU tau.  G: NB x NB global scratch.
 // slices / exps: this tile's prepared operands and row exponents; the middle
-// operand is T^T (applying H^T) or, with t_transposed false, T (applying H).
-// sm: the CTA's dynamic shared memory (oz::kSmemBytes).  False on a device
-// time-out.
+// operand is T^T (applying H^T) or, with t_transposed false, T (applying H);
+// with also_t, T goes to slot kOzT as well.  sm: the CTA's dynamic shared
+// memory (oz::kSmemBytes).  False on a device time-out.
 inline __device__ bool task_ozprep(const double* V, const double* tau, double* G, int vkind,
                                    uint8_t* slices, int* exps, uint8_t* sm, uint32_t tmem,
-                                   unsigned* err, bool t_transposed) {
+                                   unsigned* err, bool t_transposed, bool also_t) {
   using namespace oz;
   constexpr size_t ob = operand_bytes();
   // 1. V^T and V from a shared-memory copy of the tile
@@ -141,27 +144,29 @@ inline __device__ bool task_ozprep(const double* V, const double* tau, double* G
   }
   __syncthreads();
   t_recurrence(sG, sT, sX, tau);
-  // 4. T^T or T
+  // 4. T^T or T (and T)
   slice_left(PackedTAcc{sT, t_transposed}, slices + kOzTT * ob, exps + kOzTT * kK, sE);
+  if (also_t) slice_left(PackedTAcc{sT, false}, slices + kOzT * ob, exps + kOzT * kK, sE);
   return true;
 }
 
 // One 64-column block of the update.  Ctop: A1 block (SSRFB) or nullptr
-// (LARFB); Cbot: A2 block (SSRFB) or the C block (LARFB); ld NB.  Returns
-// false on a device time-out (error word already set).  G: t-groups of the
-// three products (8: FP64-level; 4: the reduced form, see oz::product).
+// (LARFB); Cbot: A2 block (SSRFB) or the C block (LARFB); ld NB.  mid: the
+// slot of the middle operand (kOzTT, or kOzT for Q generation on the
+// factorization's slices).  Returns false on a device time-out (error word
+// already set).  G: t-groups of the three products (8: FP64-level; 4: the
+// reduced form, see oz::product).
 template <int G = oz::kGroups>
 inline __device__ bool task_ozapply(oz::Ctx& c, const uint8_t* slices, const int* exps, double* Ctop,
-                                    double* Cbot) {
+                                    double* Cbot, int mid) {
   using namespace oz;
   constexpr size_t ob = operand_bytes();
   prefetch<G>(c, slices + kOzVT * ob);
   stage_y(c, Cbot, kK, -1);
-  if (!product<G>(c, slices + kOzVT * ob, slices + kOzTT * ob, exps + kOzVT * kK, kEpiToY, nullptr, 0, Ctop,
-                  kK))
+  if (!product<G>(c, slices + kOzVT * ob, slices + mid * ob, exps + kOzVT * kK, kEpiToY, nullptr, 0, Ctop, kK))
     return false;
-  if (!product<G>(c, slices + kOzTT * ob, slices + kOzV * ob, exps + kOzTT * kK, kEpiToYSubTop, nullptr, 0,
-                  Ctop, kK))
+  if (!product<G>(c, slices + mid * ob, slices + kOzV * ob, exps + mid * kK, kEpiToYSubTop, nullptr, 0, Ctop,
+                  kK))
     return false;
   if (!product<G>(c, slices + kOzV * ob, nullptr, exps + kOzV * kK, kEpiSubInto, Cbot, kK, nullptr, 0))
     return false;

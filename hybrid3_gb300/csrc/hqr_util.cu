@@ -225,6 +225,82 @@ __global__ void k_fp64_peak(double* out, double b, double c) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
 }
 
+// FP64 tensor-core (DMMA) issue-rate probe: mma.sync f64 on independent
+// accumulators, no memory traffic.  SHAPE 0: m8n8k4 (A 1, B 1, C 2 doubles per
+// thread); 1: m16n8k16 (A 8, B 4, C 4).
+constexpr int kMmaIter = 1024;
+constexpr int kMmaAcc = 4;
+template <int SHAPE>
+__global__ void __launch_bounds__(256) k_fp64_mma_peak(double* out, double av, double bv) {
+  double a[8], b[4], d[kMmaAcc][4];
+#pragma unroll
+  for (int i = 0; i < 8; i++) a[i] = av * (threadIdx.x + i);
+#pragma unroll
+  for (int i = 0; i < 4; i++) b[i] = bv * (i + 1);
+#pragma unroll
+  for (int q = 0; q < kMmaAcc; q++)
+#pragma unroll
+    for (int i = 0; i < 4; i++) d[q][i] = 0.0;
+  for (int it = 0; it < kMmaIter; it++) {
+#pragma unroll
+    for (int q = 0; q < kMmaAcc; q++) {
+      if (SHAPE == 0) {
+        asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                     : "+d"(d[q][0]), "+d"(d[q][1])
+                     : "d"(a[q]), "d"(b[q]));
+      } else {
+        asm volatile(
+            "mma.sync.aligned.m16n8k16.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, "
+            "{%4,%5,%6,%7,%8,%9,%10,%11}, {%12,%13,%14,%15}, {%0,%1,%2,%3};"
+            : "+d"(d[q][0]), "+d"(d[q][1]), "+d"(d[q][2]), "+d"(d[q][3])
+            : "d"(a[0]), "d"(a[1]), "d"(a[2]), "d"(a[3]), "d"(a[4]), "d"(a[5]), "d"(a[6]), "d"(a[7]),
+              "d"(b[0]), "d"(b[1]), "d"(b[2]), "d"(b[3]));
+      }
+    }
+  }
+  double t = 0.0;
+#pragma unroll
+  for (int q = 0; q < kMmaAcc; q++)
+#pragma unroll
+    for (int i = 0; i < 4; i++) t += d[q][i];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = t;
+}
+
+double measure_fp64_mma_peak_tflops(int shape, cudaStream_t s) {
+  if (shape != 0 && shape != 1) return -1.0;
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = nsm * 4, threads = 256;
+  double* out = nullptr;
+  if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(double)) != cudaSuccess) return -1.0;
+  auto launch = [&]() {
+    if (shape == 0)
+      k_fp64_mma_peak<0><<<blocks, threads, 0, s>>>(out, 1e-3, 1e-3);
+    else
+      k_fp64_mma_peak<1><<<blocks, threads, 0, s>>>(out, 1e-3, 1e-3);
+  };
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  launch();   // warm-up
+  cudaEventRecord(e0, s);
+  const int reps = 5;
+  for (int r = 0; r < reps; r++) launch();
+  cudaEventRecord(e1, s);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (cudaGetLastError() != cudaSuccess) return -1.0;
+  // flops per warp instruction: 2 m n k
+  const double per_mma = shape == 0 ? 2.0 * 8 * 8 * 4 : 2.0 * 16 * 8 * 16;
+  const double flops = (double)reps * blocks * (threads / 32) * kMmaIter * kMmaAcc * per_mma;
+  return ms > 0 ? flops / (ms * 1e-3) / 1e12 : -1.0;
+}
+
 double measure_fp64_peak_tflops(cudaStream_t s) {
   int dev = 0, nsm = 1;
   cudaGetDevice(&dev);

@@ -103,30 +103,37 @@ double *hqr_plan_t_factors(hqr_plan_t *plan);
 int hqr_geqrf(hqr_plan_t *plan, double *dA, double *dTAU, void *stream);
 int hqr_geqrf_async(hqr_plan_t *plan, double *dA, double *dTAU, void *stream);
 /* No counterpart in the reference.  The factorization of hqr_geqrf for callers
- * that may not allocate device memory (work captured into a CUDA graph, memory
- * owned entirely by the caller's own pool, latency paths that cannot take the
- * synchronisation an allocation may cause): it calls no cudaMalloc/cudaFree
- * and uses a fixed 64 MiB scratch array that the library reserves on each GPU
- * that loads it, for the T factors (M*N doubles) and the scheduler tables --
- * shapes that do not fit (about n > 2800 square) return HQR_ERR_UNSUPPORTED.
- * All calls share that array: calls that overlap on the GPU race, so
- * serialise them.  The first call on a device looks the array up and must
- * come before any stream capture.  Waits for completion; returns a status. */
+ * that may not allocate device memory (a process whose device memory is owned
+ * entirely by its own pool allocator, a latency path that cannot take the
+ * device-wide synchronisation an allocation may cause): it calls no
+ * cudaMalloc/cudaFree and uses a fixed 64 MiB scratch array that the library
+ * reserves on each GPU that loads it, for the T factors (M*N doubles) and the
+ * scheduler tables -- shapes that do not fit (about n > 2800 square) return
+ * HQR_ERR_UNSUPPORTED.  All calls share that array: calls that overlap on the
+ * GPU race, so serialise them.  The first call on a device looks the array's
+ * address up; make that call before any stream capture.  Each call waits for
+ * `stream` to finish (it synchronises it) and returns the scheduler's status. */
 int hqr_geqrf_noalloc(long M, long N, int NB, int IB, double *dA, double *dTAU, void *stream);
 /* Synchronise `stream`, then read and clear the scheduler's error word. */
 int hqr_plan_status(hqr_plan_t *plan, void *stream);
 int hqr_plan_stats(hqr_plan_t *plan, hqr_stats_t *out, void *stream);
 
 /* Hybrid_make_Q semantics on device arrays: dQ (M x N) <- Q^T I; the
- * reflectors of dRY are zeroed (dRY becomes R).  use_plan_t: 1 reuses the T
- * factors persisted by the last hqr_geqrf on this plan, 0 rebuilds them from
- * V and TAU. */
+ * reflectors of dRY are zeroed (dRY becomes R).  use_plan_t = 1: dRY and dTAU
+ * are the output of the last hqr_geqrf on this plan, and its T factors (FP64)
+ * or prepared operands (split precisions), kept in the plan, are used as they
+ * are -- no panel tasks run.  If a call since then rebuilt them from other
+ * reflectors (use_plan_t = 0 here or in hqr_ormqr_t, or a drop-in Hybrid_*
+ * call), they are rebuilt from dRY and dTAU instead.  use_plan_t = 0: always
+ * rebuilt from dRY and dTAU (any reflectors in this plan's shape), replacing
+ * the plan's. */
 int hqr_make_q(hqr_plan_t *plan, double *dQ, double *dRY, const double *dTAU, int use_plan_t,
                void *stream);
 int hqr_make_q_async(hqr_plan_t *plan, double *dQ, double *dRY, const double *dTAU,
                      int use_plan_t, void *stream);
 /* Hybrid_dormqr semantics: dC <- Q^T dC, dC an MT x CT tile grid (CT tile
- * columns of NB, e.g. CT = 1 for up to NB right-hand sides padded to NB). */
+ * columns of NB, e.g. CT = 1 for up to NB right-hand sides padded to NB).
+ * use_plan_t as for hqr_make_q.  Waits for completion. */
 int hqr_ormqr_t(hqr_plan_t *plan, const double *dRY, const double *dTAU, double *dC, int CT,
                 int use_plan_t, void *stream);
 
@@ -214,9 +221,19 @@ int hqr_tiles_to_colmajor_padded(long M, long N, long ld, int NB, const double *
  * NB = 128; same slicing, tensor-core products and recombination as
  * the HQR_PREC_OZAKI updates.  Synchronous. */
 int hqr_ozaki_product(int NB, const double *dX, const double *dY, double *dC, void *stream);
+/* No counterpart in the reference: where the time of the last drop-in call
+ * (Hybrid_tile_QR, Hybrid_make_Q, Hybrid_dorgqr, Hybrid_dormqr) went, in
+ * milliseconds, from CUDA events on its stream: out[0] host-to-device copies,
+ * out[1] the tile DAG, out[2] the stream idle while the host read the
+ * scheduler's status, out[3] device-to-host copies, out[4] the device total,
+ * out[5] the call's host wall time. */
+int hqr_dropin_phase_ms(double *out);
 /* Measured FP64 FMA issue rate of this GPU in TFLOP/s (a ~10 ms probe of
  * independent FMA chains): the roofline denominator of the FP64 kernels. */
 double hqr_fp64_peak_tflops(void *stream);
+/* The same for the FP64 tensor cores: mma.sync f64 (DMMA) on independent
+ * accumulators, shape 0 = m8n8k4, 1 = m16n8k16; -1 on a bad shape or error. */
+double hqr_fp64_mma_peak_tflops(int shape, void *stream);
 /* Zero the reflectors below the diagonal (Hybrid_remv_Y). */
 int hqr_zero_reflectors(long M, long N, int NB, double *dA, void *stream);
 

@@ -34,8 +34,11 @@ _dp = ctypes.POINTER(ctypes.c_double)
 _lib = None
 
 
-def build(ref_dir: str = "/root/reference", quiet: bool = True) -> None:
-    """Compile the restatement (and the reference build when ``ref_dir`` exists)."""
+def build(ref_dir: str | None = None, quiet: bool = True) -> None:
+    """Compile the restatement, and the reference build when ``ref_dir`` (else
+    the environment variable HYBRID3_REF_DIR) names the reference's source
+    tree."""
+    ref_dir = ref_dir or os.environ.get("HYBRID3_REF_DIR", "")
     args = ["make", "-C", HERE, f"REF_DIR={ref_dir}"]
     out = subprocess.run(args, capture_output=True, text=True)
     if out.returncode != 0:

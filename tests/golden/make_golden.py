@@ -8,12 +8,19 @@ not needed to run them.
 
 Usage (from the repository root, where the reference tree exists):
     OMP_NUM_THREADS=1,4 python tests/golden/make_golden.py
+    OMP_NUM_THREADS=1,8 python tests/golden/make_golden.py --norms 8192 16384
+The second form runs the reference's Hybrid_tile_QR + Hybrid_make_Q at the
+given orders (NB = 256, IB = 32, the seeded uniform input) and records its
+||A - QR||_F / ||A||_F and ||I - Q Q^T||_F in ref_norms.json: the accuracy the
+GPU path is held to at sizes where an elementwise fixture would be too large.
 The "1,P" thread list is required: the reference's Hybrid_tile_QR opens two
 nested parallel regions (Hybrid_tile_QR.c:399-405) and only terminates when the
 outer one has a single thread.
 """
+import json
 import os
 import sys
+import time
 
 import numpy as np
 
@@ -36,6 +43,54 @@ def qr_case(name, A_tiles, M, N, NB, IB, C_tiles, extra=None):
         out.update(extra)
     np.savez_compressed(os.path.join(HERE, name), **out)
     print("wrote", name)
+
+
+def slim_qr_case(name, M, N, NB, IB, seed, c_seed):
+    """A larger case stored without the inputs (regenerated from their seeds by
+    oracle.uniform_matrix) and without the Q Q^T / Q R products."""
+    A = O.to_tiles(O.uniform_matrix(M, N, seed), NB)
+    C = O.to_tiles(O.uniform_matrix(M, N, c_seed), NB)
+    a, tau = O.ref_tile_qr(A, M, N, NB, IB)
+    q, _ = O.ref_make_Q(a, tau, M, N, NB, IB)
+    c = O.ref_dormqr(a, tau, C, M, N, NB)
+    np.savez_compressed(os.path.join(HERE, name), M=M, N=N, NB=NB, IB=IB, seed=seed, c_seed=c_seed,
+                        A_qr=a, TAU=tau, Qt=q, QtC=c)
+    print("wrote", name)
+
+
+def ref_norms(orders, NB=256, IB=32, seed=20151130):
+    """The reference's own accuracy at large orders, into ref_norms.json."""
+    path = os.path.join(HERE, "ref_norms.json")
+    rec = json.load(open(path)) if os.path.exists(path) else {"cases": []}
+    for n in orders:
+        A2d = O.uniform_matrix(n, n, seed)
+        A = O.to_tiles(A2d, NB)
+        t0 = time.perf_counter()
+        a, tau = O.ref_tile_qr(A, n, n, NB, IB)
+        t1 = time.perf_counter()
+        q, r = O.ref_make_Q(a, tau, n, n, NB, IB)
+        t2 = time.perf_counter()
+        del A, a
+        Qt = O.from_tiles(q, n, n, NB)
+        del q
+        R = O.from_tiles(r, n, n, NB)
+        del r
+        E = Qt.T @ R
+        E -= A2d
+        resid = float(np.linalg.norm(E) / np.linalg.norm(A2d))
+        del E, R, A2d
+        G = Qt @ Qt.T
+        G[np.diag_indices(n)] -= 1.0
+        orth = float(np.linalg.norm(G))
+        del G, Qt
+        case = {"n": n, "NB": NB, "IB": IB, "seed": seed, "resid_fro_rel": resid, "orth_fro": orth,
+                "threads": os.environ.get("OMP_NUM_THREADS", ""), "tile_qr_s": round(t1 - t0, 2),
+                "make_q_s": round(t2 - t1, 2)}
+        rec["cases"] = [c for c in rec["cases"] if not (c["n"] == n and c["NB"] == NB and c["IB"] == IB)]
+        rec["cases"].append(case)
+        rec["cases"].sort(key=lambda c: (c["n"], c["NB"], c["IB"]))
+        json.dump(rec, open(path, "w"), indent=1)
+        print(case, flush=True)
 
 
 def tile_kernel_case(name, NB, IB, seed):
@@ -85,9 +140,12 @@ def tile_kernel_case(name, NB, IB, seed):
 
 def main():
     if not O.ref_available():
-        O.build()
+        O.build(ref_dir=os.environ.get("HYBRID3_REF_DIR", "/root/reference"))
     if not O.ref_available():
         raise SystemExit("reference build not available (needs the reference tree)")
+    if "--norms" in sys.argv:
+        ref_norms([int(v) for v in sys.argv[sys.argv.index("--norms") + 1:]])
+        return
     M = N = 128
     NB, IB = 32, 8
     A = O.to_tiles(O.uniform_matrix(M, N, 20151130), NB)
@@ -99,6 +157,8 @@ def main():
     # IB == NB (the reference's default when argv[3] is absent, main.c:87)
     qr_case("qr_uniform_n128_nb32_ib32.npz", A, M, N, NB, NB, C)
     tile_kernel_case("tile_kernels_nb32_ib8.npz", 32, 8, 7)
+    # the tile order of the CPU workload configuration (NB = 256, IB = 32)
+    slim_qr_case("qr_uniform_n512_nb256_ib32.npz", 512, 512, 256, 32, 20151130, 4242)
 
 
 if __name__ == "__main__":

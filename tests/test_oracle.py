@@ -43,6 +43,25 @@ def test_tile_qr_matches_reference(golden_dir, name):
     assert np.abs(tau - g["TAU"]).max() <= t
 
 
+def test_nb256_fixture_matches_oracle(golden_dir):
+    """The reference at the CPU workload's tile order (NB = 256, IB = 32),
+    n = 512: factorization, Q generation and Q^T C; the inputs are regenerated
+    from their seeds."""
+    g = load(golden_dir, "qr_uniform_n512_nb256_ib32.npz")
+    M, N, NB, IB = (int(g[k]) for k in ("M", "N", "NB", "IB"))
+    A2d = O.uniform_matrix(M, N, int(g["seed"]))
+    A = O.to_tiles(A2d, NB)
+    C = O.to_tiles(O.uniform_matrix(M, N, int(g["c_seed"])), NB)
+    t = tol(A2d)
+    a, tau = O.tile_qr(A, M, N, NB, IB)
+    assert np.abs(a - g["A_qr"]).max() <= t
+    assert np.abs(tau - g["TAU"]).max() <= t
+    q, _ = O.make_Q(g["A_qr"], g["TAU"], M, N, NB)
+    assert np.abs(q - g["Qt"]).max() <= t
+    c = O.dormqr(g["A_qr"], g["TAU"], C, M, N, NB, N // NB)
+    assert np.abs(c - g["QtC"]).max() <= 4 * tol(O.from_tiles(C, M, N, NB))
+
+
 @pytest.mark.parametrize("name", QR_FIXTURES)
 def test_q_generation_matches_reference(golden_dir, name):
     g = load(golden_dir, name)
