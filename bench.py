@@ -379,6 +379,27 @@ def measure(H, torch, L, args, precision: str, n: int, NB: int, IB: int, steps: 
             "stats_mq": stats_mq, "flops": step_flops(M, N) * steps * world}
 
 
+class HostArrays:
+    """Page-locked host arrays from the library's allocator (hqr_host_alloc,
+    cudaHostAlloc): the arrays a caller of the drop-in entry points hands over."""
+
+    def __init__(self, L, torch):
+        self.L, self.torch, self.ptrs = L, torch, []
+
+    def empty(self, count: int):
+        p = ctypes.c_void_p()
+        rc = self.L.hqr_host_alloc(ctypes.byref(p), ctypes.c_size_t(count * 8))
+        if rc != 0:
+            raise MemoryError(f"hqr_host_alloc of {count * 8} bytes failed ({rc})")
+        self.ptrs.append(p.value)
+        return self.torch.from_numpy(np.ctypeslib.as_array(ctypes.cast(p, DP), shape=(count,)))
+
+    def free(self):
+        for p in self.ptrs:
+            self.L.hqr_host_free(ctypes.c_void_p(p))
+        self.ptrs = []
+
+
 def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: int, dist, world: int,
                 sample_clocks: bool = False):
     """The same workload through the drop-in C entry points with pinned host arrays:
@@ -391,13 +412,15 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
     gen = torch.empty(M * N, dtype=f64, device="cuda")
     H.check(L.hqr_fill_uniform(M, N, NB, 20151130, gen.data_ptr(), None), "fill")
     torch.cuda.synchronize()
-    hA0 = torch.empty(M * N, dtype=f64).pin_memory()
+    host = HostArrays(L, torch)
+    hA0 = host.empty(M * N)
     hA0.copy_(gen.cpu())
     del gen
     torch.cuda.empty_cache()
-    hA = torch.empty_like(hA0).pin_memory()
-    hQ = torch.empty_like(hA0).pin_memory()
-    hTAU = torch.zeros((M // 2) * (N // 2), dtype=f64).pin_memory()
+    hA = host.empty(M * N)
+    hQ = host.empty(M * N)
+    hTAU = host.empty((M // 2) * (N // 2))
+    hTAU.zero_()
     st = H.status(M, N, NB)
     pa = ctypes.cast(hA.data_ptr(), DP)
     pq = ctypes.cast(hQ.data_ptr(), DP)
@@ -429,14 +452,17 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
             t_mq.append(t2 - t1)
     clk = clocks.stop() if clocks else "not sampled (host-timed region)"
     L.hqr_set_default_precision(H.HQR_PREC_FP64)
+    del hA0, hA, hQ, hTAU
+    host.free()
     rate = job_rate(steps * step_flops(M, N), sum(times), dist)
     nbytes = M * N * 8
     tau_b = (M // NB) * (N // NB) * NB * 8
     return {"value": round(rate / 1e12, 6), "unit": "TFLOP/s",
             # Hybrid_tile_QR: A, TAU in and out; Hybrid_make_Q: RY, TAU in (a square
-            # Q is written whole on the device, not copied in), Q, RY out
+            # Q is written whole on the device, not copied in), Q out (R is the
+            # caller's RY with its reflectors zeroed on the host during the DAG)
             "h2d_bytes_per_step": 2 * nbytes + 2 * tau_b,
-            "d2h_bytes_per_step": nbytes + tau_b + 2 * nbytes,
+            "d2h_bytes_per_step": nbytes + tau_b + nbytes,
             "steps": steps, "warmup": 1, "precision": precision,
             "phases_ms": {"Hybrid_tile_QR": round(1e3 * float(np.mean(t_qr)), 3),
                           "Hybrid_make_Q": round(1e3 * float(np.mean(t_mq)), 3)},
@@ -446,7 +472,7 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
                                (round(float(v), 3) for v in np.mean(np.array(rows), axis=0))))
                 for name, rows in (("Hybrid_tile_QR", ph_qr), ("Hybrid_make_Q", ph_mq))},
             "clocks": clk,
-            "api": "Hybrid_tile_QR + Hybrid_make_Q (pinned host arrays)"}
+            "api": "Hybrid_tile_QR + Hybrid_make_Q (page-locked host arrays from hqr_host_alloc)"}
 
 
 def lstsq_flops(m: int, n: int, nrhs: int, refine: int) -> float:

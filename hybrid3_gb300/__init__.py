@@ -131,6 +131,8 @@ SIGNATURES = {
     "hqr_fp64_peak_tflops": (_D, [_vp]),
     "hqr_fp64_mma_peak_tflops": (_D, [_I, _vp]),
     "hqr_dropin_phase_ms": (_I, [ctypes.POINTER(ctypes.c_double)]),
+    "hqr_host_alloc": (_I, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]),
+    "hqr_host_free": (_I, [_vp]),
     "hqr_ozaki_product": (_I, [_I, _vp, _vp, _vp, _vp]),
     # include/tile_kernel.h (pointer arguments: host or device addresses)
     "tile_init": (_vp, [ctypes.c_char, _I, _I]),

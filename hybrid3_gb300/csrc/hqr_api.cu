@@ -6,12 +6,14 @@
 // friends call MPI_Abort): each call stages its operands in device buffers
 // owned by the library, runs the tile DAG on the GPU and copies results back.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "Hybrid_tile_QR.h"
@@ -47,6 +49,7 @@ struct Staging {
   double* buf[4] = {nullptr, nullptr, nullptr, nullptr};
   size_t cap[4] = {0, 0, 0, 0};
   cudaStream_t stream = nullptr;
+  cudaEvent_t h2d_done = nullptr;   // recorded after a call's host-to-device copies
   hqr_plan* plan = nullptr;
 };
 Staging g_stage;
@@ -69,8 +72,34 @@ int stage_stream(cudaStream_t* s) {
     if (cudaStreamCreateWithFlags(&g_stage.stream, cudaStreamNonBlocking) != cudaSuccess)
       return HQR_ERR_CUDA;
   }
+  if (!g_stage.h2d_done && cudaEventCreateWithFlags(&g_stage.h2d_done, cudaEventDisableTiming) != cudaSuccess)
+    return HQR_ERR_CUDA;
   *s = g_stage.stream;
   return HQR_OK;
+}
+
+// Hybrid_remv_Y on a host array in tile layout (what the device's
+// zero_reflectors does): the strictly lower triangle of each diagonal tile and
+// every tile below it, in the first min(MT, NT) tile columns.  Host threads
+// take tile columns from a shared counter.
+void host_zero_reflectors(double* A, long M, long N, int NB) {
+  const int MT = (int)(M / NB), NT = (int)(N / NB), steps = std::min(MT, NT);
+  const size_t tsz = (size_t)NB * NB;
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (int tj; (tj = next.fetch_add(1)) < steps;) {
+      double* col = A + (size_t)tj * MT * tsz;   // tile (0, tj)
+      double* d = col + (size_t)tj * tsz;
+      for (int c = 0; c + 1 < NB; c++) memset(d + (size_t)c * NB + c + 1, 0, (size_t)(NB - c - 1) * sizeof(double));
+      if (tj + 1 < MT) memset(col + (size_t)(tj + 1) * tsz, 0, (size_t)(MT - tj - 1) * tsz * sizeof(double));
+    }
+  };
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int nt = (int)std::min<unsigned>(16u, std::max(1u, std::min<unsigned>(hw, (unsigned)steps)));
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; t++) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
 }
 
 // Plan for the drop-in calls, rebuilt when the shape changes.
@@ -189,10 +218,10 @@ void phase_end() {
 }
 
 int h2d(double* d, const double* h, size_t n, cudaStream_t s) {
-  return cuda_rc(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  return cuda_rc(hqr::copy_host_to_device(d, h, n, s));
 }
 int d2h(double* h, const double* d, size_t n, cudaStream_t s) {
-  return cuda_rc(cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  return cuda_rc(hqr::copy_device_to_host(h, d, n, s));
 }
 
 }  // namespace
@@ -503,6 +532,14 @@ double hqr_fp64_peak_tflops(void* stream) {
   return hqr::measure_fp64_peak_tflops((cudaStream_t)stream);
 }
 
+int hqr_host_alloc(void** ptr, size_t bytes) {
+  if (!ptr || bytes == 0) return HQR_ERR_INVALID;
+  *ptr = nullptr;
+  return cudaHostAlloc(ptr, bytes, cudaHostAllocDefault) == cudaSuccess ? HQR_OK : HQR_ERR_NOMEM;
+}
+
+int hqr_host_free(void* ptr) { return ptr ? cuda_rc(cudaFreeHost(ptr)) : HQR_OK; }
+
 int hqr_dropin_phase_ms(double* out) {
   if (!out) return HQR_ERR_INVALID;
   std::lock_guard<std::mutex> lk(g_mu);
@@ -583,6 +620,7 @@ static int do_apply(mat_stat_t* st, double* Q, double* RY, double* TAU, int rank
   TRY(h2d(dRY, RY, (size_t)M * N, s));
   TRY(h2d(dTAU, TAU, tau_len(plan->g), s));
   if (mode == 2 || (mode == 0 && plan->g.M != plan->g.N)) TRY(h2d(dQ, Q, (size_t)M * N, s));
+  TRY(cuda_rc(cudaEventRecord(g_stage.h2d_done, s)));
   phase_mark(1, s);
   if (mode == 2) {
     plan->factors_valid = 0;
@@ -595,12 +633,14 @@ static int do_apply(mat_stat_t* st, double* Q, double* RY, double* TAU, int rank
     TRY(build_qt(plan, dQ, dRY, dTAU, true, s));
   }
   phase_mark(2, s);
+  if (mode == 0) {
+    // R is the caller's RY with the reflectors zeroed: done on the host array
+    // once the device has its copy, while the DAG runs (no copy back)
+    TRY(cuda_rc(cudaEventSynchronize(g_stage.h2d_done)));
+    host_zero_reflectors(RY, M, N, NB);
+  }
   TRY(hqr_plan_status(plan, s));
   phase_mark(3, s);
-  if (mode == 0) {
-    hqr::zero_reflectors(dRY, M, N, NB, s);
-    TRY(d2h(RY, dRY, (size_t)M * N, s));
-  }
   TRY(d2h(Q, dQ, (size_t)M * N, s));
   phase_mark(4, s);
   TRY(cuda_rc(cudaStreamSynchronize(s)));

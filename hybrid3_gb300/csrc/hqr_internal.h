@@ -151,6 +151,13 @@ void fill_uniform(double* dA, long M, long N, int NB, uint64_t seed, cudaStream_
 void make_identity(double* dQ, long M, long N, int NB, bool zero_first, cudaStream_t s);
 // In-place transpose of a square N x N tile-layout matrix (NB a multiple of 32).
 void transpose_tiles(double* dQ, long N, int NB, cudaStream_t s);
+// Host <-> device copies of n doubles for the drop-in calls.  A host array
+// that is page-locked and mapped (cudaHostAlloc, cudaHostRegister) is moved
+// by SM loads / stores through its device mapping: on this part the copy
+// engines' rate to host memory drops at times to a tenth, the SMs' does not.
+// Pageable host memory goes through cudaMemcpyAsync.
+cudaError_t copy_host_to_device(double* d, const double* h, size_t n, cudaStream_t s);
+cudaError_t copy_device_to_host(double* h, const double* d, size_t n, cudaStream_t s);
 void zero_reflectors(double* dA, long M, long N, int NB, cudaStream_t s);
 void dgemm_tn_tiles(const double* dA, const double* dB, double* dC, long M, long N, int NB,
                     cudaStream_t s);

@@ -72,6 +72,21 @@ __global__ void k_transpose_tiles(double* Q, long N, int NB) {
   }
 }
 
+// Streaming copy of n doubles by SM loads and stores (one side may be a
+// page-locked host array's device mapping); vec: both addresses 16-byte
+// aligned.
+__global__ void k_copy_stream(double* __restrict__ dst, const double* __restrict__ src, size_t n, int vec) {
+  const size_t tid = blockIdx.x * (size_t)blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+  if (vec) {
+    const size_t n2 = n / 2;
+    for (size_t i = tid; i < n2; i += stride)
+      reinterpret_cast<double2*>(dst)[i] = reinterpret_cast<const double2*>(src)[i];
+    if (tid == 0 && (n & 1)) dst[n - 1] = src[n - 1];
+  } else {
+    for (size_t i = tid; i < n; i += stride) dst[i] = src[i];
+  }
+}
+
 // Zero V: the strictly lower part of the diagonal tiles (i,i) and every tile
 // (k,i), k > i, of the first min(MT, NT) tile columns.
 __global__ void k_zero_reflectors(double* A, long M, long N, int NB) {
@@ -342,6 +357,48 @@ void transpose_tiles(double* dQ, long N, int NB, cudaStream_t s) {
   const int nb = (int)(N / 32);
   k_transpose_tiles<<<dim3(nb, nb), dim3(32, 8), 0, s>>>(dQ, N, NB);
 }
+// Device address of host array h[0, n) when all of it is page-locked memory
+// mapped into the device's address space, else null (pageable memory).
+static double* mapped_range(const double* h, size_t n) {
+  if (!h || n == 0) return nullptr;
+  cudaPointerAttributes a{}, b{};
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess || a.type != cudaMemoryTypeHost || !a.devicePointer) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (cudaPointerGetAttributes(&b, h + (n - 1)) != cudaSuccess || b.type != cudaMemoryTypeHost ||
+      static_cast<double*>(b.devicePointer) != static_cast<double*>(a.devicePointer) + (n - 1)) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return static_cast<double*>(a.devicePointer);
+}
+
+static int copy_blocks() {
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return 4 * nsm;
+}
+
+static int aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0 ? 1 : 0; }
+
+cudaError_t copy_host_to_device(double* d, const double* h, size_t n, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  double* m = mapped_range(h, n);
+  if (!m) return cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, s);
+  k_copy_stream<<<copy_blocks(), 256, 0, s>>>(d, m, n, aligned16(d) & aligned16(m));
+  return cudaGetLastError();
+}
+
+cudaError_t copy_device_to_host(double* h, const double* d, size_t n, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  double* m = mapped_range(h, n);
+  if (!m) return cudaMemcpyAsync(h, d, n * sizeof(double), cudaMemcpyDeviceToHost, s);
+  k_copy_stream<<<copy_blocks(), 256, 0, s>>>(m, d, n, aligned16(d) & aligned16(m));
+  return cudaGetLastError();
+}
+
 void zero_reflectors(double* dA, long M, long N, int NB, cudaStream_t s) {
   k_zero_reflectors<<<grid_for((size_t)M * N), 256, 0, s>>>(dA, M, N, NB);
 }

@@ -221,6 +221,14 @@ int hqr_tiles_to_colmajor_padded(long M, long N, long ld, int NB, const double *
  * NB = 128; same slicing, tensor-core products and recombination as
  * the HQR_PREC_OZAKI updates.  Synchronous. */
 int hqr_ozaki_product(int NB, const double *dX, const double *dY, double *dC, void *stream);
+/* No counterpart in the reference (its driver mallocs its arrays).  Page-locked
+ * host memory (cudaHostAlloc) for the arrays given to the drop-in calls: their
+ * host<->device copies then run at the link's full rate, on every call (they
+ * are made by SM loads and stores through the arrays' device mapping).
+ * Pageable memory works as well (cudaMemcpyAsync); so does memory the caller
+ * locked by other means.  Free with hqr_host_free. */
+int hqr_host_alloc(void **ptr, size_t bytes);
+int hqr_host_free(void *ptr);
 /* No counterpart in the reference: where the time of the last drop-in call
  * (Hybrid_tile_QR, Hybrid_make_Q, Hybrid_dorgqr, Hybrid_dormqr) went, in
  * milliseconds, from CUDA events on its stream: out[0] host-to-device copies,
