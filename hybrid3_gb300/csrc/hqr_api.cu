@@ -165,13 +165,17 @@ int build_qt(hqr_plan* plan, double* dQ, const double* dRY, const double* dTAU, 
     return hqr::launch_apply_qt_tree(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g.NT, g_timeout_ns, s,
                                      &plan->oz, &plan->tree);
   }
-  if (rebuild_t) plan->factors_valid = 0;
   if (g.M == g.N && g.NB % 32 == 0) {
+    // backward accumulation applies H, not H^T: the split precisions prepare
+    // [T V^T | T] for it (the factorization prepared [T^T V^T | T^T])
+    const bool rb = rebuild_t || plan->oz.slices != nullptr;
+    if (rb) plan->factors_valid = 0;
     hqr::make_identity(dQ, g.M, g.N, g.NB, true, s);
-    TRY(hqr::launch_build_q(g, &plan->ws, dRY, plan->dT, dTAU, dQ, rebuild_t, g_timeout_ns, s, &plan->oz));
+    TRY(hqr::launch_build_q(g, &plan->ws, dRY, plan->dT, dTAU, dQ, rb, g_timeout_ns, s, &plan->oz));
     hqr::transpose_tiles(dQ, g.N, g.NB, s);
     return cuda_rc(cudaGetLastError());
   }
+  if (rebuild_t) plan->factors_valid = 0;
   hqr::make_identity(dQ, g.M, g.N, g.NB, false, s);
   return hqr::launch_apply_qt(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g.NT, rebuild_t, g_timeout_ns, s,
                               &plan->oz);

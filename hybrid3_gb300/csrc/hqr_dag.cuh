@@ -781,16 +781,14 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
         if (threadIdx.x == 0) atomicOr((int*)(q.ctl + kErr), kErrBadTask);
     }
     if (ts_a1) task_tsqrt_blk(ts_a1, ts_a2, ts_t, ts_tau, q.sh, smem, q.sp, t.c, ts_upper);
-    // the factorization's preparations also keep T for Q generation
+    // Q generation applies H (M = T), the other modes H^T (M = T^T)
     if (OZ && prep_v)
       task_ozprep(prep_v, prep_tau, prep_g, prep_kind, prep_slices, prep_exps, reinterpret_cast<uint8_t*>(smem),
-                  s_tmem, q.ctl + kErr, q.mode != kModeBuildQ, q.mode == kModeFactor && t.type == kOZPREP);
+                  s_tmem, q.ctl + kErr, q.mode != kModeBuildQ);
     if (OZ && oz_bot) {
       oz::Ctx c;
       oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, q.ctl + kErr);
-      // Q generation on the factorization's slices takes T from its own slot
-      task_ozapply<OZG>(c, oz_slices, oz_exps, oz_top, oz_bot,
-                        (q.mode == kModeBuildQ && q.skip_panels) ? (int)kOzT : (int)kOzTT);
+      task_ozapply<OZG>(c, oz_slices, oz_exps, oz_top, oz_bot);
     }
     fence_acq_rel_gpu();   // release: this task's writes before its dependents' counters
     __syncthreads();

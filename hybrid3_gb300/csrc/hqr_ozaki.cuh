@@ -132,6 +132,12 @@ __device__ __forceinline__ void tma_load_1d(void* dst_smem, const void* src_gmem
       "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar))
       : "memory");
 }
+// 16-byte asynchronous global -> shared copies (L2 only), all in flight
+// until cp_async_wait_all.
+__device__ __forceinline__ void cp_async16(void* dst_smem, const void* src_gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst_smem)), "l"(src_gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
@@ -328,8 +334,9 @@ __device__ __forceinline__ void set_err(const Ctx& c) {
 }
 
 // Column exponents (max biased exponent) of the staged right operand into
-// sEb[c.yb].
-__device__ __forceinline__ void y_exponents(Ctx& c) {
+// sEb[c.yb]; with Y2 (shared, kK x kN, ld kK) the exponents span both, for a
+// right operand whose second half is reloaded into sY during the product.
+__device__ __forceinline__ void y_exponents(Ctx& c, const double* Y2 = nullptr) {
   constexpr int kTPC = kThreads / kN;   // threads per column
   static_assert(kTPC >= 1 && kTPC <= 32 && (kTPC & (kTPC - 1)) == 0, "column split");
   const int col = threadIdx.x / kTPC, part = threadIdx.x % kTPC;
@@ -337,6 +344,11 @@ __device__ __forceinline__ void y_exponents(Ctx& c) {
   const double* y = c.sY + col * kLdY;
 #pragma unroll 4
   for (int r = part; r < kK; r += kTPC) e = max(e, biased_exp(y[r]));
+  if (Y2) {
+    const double* y2 = Y2 + (size_t)col * kK;
+#pragma unroll 4
+    for (int r = part; r < kK; r += kTPC) e = max(e, biased_exp(y2[r]));
+  }
 #pragma unroll
   for (int o = 1; o < kTPC; o <<= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
   if (part == 0) c.sEb[c.yb * kN + col] = e;
@@ -347,8 +359,31 @@ __device__ __forceinline__ void y_exponents(Ctx& c) {
 // shared memory.  col0 >= 0: Y is the column block starting at column col0 of
 // a unit-lower V (zero above the diagonal, one on it), or with `upper` of an
 // upper-triangular V (zero below the diagonal).
-__device__ __forceinline__ void stage_y(Ctx& c, const double* Y, int ldy, int col0, bool upper = false) {
+// A kK x kN column block (global, column stride ld doubles, 16-byte aligned
+// columns) into shared memory at dst (column stride ldd) with asynchronous
+// copies issued by threads t0, t0 + nt, ... (not waited for).
+__device__ __forceinline__ void cp_async_block(double* dst, int ldd, const double* src, int ld, int t0, int nt) {
+  for (int e = t0; e < kK * kN / 2; e += nt) {
+    const int col = e / (kK / 2), r = 2 * (e % (kK / 2));
+    cp_async16(dst + col * ldd + r, src + (size_t)col * ld + r);
+  }
+}
+
+__device__ __forceinline__ void stage_y(Ctx& c, const double* Y, int ldy, int col0, bool upper = false,
+                                        const double* Yjoint = nullptr) {
   static_assert(kK * kN / 2 % kThreads == 0, "staging loop");
+  static_assert(kBStages * kBChunkBytes == kK * kN * 8, "the B ring holds one column block");
+  if (col0 < 0) {
+    // unmasked: every copy in flight at once; Yjoint (ld kK) goes to the B
+    // ring, idle until the product starts, for its column exponents
+    cp_async_block(c.sY, kLdY, Y, ldy, threadIdx.x, kThreads);
+    double* sJ = reinterpret_cast<double*>(c.sB);
+    if (Yjoint) cp_async_block(sJ, kK, Yjoint, kK, threadIdx.x, kThreads);
+    cp_async_wait_all();
+    __syncthreads();
+    y_exponents(c, Yjoint ? sJ : nullptr);
+    return;
+  }
   constexpr int kIter = kK * kN / 2 / kThreads;   // pairs per thread
 #pragma unroll 4
   for (int it = 0; it < kIter; it++) {
@@ -366,6 +401,35 @@ __device__ __forceinline__ void stage_y(Ctx& c, const double* Y, int ldy, int co
       }
     }
     *reinterpret_cast<double2*>(c.sY + col * kLdY + r) = v;
+  }
+  __syncthreads();
+  y_exponents(c, Yjoint);
+}
+
+// Element masks of a panel tile's reflectors V (row i, column j of the tile).
+enum Kind : int {
+  kDense = 0,
+  kUnitLower = 1,    // V of a GEQRT tile: zero above the diagonal, one on it
+  kUnitUpper = 2,    // V^T of a GEQRT tile
+  kUpperIncl = 3,    // V of a TT merge: upper triangle with the diagonal, zero below
+  kLowerIncl = 4,    // V^T of a TT merge
+};
+__device__ __forceinline__ double mask_v(double v, int i, int j, int kind) {
+  if (kind == kUnitLower) return (i > j) ? v : (i == j ? 1.0 : 0.0);
+  if (kind == kUpperIncl) return (i <= j) ? v : 0.0;
+  return v;
+}
+
+// Stage the column block col0.. of V^T as the right operand: Y(r, cc) =
+// V(col0 + cc, r), V a 128 x 128 tile (global, ld kK) with mask `kind`.
+__device__ __forceinline__ void stage_yt(Ctx& c, const double* V, int col0, int kind) {
+  constexpr int kIter = kK * kN / kThreads;
+#pragma unroll 4
+  for (int it = 0; it < kIter; it++) {
+    const int e = threadIdx.x + it * kThreads;
+    const int cc = e % kN, r = e / kN;   // consecutive threads read consecutive rows of V's column r
+    const int i = col0 + cc;
+    c.sY[cc * kLdY + r] = mask_v(__ldcg(V + (size_t)i + (size_t)r * kK), i, r, kind);
   }
   __syncthreads();
   y_exponents(c);
@@ -421,15 +485,24 @@ __device__ __forceinline__ void prefetch(Ctx& c, const uint8_t* X) {
   }
 }
 
+// Barrier among the slicer warps only (warp 0 keeps issuing MMAs).
+__device__ __forceinline__ void slicer_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kSlicerWarps * 32) : "memory");
+}
+
 // The 8 t-group accumulators of X (prepared slices) times the staged right
 // operand; Xnext (or nullptr): the left operand of the next product, whose
 // first chunks are fetched as soon as their stages are free.  Warp 0, one
 // thread: bulk copies of A and the MMAs; warps 1..7: slicing of B, up to
 // kBStages chunks ahead of the MMAs.  On return (true) the accumulators are
 // final in TMEM.  G < 8: only the pairs of weight p + q < G (accumulators
-// 0..G-1; the others are left as they are).
+// 0..G-1; the others are left as they are).  nch: K chunks (8, or 16 for a
+// K = 256 product whose right operand's second half, `reload` (global, kK x
+// kN, ld kK), replaces the staged one once the slicers are past chunk 7; the
+// column exponents must already span both halves).
 template <int G = kGroups>
-inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
+inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext, int nch = kChunks,
+                            const double* reload = nullptr) {
   static_assert(G >= 1 && G <= kGroups, "t-groups");
   const int n0 = c.n;
   bool ok = true;
@@ -442,7 +515,7 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
       fence_proxy_async_global();
       // chunks of this product not prefetched yet (stages free: every earlier MMA is done)
       for (; c.na < n0 + kAStages; c.na++) issue_a<G>(c, X, c.na - n0, c.na);
-      for (int j = 0; j < kChunks && ok; j++) {
+      for (int j = 0; j < nch && ok; j++) {
         const int n = n0 + j;
         if (!wait_chunk(c, kBarAFull, kAStages, n) || !wait_chunk(c, kBarBFull, kBStages, n)) {
           ok = false;
@@ -465,7 +538,7 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
         }
         mma_commit(c.bar + kBarDone + n % kDoneStages);
         // refill the A stage of chunk n - 1 with chunk n - 1 + kAStages once its MMAs are done
-        if (j >= 1 && j + kAStages - 1 < kChunks) {
+        if (j >= 1 && j + kAStages - 1 < nch) {
           if (!wait_chunk(c, kBarDone, kDoneStages, n - 1)) {
             ok = false;
             break;
@@ -477,38 +550,49 @@ inline __device__ bool gemm(Ctx& c, const uint8_t* X, const uint8_t* Xnext) {
       // prefetch the next product's first chunks into the stages of the last kAStages
       if (ok && Xnext) {
         for (int j = 0; j < kAStages; j++) {
-          if (!wait_chunk(c, kBarDone, kDoneStages, n0 + kChunks - kAStages + j)) {
+          if (!wait_chunk(c, kBarDone, kDoneStages, n0 + nch - kAStages + j)) {
             ok = false;
             break;
           }
-          issue_a<G>(c, Xnext, j, n0 + kChunks + j);
+          issue_a<G>(c, Xnext, j, n0 + nch + j);
         }
-        if (ok) c.na = n0 + kChunks + kAStages;
+        if (ok) c.na = n0 + nch + kAStages;
       }
     }
     __syncwarp();
   } else {
-    // slicer thread ts owns quads ts, ts + 224, ... of the product's 8 x 256
+    // slicer thread ts owns quads ts, ts + 224, ... of the product's nch x 256;
+    // every slicer thread passes every loop step and the reload barriers, so
+    // a failed wait (ok false, warp-uniform) skips work but never a barrier
     const int ts = threadIdx.x - 32;
     constexpr int kStride = kSlicerWarps * 32;
     int g = ts;
-    for (int j = 0; j < kChunks && ok; j++) {
+    for (int j = 0; j < nch; j++) {
       const int n = n0 + j;
-      if (n >= kBStages && !wait_chunk(c, kBarDone, kDoneStages, n - kBStages)) {
-        ok = false;
-        break;
+      if (ok && n >= kBStages && !wait_chunk(c, kBarDone, kDoneStages, n - kBStages)) ok = false;
+      ok = __all_sync(0xffffffffu, ok);
+      if (reload && j == kChunks) {
+        // the second half of the right operand: every slicer is past chunk 7
+        slicer_sync();
+        if (ok) {
+          cp_async_block(c.sY, kLdY, reload, kK, ts, kStride);
+          cp_async_wait_all();
+        }
+        slicer_sync();
       }
-      uint8_t* stage = c.sB + (n % kBStages) * kBChunkBytes;
-      for (; g < (j + 1) * 256; g += kStride) slice_b_quad<G>(c, stage, g & 255, j * kKC);
-      fence_proxy_async();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(c.bar + kBarBFull + n % kBStages);
+      if (ok) {
+        uint8_t* stage = c.sB + (n % kBStages) * kBChunkBytes;
+        for (; g < (j + 1) * 256; g += kStride) slice_b_quad<G>(c, stage, g & 255, (j % kChunks) * kKC);
+        fence_proxy_async();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(c.bar + kBarBFull + n % kBStages);
+      }
     }
   }
   // every thread: the last chunk's MMAs (and with them all earlier ones) are done
-  if (ok && !wait_chunk(c, kBarDone, kDoneStages, n0 + kChunks - 1)) ok = false;
+  if (ok && !wait_chunk(c, kBarDone, kDoneStages, n0 + nch - 1)) ok = false;
   tc_fence_after();
-  c.n = n0 + kChunks;
+  c.n = n0 + nch;
   ok = __syncthreads_and(ok) != 0;   // uniform across the CTA
   if (!ok && threadIdx.x == 0) set_err(c);
   return ok;
@@ -650,8 +734,9 @@ inline __device__ void drain(Ctx& c, const int* Ea, int mode, double* g, int ldg
 // about 2^-30 of rowmax * colmax * K).
 template <int G = kGroups>
 inline __device__ bool product(Ctx& c, const uint8_t* Xprep, const uint8_t* Xnext, const int* Ea,
-                               int mode, double* g, int ldg, double* gm, int ldm) {
-  if (!gemm<G>(c, Xprep, Xnext)) return false;
+                               int mode, double* g, int ldg, double* gm, int ldm, int nch = kChunks,
+                               const double* reload = nullptr) {
+  if (!gemm<G>(c, Xprep, Xnext, nch, reload)) return false;
   drain<G>(c, Ea, mode, g, ldg, gm, ldm);
   return true;
 }
@@ -659,31 +744,13 @@ inline __device__ bool product(Ctx& c, const uint8_t* Xprep, const uint8_t* Xnex
 // ---------------------------------------------------------------------------
 // Preparation of a left operand (once per panel tile)
 // ---------------------------------------------------------------------------
-// Element masks of the panel tile's operands.
-enum Kind : int {
-  kDense = 0,
-  kUnitLower = 1,    // V of a GEQRT tile: zero above the diagonal, one on it
-  kUnitUpper = 2,    // V^T of a GEQRT tile
-  kUpperIncl = 3,    // V of a TT merge: upper triangle with the diagonal, zero below
-  kLowerIncl = 4,    // V^T of a TT merge
-};
-
-// Slice the 128 x 128 left operand X(r, k) = acc(r, k) (shared memory) into
-// the [kc][slice][core layout] order at dst (global) and write its row
-// exponents to Ea (global); sE: 128 ints of shared scratch.
+// Columns k < kcount of X(r, k) = acc(r, k) (kcount a multiple of kKC) into
+// dst in the [kc][slice][core layout] order, with the row exponents sE
+// (shared) already known.
 template <class Acc>
-inline __device__ void slice_left(const Acc& acc, uint8_t* dst, int* Ea, int* sE) {
-  if (threadIdx.x < kK) {
-    const int r = threadIdx.x;
-    int e = 0;
-#pragma unroll 8
-    for (int k = 0; k < kK; k++) e = max(e, biased_exp(acc(r, k)));
-    sE[r] = e;
-    Ea[r] = e;
-  }
-  __syncthreads();
-  constexpr int kQuads = kK * kK / 4;
-  for (int qd = threadIdx.x; qd < kQuads; qd += kThreads) {
+inline __device__ void slice_cols(const Acc& acc, uint8_t* dst, const int* sE, int kcount) {
+  const int quads = kK * kcount / 4;
+  for (int qd = threadIdx.x; qd < quads; qd += kThreads) {
     const int r = qd % kK;
     const int k4 = (qd / kK) * 4;
     const int E = sE[r];
@@ -703,6 +770,29 @@ inline __device__ void slice_left(const Acc& acc, uint8_t* dst, int* Ea, int* sE
   fence_proxy_async_global();
   __syncthreads();
 }
+
+// Slice the 128 x 128 left operand X(r, k) = acc(r, k) into the
+// [kc][slice][core layout] order at dst (global) and write its row exponents
+// to Ea (global); sE: 128 ints of shared scratch.
+template <class Acc>
+inline __device__ void slice_left(const Acc& acc, uint8_t* dst, int* Ea, int* sE) {
+  if (threadIdx.x < kK) {
+    const int r = threadIdx.x;
+    int e = 0;
+#pragma unroll 8
+    for (int k = 0; k < kK; k++) e = max(e, biased_exp(acc(r, k)));
+    sE[r] = e;
+    Ea[r] = e;
+  }
+  __syncthreads();
+  slice_cols(acc, dst, sE, kK);
+}
+
+// A 128 x 128 column-major matrix in global memory (ld kK) as a left operand.
+struct GlobalAcc {
+  const double* g;
+  __device__ __forceinline__ double operator()(int r, int k) const { return __ldcg(g + r + (size_t)k * kK); }
+};
 
 // Accessor of a 128 x 128 column-major matrix S staged in shared memory with
 // leading dimension kLdT: X = S or X = S^T, with an element mask.

@@ -1,24 +1,32 @@
 // hqr_oztasks.cuh -- tile tasks of the split-precision path (NB = 128).
 //
-//   OZPREP(i,k): the sliced left operands V^T, T^T and V of panel tile (k,i),
-//     with the full NB x NB upper T of the tile (LAPACK dlarft, forward,
-//     columnwise, from V and TAU -- the rebuild Hybrid_make_Q does with
-//     IB = NB, Hybrid_make_Q.c:124-130,159-163).  G = V^T V runs on the tensor
-//     cores (two products); the T recurrence runs in shared memory.
-//   OZAPPLY: one 64-column block of a LARFB (CORE_dormqr, V unit lower) or
-//     SSRFB (CORE_dtsmqr, V dense) as three products:
-//       W = C_top + V^T C_bot;  W2 = T^T W;  C_top -= W2;  C_bot -= V W2,
-//     with W and W2 kept in shared memory between the products.
+// A block reflector H = I - [I; V] T [I; V]^T applied as H^T (the
+// factorization, Q^T C; CORE_dtsmqr / CORE_dormqr) or as H (Q generation)
+// to a column block [C_top; C_bot] needs W2 = M (C_top + V^T C_bot), M = T^T
+// or T, then C_top -= W2 and C_bot -= V W2.  With Z = M V^T prepared once per
+// panel tile, W2 = Z C_bot + M C_top is ONE product of K = 256:
+//
+//   OZPREP(i,k): T from V and TAU (LAPACK dlarft, forward, columnwise -- the
+//     full NB x NB T Hybrid_make_Q rebuilds with IB = NB,
+//     Hybrid_make_Q.c:124-130,159-163; G = V^T V on the tensor cores, the
+//     recurrence in shared memory), Z = M V^T on the tensor cores, and the
+//     sliced left operands X1 = [Z | M] (128 x 256, one row exponent per row
+//     over both halves) and V.
+//   OZAPPLY: one 64-column block of an SSRFB (V dense) or LARFB (V unit
+//     lower, no C_top) as two products:
+//       W2 = [Z | M] [C_bot; C_top]   (LARFB: Z C)  -> C_top -= W2
+//       C_bot -= V W2,
+//     with W2 kept in shared memory between them: two epilogues per task.
 #pragma once
 #include "hqr_ozaki.cuh"
 
 namespace hqr {
 
-// Slots of a panel tile's prepared operands (and of their row exponents):
-// V^T, the middle operand (T^T, or T where the preparation applies H itself),
-// V, and -- written by the factorization's preparation only -- T, so that Q
-// generation (which applies H, not H^T) can reuse the factorization's slices.
-constexpr size_t kOzVT = 0, kOzTT = 1, kOzV = 2, kOzT = 3;
+// Slots of a panel tile's prepared operands (operand_bytes() each) and of
+// their row exponents (kK ints each): X1 = [Z | M] (slots 0-1: 16 K chunks,
+// one exponent per row in slot 0), V (slot 2), and slot 3, scratch of the
+// preparation (V^T, then M with its own exponents).
+constexpr size_t kOzX = 0, kOzV = 2, kOzS = 3;
 
 // T upper triangular, packed by columns in shared memory: T(a, b) (a <= b)
 // at b (b + 1) / 2 + a.  As a left operand: X = T^T (transposed) or X = T.
@@ -92,35 +100,41 @@ enum VKind : int {
   kVUpper = 2,       // TT merge: the upper triangle with the diagonal
 };
 
-// OZPREP of panel tile V (global, NB x NB, of shape vkind) with TAU tau.  G: NB x NB global scratch.
-// slices / exps: this tile's prepared operands and row exponents; the middle
-// operand is T^T (applying H^T) or, with t_transposed false, T (applying H);
-// with also_t, T goes to slot kOzT as well.  sm: the CTA's dynamic shared
-// memory (oz::kSmemBytes).  False on a device time-out.
+// OZPREP of panel tile V (global, NB x NB, of shape vkind) with TAU tau.
+// G: NB x NB global scratch (it ends holding M).  slices / exps: this tile's
+// prepared operands and row exponents; M = T^T (applying H^T) or, with
+// t_transposed false, T (applying H).  sm: the CTA's dynamic shared memory
+// (oz::kSmemBytes).  False on a device time-out.
 inline __device__ bool task_ozprep(const double* V, const double* tau, double* G, int vkind,
                                    uint8_t* slices, int* exps, uint8_t* sm, uint32_t tmem,
-                                   unsigned* err, bool t_transposed, bool also_t) {
+                                   unsigned* err, bool t_transposed) {
   using namespace oz;
   constexpr size_t ob = operand_bytes();
-  // 1. V^T and V from a shared-memory copy of the tile
+  uint8_t* X1 = slices + kOzX * ob;
+  uint8_t* XV = slices + kOzV * ob;
+  uint8_t* XS = slices + kOzS * ob;
+  // Z (FP64, ld kK) waits in X1's last 4 chunks until X1 is sliced
+  double* Zs = reinterpret_cast<double*>(X1 + 12 * (size_t)kAChunkBytes);
+  static_assert(12 * kAChunkBytes + kK * kK * 8 == 2 * operand_bytes(), "Z scratch");
+  const int kv = vkind == kVUnitLower ? kUnitLower : vkind == kVUpper ? kUpperIncl : kDense;
+  // 1. V^T (scratch) and V from a shared-memory copy of the tile
   {
     double* sV = reinterpret_cast<double*>(sm);
     int* sE = reinterpret_cast<int*>(sm + kLdT * kK * 8);
     stage_tile(sV, V);
     const int kt = vkind == kVUnitLower ? kUnitUpper : vkind == kVUpper ? kLowerIncl : kDense;
-    const int kv = vkind == kVUnitLower ? kUnitLower : vkind == kVUpper ? kUpperIncl : kDense;
-    slice_left(StagedAcc{sV, kLdT, 1, kt}, slices + kOzVT * ob, exps + kOzVT * kK, sE);
-    slice_left(StagedAcc{sV, 1, kLdT, kv}, slices + kOzV * ob, exps + kOzV * kK, sE);
+    slice_left(StagedAcc{sV, kLdT, 1, kt}, XS, exps + kOzS * kK, sE);
+    slice_left(StagedAcc{sV, 1, kLdT, kv}, XV, exps + kOzV * kK, sE);
   }
   // 2. G = V^T V on the tensor cores, by 64-column blocks, into G (global)
   {
     Ctx c;
     ctx_init(c, sm, tmem, err);
     for (int cb = 0; cb < kK / kN; cb++) {
-      prefetch(c, slices + kOzVT * ob);
+      prefetch(c, XS);
       stage_y(c, V + (size_t)cb * kN * kK, kK, vkind == kVDense ? -1 : cb * kN, vkind == kVUpper);
-      if (!product(c, slices + kOzVT * ob, (cb + 1 < kK / kN) ? slices + kOzVT * ob : nullptr,
-                   exps + kOzVT * kK, kEpiStore, G + (size_t)cb * kN * kK, kK, nullptr, 0))
+      if (!product(c, XS, (cb + 1 < kK / kN) ? XS : nullptr, exps + kOzS * kK, kEpiStore,
+                   G + (size_t)cb * kN * kK, kK, nullptr, 0))
         return false;
     }
     ctx_release(c);
@@ -144,32 +158,69 @@ inline __device__ bool task_ozprep(const double* V, const double* tau, double* G
   }
   __syncthreads();
   t_recurrence(sG, sT, sX, tau);
-  // 4. T^T or T (and T)
-  slice_left(PackedTAcc{sT, t_transposed}, slices + kOzTT * ob, exps + kOzTT * kK, sE);
-  if (also_t) slice_left(PackedTAcc{sT, false}, slices + kOzT * ob, exps + kOzT * kK, sE);
+  // 4. M to G (global, its last use of G was above) and sliced with its own
+  //    row exponents into the scratch slot (V^T is not needed any more)
+  {
+    const PackedTAcc m{sT, t_transposed};
+    for (int e = threadIdx.x; e < kK * kK; e += kThreads) stg_cg(G + e, m(e % kK, e / kK));
+    slice_left(m, XS, exps + kOzS * kK, sE);
+  }
+  // 5. Z = M V^T on the tensor cores, into Zs
+  {
+    Ctx c;
+    ctx_init(c, sm, tmem, err);
+    for (int cb = 0; cb < kK / kN; cb++) {
+      prefetch(c, XS);
+      stage_yt(c, V, cb * kN, kv);
+      if (!product(c, XS, (cb + 1 < kK / kN) ? XS : nullptr, exps + kOzS * kK, kEpiStore,
+                   Zs + (size_t)cb * kN * kK, kK, nullptr, 0))
+        return false;
+    }
+    ctx_release(c);
+  }
+  __threadfence_block();
+  // 6. row exponents of X1 = [Z | M] over both halves
+  //    (threads 0..127 scan Z's rows, threads 128..255 M's)
+  static_assert(kThreads == 2 * kK, "one thread per row and half");
+  int* sE1 = reinterpret_cast<int*>(sm);
+  if (threadIdx.x < kK) sE1[threadIdx.x] = 0;
+  __syncthreads();
+  {
+    const int r = threadIdx.x % kK;
+    const double* src = threadIdx.x < kK ? Zs : G;
+    int e = 0;
+#pragma unroll 8
+    for (int k = 0; k < kK; k++) e = max(e, biased_exp(__ldcg(src + r + (size_t)k * kK)));
+    atomicMax(sE1 + r, e);
+  }
+  __syncthreads();
+  if (threadIdx.x < kK) exps[kOzX * kK + threadIdx.x] = sE1[threadIdx.x];
+  // 7. X1: Z into chunks 0-7 (all of Zs read before chunks 12-15 are written),
+  //    then M into chunks 8-15
+  slice_cols(GlobalAcc{Zs}, X1, sE1, kK);
+  slice_cols(GlobalAcc{G}, X1 + (size_t)kChunks * kAChunkBytes, sE1, kK);
   return true;
 }
 
 // One 64-column block of the update.  Ctop: A1 block (SSRFB) or nullptr
-// (LARFB); Cbot: A2 block (SSRFB) or the C block (LARFB); ld NB.  mid: the
-// slot of the middle operand (kOzTT, or kOzT for Q generation on the
-// factorization's slices).  Returns false on a device time-out (error word
-// already set).  G: t-groups of the three products (8: FP64-level; 4: the
-// reduced form, see oz::product).
+// (LARFB); Cbot: A2 block (SSRFB) or the C block (LARFB); ld NB.  Returns
+// false on a device time-out (error word already set).  G: t-groups of the
+// products (8: FP64-level; 4: the reduced form, see oz::product).
 template <int G = oz::kGroups>
 inline __device__ bool task_ozapply(oz::Ctx& c, const uint8_t* slices, const int* exps, double* Ctop,
-                                    double* Cbot, int mid) {
+                                    double* Cbot) {
   using namespace oz;
   constexpr size_t ob = operand_bytes();
-  prefetch<G>(c, slices + kOzVT * ob);
-  stage_y(c, Cbot, kK, -1);
-  if (!product<G>(c, slices + kOzVT * ob, slices + mid * ob, exps + kOzVT * kK, kEpiToY, nullptr, 0, Ctop, kK))
+  const uint8_t* X1 = slices + kOzX * ob;
+  const uint8_t* XV = slices + kOzV * ob;
+  prefetch<G>(c, X1);
+  // the right operand [C_bot; C_top]: C_bot staged, C_top loaded after chunk 7;
+  // column exponents over both
+  stage_y(c, Cbot, kK, -1, false, Ctop);
+  if (!product<G>(c, X1, XV, exps + kOzX * kK, kEpiToYSubTop, nullptr, 0, Ctop, kK,
+                  Ctop ? 2 * kChunks : kChunks, Ctop))
     return false;
-  if (!product<G>(c, slices + mid * ob, slices + kOzV * ob, exps + mid * kK, kEpiToYSubTop, nullptr, 0, Ctop,
-                  kK))
-    return false;
-  if (!product<G>(c, slices + kOzV * ob, nullptr, exps + kOzV * kK, kEpiSubInto, Cbot, kK, nullptr, 0))
-    return false;
+  if (!product<G>(c, XV, nullptr, exps + kOzV * kK, kEpiSubInto, Cbot, kK, nullptr, 0)) return false;
   ctx_release(c);
   return true;
 }

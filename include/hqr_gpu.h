@@ -126,7 +126,9 @@ int hqr_plan_stats(hqr_plan_t *plan, hqr_stats_t *out, void *stream);
  * reflectors (use_plan_t = 0 here or in hqr_ormqr_t, or a drop-in Hybrid_*
  * call), they are rebuilt from dRY and dTAU instead.  use_plan_t = 0: always
  * rebuilt from dRY and dTAU (any reflectors in this plan's shape), replacing
- * the plan's. */
+ * the plan's.  Square Q generation with a split precision applies H itself,
+ * not H^T, so it always prepares its own operands ([T V^T | T] where the
+ * factorization and Q^T C use [T^T V^T | T^T]). */
 int hqr_make_q(hqr_plan_t *plan, double *dQ, double *dRY, const double *dTAU, int use_plan_t,
                void *stream);
 int hqr_make_q_async(hqr_plan_t *plan, double *dQ, double *dRY, const double *dTAU,

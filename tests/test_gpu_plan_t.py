@@ -1,8 +1,9 @@
-"""use_plan_t of hqr_make_q / hqr_ormqr_t: after hqr_geqrf on a plan, Q
-generation and Q^T C reuse the factorization's T factors (FP64) or prepared
-operands (split precision) -- no panel task runs -- and give the oracle's
-results; once a call has rebuilt them from other reflectors, use_plan_t = 1
-rebuilds again instead of using stale ones.
+"""use_plan_t of hqr_make_q / hqr_ormqr_t: after hqr_geqrf on a plan, Q^T C
+reuses the factorization's T factors (FP64) or prepared operands (split
+precision) -- no panel task runs -- and so does Q generation in FP64; split
+Q generation applies H, not H^T, and prepares its own operands.  Results are
+the oracle's; once a call has rebuilt the plan's factors from other
+reflectors, use_plan_t = 1 rebuilds again instead of using stale ones.
 
 Elementwise bar as in the other parity tests: n * eps * ||A||_F for Q, 4x that
 of ||C||_F for Q^T C.
@@ -62,16 +63,17 @@ def test_q_from_the_plans_factors(env, NB, IB, prec):
                 "ormqr")
         return dC.cpu().numpy(), plan.stats()
 
-    # reuse: no panel tasks
-    q, st = make_q(1)
-    assert st["count"][panel_slot] == 0
-    assert np.abs(q - oq).max() <= tol(A2d)
+    panels = (M // NB) * (M // NB + 1) // 2
+    # reuse: no panel tasks for Q^T C; Q generation too in FP64
     c, st = ormqr(1)
     assert st["count"][panel_slot] == 0
     assert np.abs(c - oc).max() <= 4 * tol(C2d)
+    q, st = make_q(1)
+    assert st["count"][panel_slot] == (panels if prec else 0)
+    assert np.abs(q - oq).max() <= tol(A2d)
     # a rebuild replaces the plan's factors; use_plan_t = 1 then rebuilds too
     q, st = make_q(0)
-    assert st["count"][panel_slot] == (M // NB) * (M // NB + 1) // 2
+    assert st["count"][panel_slot] == panels
     assert np.abs(q - oq).max() <= tol(A2d)
     c, st = ormqr(1)
     assert st["count"][panel_slot] > 0
@@ -79,7 +81,7 @@ def test_q_from_the_plans_factors(env, NB, IB, prec):
     # a new factorization makes them reusable again
     dA.copy_(torch.from_numpy(A.copy()))
     H.check(L.hqr_geqrf(plan.h, dA.data_ptr(), dTAU.data_ptr(), None), "geqrf")
-    q, st = make_q(1)
+    c, st = ormqr(1)
     assert st["count"][panel_slot] == 0
-    assert np.abs(q - oq).max() <= tol(A2d)
+    assert np.abs(c - oc).max() <= 4 * tol(C2d)
     plan.close()
