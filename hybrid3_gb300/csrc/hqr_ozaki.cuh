@@ -337,21 +337,26 @@ __device__ __forceinline__ void set_err(const Ctx& c) {
 // sEb[c.yb]; with Y2 (shared, kK x kN, ld kK) the exponents span both, for a
 // right operand whose second half is reloaded into sY during the product.
 __device__ __forceinline__ void y_exponents(Ctx& c, const double* Y2 = nullptr) {
-  constexpr int kTPC = kThreads / kN;   // threads per column
-  static_assert(kTPC >= 1 && kTPC <= 32 && (kTPC & (kTPC - 1)) == 0, "column split");
-  const int col = threadIdx.x / kTPC, part = threadIdx.x % kTPC;
-  int e = 0;
-  const double* y = c.sY + col * kLdY;
-#pragma unroll 4
-  for (int r = part; r < kK; r += kTPC) e = max(e, biased_exp(y[r]));
-  if (Y2) {
-    const double* y2 = Y2 + (size_t)col * kK;
-#pragma unroll 4
-    for (int r = part; r < kK; r += kTPC) e = max(e, biased_exp(y2[r]));
-  }
+  // warp w takes columns w * kColsW ..; its lanes read consecutive rows
+  // (conflict-free), one warp max-reduction per column
+  constexpr int kColsW = kN / kWarps;
+  static_assert(kColsW * kWarps == kN, "columns per warp");
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll 2
+  for (int cc = 0; cc < kColsW; cc++) {
+    const int col = w * kColsW + cc;
+    const double* y = c.sY + col * kLdY;
+    int e = 0;
 #pragma unroll
-  for (int o = 1; o < kTPC; o <<= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
-  if (part == 0) c.sEb[c.yb * kN + col] = e;
+    for (int r = lane; r < kK; r += 32) e = max(e, biased_exp(y[r]));
+    if (Y2) {
+      const double* y2 = Y2 + col * kK;
+#pragma unroll
+      for (int r = lane; r < kK; r += 32) e = max(e, biased_exp(y2[r]));
+    }
+    e = (int)__reduce_max_sync(0xffffffffu, (unsigned)e);
+    if (lane == 0) c.sEb[c.yb * kN + col] = e;
+  }
   __syncthreads();
 }
 
