@@ -107,6 +107,7 @@ SIGNATURES = {
     "hqr_make_q_async": (_I, [_vp, _vp, _vp, _vp, _I, _vp]),
     "hqr_ormqr_t": (_I, [_vp, _vp, _vp, _vp, _I, _I, _vp]),
     "hqr_lstsq": (_I, [_vp, _vp, _vp, _I, _I, _vp, _I, _I, _vp, _vp]),
+    "hqr_lstsq_aug": (_I, [_vp, _vp, _vp, _I, _I, _vp, _I, _I, _vp, _vp]),
     "hqr_plan_set_tree": (_I, [_vp, _I]),
     "hqr_colmajor_to_tiles_padded": (_I, [_L, _L, _L, _I, _vp, _vp, _vp]),
     "hqr_tiles_to_colmajor_padded": (_I, [_L, _L, _L, _I, _vp, _vp, _vp]),
@@ -132,6 +133,8 @@ SIGNATURES = {
     "hqr_fp64_mma_peak_tflops": (_D, [_I, _vp]),
     "hqr_dropin_phase_ms": (_I, [ctypes.POINTER(ctypes.c_double)]),
     "hqr_host_alloc": (_I, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]),
+    "hqr_ormqr_n": (_I, [_vp, _vp, _vp, _vp, _I, _I, _vp]),
+    "hqr_ormqr_n_async": (_I, [_vp, _vp, _vp, _vp, _I, _I, _vp]),
     "hqr_host_free": (_I, [_vp]),
     "hqr_ozaki_product": (_I, [_I, _vp, _vp, _vp, _vp]),
     # include/tile_kernel.h (pointer arguments: host or device addresses)
@@ -211,12 +214,14 @@ class Plan:
         """Domain tree of domain_tiles tiles for the factorizations on this plan (0: flat)."""
         check(lib().hqr_plan_set_tree(self.h, domain_tiles), "hqr_plan_set_tree")
 
-    def lstsq(self, dA, dB, nrhs, dX, refine_steps=1, ldb=None, ldx=None, stream=None):
-        """hqr_lstsq on device addresses (tile-layout A of this plan's shape,
-        column-major B and X); returns ||b - A x||_2 per right-hand side."""
+    def lstsq(self, dA, dB, nrhs, dX, refine_steps=1, ldb=None, ldx=None, stream=None, augmented=False):
+        """hqr_lstsq (hqr_lstsq_aug with augmented=True) on device addresses
+        (tile-layout A of this plan's shape, column-major B and X); returns
+        ||b - A x||_2 per right-hand side."""
         res = (ctypes.c_double * nrhs)()
-        check(lib().hqr_lstsq(self.h, dA, dB, ldb or self.M, nrhs, dX, ldx or self.N, refine_steps,
-                              res, stream), "hqr_lstsq")
+        fn = lib().hqr_lstsq_aug if augmented else lib().hqr_lstsq
+        name = "hqr_lstsq_aug" if augmented else "hqr_lstsq"
+        check(fn(self.h, dA, dB, ldb or self.M, nrhs, dX, ldx or self.N, refine_steps, res, stream), name)
         return list(res)
 
     def stats(self, stream=None):

@@ -26,9 +26,14 @@ struct hqr_plan {
   hqr::DagWorkspace ws;
   hqr::OzWorkspace oz;   // allocated for the split precisions only
   hqr::TreeWorkspace tree;   // domain tree (hqr_plan_set_tree); S = 0: flat
-  // 1 while dT / oz hold the T factors / prepared operands of the last
-  // factorization on this plan (a rebuild from other reflectors replaces them)
+  // split precisions: the prepared operands of H itself (Q generation, Q C),
+  // allocated on first use; oz holds those of H^T (factorization, Q^T C)
+  hqr::OzWorkspace ozh;
+  // 1 while dT / oz (h_valid: ozh) hold the T factors / prepared operands of
+  // the last factorization on this plan (a rebuild from other reflectors
+  // replaces them)
   int factors_valid = 0;
+  int h_valid = 0;
 };
 
 namespace {
@@ -154,36 +159,55 @@ bool split_precision(int precision) { return precision == HQR_PREC_OZAKI || prec
 // tile columns that are still unit vectors (2/3 of the forward updates), then
 // transposed in place; the identity is written whole, so the result does not
 // depend on dQ's prior contents.  Other shapes: the forward application.
-// rebuild_t: rebuild the T factors / prepared operands from dRY, dTAU (they
-// then replace the factorization's in the plan); else use the factorization's.
-int build_qt(hqr_plan* plan, double* dQ, const double* dRY, const double* dTAU, bool rebuild_t,
+// The T factors (FP64: one set for both directions) or prepared operands
+// (split: the H^T set oz, or with h the H set ozh) a Q application uses, and
+// whether its panel tasks rebuild them from the given reflectors.  plan_refl:
+// the caller vouches that those are the last factorization's on this plan
+// (use_plan_t); they are then rebuilt only if a rebuild from other reflectors
+// has replaced them, and are valid again afterwards.  Null: no memory for ozh.
+const hqr::OzWorkspace* apply_operands(hqr_plan* plan, bool h, bool plan_refl, bool* rebuild) {
+  const bool split = plan->oz.slices != nullptr;
+  if (split && h && !plan->ozh.slices) {
+    plan->ozh.groups = plan->oz.groups;
+    if (cudaMalloc(&plan->ozh.slices, hqr::oz_slice_bytes(plan->g)) != cudaSuccess ||
+        cudaMalloc(&plan->ozh.sexp, hqr::oz_exp_bytes(plan->g)) != cudaSuccess) {
+      cudaFree(plan->ozh.slices);
+      plan->ozh = hqr::OzWorkspace{};
+      return nullptr;
+    }
+  }
+  int* valid = (split && h) ? &plan->h_valid : &plan->factors_valid;
+  *rebuild = !plan_refl || !*valid;
+  if (*rebuild) *valid = plan_refl ? 1 : 0;
+  return (split && h) ? &plan->ozh : &plan->oz;
+}
+
+// dQ <- Q^T of the factorization (dRY, dTAU); plan_refl as for apply_operands.
+// untransposed (square matrices): if not null, the backward accumulation
+// leaves Q itself in dQ and *untransposed is set; the caller transposes it.
+int build_qt(hqr_plan* plan, double* dQ, const double* dRY, const double* dTAU, bool plan_refl,
              cudaStream_t s) {
   const hqr::Geometry& g = plan->g;
   if (plan->tree.S > 0) {   // a tree's merges live in the plan: forward application on I
-    if (rebuild_t) return HQR_ERR_UNSUPPORTED;
+    if (!plan_refl) return HQR_ERR_UNSUPPORTED;
     hqr::make_identity(dQ, g.M, g.N, g.NB, true, s);
     return hqr::launch_apply_qt_tree(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g.NT, g_timeout_ns, s,
                                      &plan->oz, &plan->tree);
   }
+  bool rebuild;
   if (g.M == g.N && g.NB % 32 == 0) {
-    // backward accumulation applies H, not H^T: the split precisions prepare
-    // [T V^T | T] for it (the factorization prepared [T^T V^T | T^T])
-    const bool rb = rebuild_t || plan->oz.slices != nullptr;
-    if (rb) plan->factors_valid = 0;
+    // backward accumulation Q = H_0 (H_1 (... I)): H itself
+    const hqr::OzWorkspace* oz = apply_operands(plan, true, plan_refl, &rebuild);
+    if (!oz) return HQR_ERR_NOMEM;
     hqr::make_identity(dQ, g.M, g.N, g.NB, true, s);
-    TRY(hqr::launch_build_q(g, &plan->ws, dRY, plan->dT, dTAU, dQ, rb, g_timeout_ns, s, &plan->oz));
+    TRY(hqr::launch_build_q(g, &plan->ws, dRY, plan->dT, dTAU, dQ, rebuild, g_timeout_ns, s, oz));
     hqr::transpose_tiles(dQ, g.N, g.NB, s);
     return cuda_rc(cudaGetLastError());
   }
-  if (rebuild_t) plan->factors_valid = 0;
+  const hqr::OzWorkspace* oz = apply_operands(plan, false, plan_refl, &rebuild);
   hqr::make_identity(dQ, g.M, g.N, g.NB, false, s);
-  return hqr::launch_apply_qt(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g.NT, rebuild_t, g_timeout_ns, s,
-                              &plan->oz);
+  return hqr::launch_apply_qt(g, &plan->ws, dRY, plan->dT, dTAU, dQ, g.NT, rebuild, g_timeout_ns, s, oz);
 }
-
-// Whether a Q application must rebuild its T factors: always unless the
-// caller vouches for the plan's (use_plan_t) and nothing has replaced them.
-bool must_rebuild(const hqr_plan* plan, int use_plan_t) { return !use_plan_t || !plan->factors_valid; }
 
 // Phases of the last drop-in call, from CUDA events on the staging stream:
 // marks 0..4 = before the host-to-device copies, after them, after the DAG
@@ -345,6 +369,8 @@ int hqr_plan_destroy(hqr_plan_t* plan) {
   if (plan->dT) cudaFree(plan->dT);
   if (plan->oz.slices) cudaFree(plan->oz.slices);
   if (plan->oz.sexp) cudaFree(plan->oz.sexp);
+  if (plan->ozh.slices) cudaFree(plan->ozh.slices);
+  if (plan->ozh.sexp) cudaFree(plan->ozh.sexp);
   hqr::dag_workspace_free(&plan->ws);
   delete plan;
   return HQR_OK;
@@ -355,6 +381,7 @@ double* hqr_plan_t_factors(hqr_plan_t* plan) { return plan ? plan->dT : nullptr;
 int hqr_geqrf_async(hqr_plan_t* plan, double* dA, double* dTAU, void* stream) {
   if (!plan || !dA || !dTAU) return HQR_ERR_INVALID;
   plan->factors_valid = 0;
+  plan->h_valid = 0;
   TRY(hqr::launch_factor(plan->g, &plan->ws, dA, plan->dT, dTAU, g_timeout_ns, (cudaStream_t)stream, &plan->oz,
                          &plan->tree));
   plan->factors_valid = 1;
@@ -388,7 +415,7 @@ int hqr_make_q_async(hqr_plan_t* plan, double* dQ, double* dRY, const double* dT
   if (!plan || !dQ || !dRY || !dTAU) return HQR_ERR_INVALID;
   const hqr::Geometry& g = plan->g;
   cudaStream_t s = (cudaStream_t)stream;
-  TRY(build_qt(plan, dQ, dRY, dTAU, plan->tree.S > 0 ? !use_plan_t : must_rebuild(plan, use_plan_t), s));
+  TRY(build_qt(plan, dQ, dRY, dTAU, use_plan_t != 0, s));
   hqr::zero_reflectors(dRY, g.M, g.N, g.NB, s);
   return cuda_rc(cudaGetLastError());
 }
@@ -407,11 +434,28 @@ int hqr_ormqr_t(hqr_plan_t* plan, const double* dRY, const double* dTAU, double*
     TRY(hqr::launch_apply_qt_tree(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, g_timeout_ns,
                                   (cudaStream_t)stream, &plan->oz, &plan->tree));
   } else {
-    const bool rebuild = must_rebuild(plan, use_plan_t);
-    if (rebuild) plan->factors_valid = 0;
+    bool rebuild;
+    const hqr::OzWorkspace* oz = apply_operands(plan, false, use_plan_t != 0, &rebuild);
     TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, rebuild, g_timeout_ns,
-                             (cudaStream_t)stream, &plan->oz));
+                             (cudaStream_t)stream, oz));
   }
+  return hqr_plan_status(plan, stream);
+}
+
+int hqr_ormqr_n_async(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT,
+                      int use_plan_t, void* stream) {
+  if (!plan || !dRY || !dTAU || !dC || CT <= 0) return HQR_ERR_INVALID;
+  if (plan->tree.S > 0) return HQR_ERR_UNSUPPORTED;
+  bool rebuild;
+  const hqr::OzWorkspace* oz = apply_operands(plan, true, use_plan_t != 0, &rebuild);
+  if (!oz) return HQR_ERR_NOMEM;
+  return hqr::launch_apply_q(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, rebuild, g_timeout_ns,
+                             (cudaStream_t)stream, oz);
+}
+
+int hqr_ormqr_n(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT, int use_plan_t,
+                void* stream) {
+  TRY(hqr_ormqr_n_async(plan, dRY, dTAU, dC, CT, use_plan_t, stream));
   return hqr_plan_status(plan, stream);
 }
 
@@ -423,12 +467,13 @@ struct LstsqWork {
   double* C = nullptr;    // right-hand sides / residuals in tile layout
   double* R = nullptr;    // residual, column-major M x nrhs
   double* nrm = nullptr;
+  // augmented-system refinement only
+  double* G = nullptr;    // [h; d2] in tile layout, then the residual's correction
+  double* r = nullptr;    // the refined least-squares residual, column-major M x nrhs
+  double* g = nullptr;    // -A^T r, column-major N x nrhs
+  double* P = nullptr;    // partial sums of A^T r
   ~LstsqWork() {
-    cudaFree(Af);
-    cudaFree(tau);
-    cudaFree(C);
-    cudaFree(R);
-    cudaFree(nrm);
+    for (double* p : {Af, tau, C, R, nrm, G, r, g, P}) cudaFree(p);
   }
 };
 int dmalloc(double** p, size_t n) {
@@ -462,6 +507,73 @@ int hqr_lstsq(hqr_plan_t* plan, const double* dA, const double* dB, int ldb, int
     TRY(hqr_ormqr_t(plan, w.Af, w.tau, w.C, CT, 1, stream));
     TRY(hqr::trsm_tiles(w.Af, g.M, g.N, g.NB, w.C, nrhs, s));
     hqr::update_x(w.C, g.M, g.NB, g.N, nrhs, dX, ldx, it > 0, s);
+    TRY(cuda_rc(cudaGetLastError()));
+  }
+  if (resid) {
+    TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, w.R, g.M, nrhs, s));
+    hqr::col_norm2(w.R, g.M, g.M, nrhs, w.nrm, s);
+    TRY(cuda_rc(cudaMemcpyAsync(resid, w.nrm, (size_t)nrhs * sizeof(double), cudaMemcpyDeviceToHost, s)));
+  }
+  TRY(cuda_rc(cudaStreamSynchronize(s)));
+  if (resid)
+    for (int q = 0; q < nrhs; q++) resid[q] = sqrt(resid[q]);
+  return HQR_OK;
+}
+
+// Bjorck's refinement on the augmented system [I A; A^T 0][r; x] = [b; 0]:
+// each step forms f = b - r - A x and g = -A^T r in FP64 and solves the
+// correction system with the factorization -- h = R^-T g, d = Q^T f,
+// dx = R^-1 (d(1:N) - h), dr = Q [h; d(N+1:M)] -- so the floor of x is set by
+// the FP64 residuals (kappa u), not by the factorization's precision.
+int hqr_lstsq_aug(hqr_plan_t* plan, const double* dA, const double* dB, int ldb, int nrhs, double* dX,
+                  int ldx, int refine_steps, double* resid, void* stream) {
+  if (!plan || !dA || !dB || !dX || nrhs <= 0 || refine_steps < 0) return HQR_ERR_INVALID;
+  const hqr::Geometry& g = plan->g;
+  if (g.M < g.N || ldb < g.M || ldx < g.N) return HQR_ERR_INVALID;
+  if (plan->tree.S > 0) return HQR_ERR_UNSUPPORTED;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int CT = (nrhs + g.NB - 1) / g.NB;
+  const int S = hqr::atr_slices(g.M, g.N, g.NB, nrhs);
+  LstsqWork w;
+  TRY(dmalloc(&w.Af, (size_t)g.M * g.N));
+  TRY(dmalloc(&w.tau, tau_len(g)));
+  TRY(dmalloc(&w.C, (size_t)g.M * CT * g.NB));
+  TRY(dmalloc(&w.G, (size_t)g.M * CT * g.NB));
+  TRY(dmalloc(&w.R, (size_t)g.M * nrhs));
+  TRY(dmalloc(&w.r, (size_t)g.M * nrhs));
+  TRY(dmalloc(&w.g, (size_t)g.N * nrhs));
+  TRY(dmalloc(&w.P, (size_t)S * g.N * nrhs));
+  TRY(dmalloc(&w.nrm, (size_t)nrhs));
+  TRY(cuda_rc(cudaMemcpyAsync(w.Af, dA, (size_t)g.M * g.N * sizeof(double), cudaMemcpyDeviceToDevice, s)));
+  TRY(hqr_geqrf(plan, w.Af, w.tau, stream));
+  // x0 = R^-1 (Q^T b)(1:N), r0 = b - A x0
+  hqr::pack_rhs(dB, ldb, nrhs, w.C, g.M, g.NB, CT, s);
+  TRY(cuda_rc(cudaGetLastError()));
+  TRY(hqr_ormqr_t(plan, w.Af, w.tau, w.C, CT, 1, stream));
+  TRY(hqr::trsm_tiles(w.Af, g.M, g.N, g.NB, w.C, nrhs, s));
+  hqr::update_x(w.C, g.M, g.NB, g.N, nrhs, dX, ldx, false, s);
+  TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, w.r, g.M, nrhs, s));
+  const int MT = (int)(g.M / g.NB), NT = (int)(g.N / g.NB);
+  for (int it = 0; it < refine_steps; it++) {
+    // f = b - A x - r, g = -A^T r
+    TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, w.R, g.M, nrhs, s));
+    hqr::sub_colmajor(w.R, g.M, w.r, g.M, g.M, nrhs, s);
+    TRY(hqr::at_times(dA, g.M, g.N, g.NB, w.r, g.M, nrhs, -1.0, w.g, g.N, w.P, S, s));
+    // d = Q^T f; h = R^-T g
+    hqr::pack_rhs(w.R, g.M, nrhs, w.C, g.M, g.NB, CT, s);
+    TRY(cuda_rc(cudaGetLastError()));
+    TRY(hqr_ormqr_t(plan, w.Af, w.tau, w.C, CT, 1, stream));
+    hqr::pack_rhs_rows(w.g, g.N, nrhs, g.N, w.G, g.M, g.NB, CT, s);
+    TRY(hqr::trsmt_tiles(w.Af, g.M, g.N, g.NB, w.G, nrhs, s));
+    // G = [h; d2], C = [d1 - h; d2]
+    hqr::tile_rows(w.C, w.G, g.M, g.NB, CT, NT, MT, false, s);
+    hqr::tile_rows(w.C, w.G, g.M, g.NB, CT, 0, NT, true, s);
+    // x += R^-1 (d1 - h); r += Q [h; d2]
+    TRY(hqr::trsm_tiles(w.Af, g.M, g.N, g.NB, w.C, nrhs, s));
+    hqr::update_x(w.C, g.M, g.NB, g.N, nrhs, dX, ldx, true, s);
+    TRY(cuda_rc(cudaGetLastError()));
+    TRY(hqr_ormqr_n(plan, w.Af, w.tau, w.G, CT, 1, stream));
+    hqr::add_unpack(w.r, g.M, w.G, g.M, g.NB, nrhs, s);
     TRY(cuda_rc(cudaGetLastError()));
   }
   if (resid) {
@@ -627,14 +739,15 @@ static int do_apply(mat_stat_t* st, double* Q, double* RY, double* TAU, int rank
   TRY(cuda_rc(cudaEventRecord(g_stage.h2d_done, s)));
   phase_mark(1, s);
   if (mode == 2) {
-    plan->factors_valid = 0;
-    TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dQ, plan->g.NT, true,
-                             g_timeout_ns, s, &plan->oz));
+    bool rebuild;
+    const hqr::OzWorkspace* oz = apply_operands(plan, false, false, &rebuild);
+    TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dQ, plan->g.NT, rebuild,
+                             g_timeout_ns, s, oz));
   } else {
     // make_Q (caller-zeroed Q, Hybrid_make_Q.c:91-95) and dorgqr (Q := I,
     // Hybrid_dorgqr.c:56) both produce Q^T of the factorization
     if (mode == 1) hqr::make_identity(dQ, M, N, NB, true, s);
-    TRY(build_qt(plan, dQ, dRY, dTAU, true, s));
+    TRY(build_qt(plan, dQ, dRY, dTAU, false, s));   // the caller's reflectors: always prepared
   }
   phase_mark(2, s);
   if (mode == 0) {

@@ -279,6 +279,32 @@ int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double
   return run_dag(p, ws, g, stream);
 }
 
+int launch_apply_q(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT, const double* dTAU,
+                   double* dC, int CT, bool rebuild_t, long long timeout_ns, cudaStream_t stream,
+                   const OzWorkspace* ozw) {
+  if (CT <= 0) return HQR_ERR_INVALID;
+  DagParams p{};
+  p.mode = kModeApplyQ;
+  p.MT = g.MT;
+  p.NT = g.NT;
+  p.CT = CT;
+  p.steps = g.steps;
+  p.J = CT;
+  p.A = const_cast<double*>(dA);
+  p.T = dT;
+  p.TAU = const_cast<double*>(dTAU);
+  p.C = dC;
+  p.timeout_ns = timeout_ns;
+  set_oz(p, g, ozw);
+  p.prep = 0;
+  p.nblk = 1;
+  p.skip_panels = rebuild_t ? 0 : 1;
+  long long n = 0;
+  for (int i = 0; i < g.steps; i++) n += (rebuild_t ? (g.MT - i) : 0) + (long long)p.NC * CT * (g.MT - i);
+  p.n_tasks = (int)n;
+  return run_dag(p, ws, g, stream);
+}
+
 // --- batches of independent matrices (FP64) ---------------------------------------
 size_t mat_desc_bytes() { return sizeof(MatDesc); }
 

@@ -42,7 +42,13 @@ enum DagMode : int {
   // from the bottom up; step i touches tile columns j >= i only (columns j < i
   // are still unit vectors in rows >= i), 2/3 of the updates of kModeApplyQt.
   kModeBuildQ = 2,
+  // C <- Q C = H_0 H_1 ... H_{steps-1} C for a general C of CT tile columns
+  // (LAPACK dormqr 'L','N'): kModeBuildQ's order and arithmetic (H, not H^T)
+  // on every tile column.
+  kModeApplyQ = 3,
 };
+// The modes that apply H itself (not H^T).
+__host__ __device__ __forceinline__ bool applies_h(int mode) { return mode == kModeBuildQ || mode == kModeApplyQ; }
 
 // With split precision (DagParams::oz) the update tasks run OZAPPLY and every
 // panel tile gets an OZPREP task (in the factorization it follows the
@@ -394,8 +400,9 @@ __device__ int init_deps(const DagParams& p, int id) {
     const int j = u % p.J;
     const int i = u / p.J;
     if (k >= i && i < p.steps && update_valid(p, i, j)) {
-      if (p.mode == kModeBuildQ)   // panel (unless given) + chain from the tile below + step i+1's write of (k, j)
-        deps = (p.skip_panels ? 0 : 1) + (k < p.MT - 1 ? 1 : 0) + ((k > i && j > i && i + 1 < p.steps) ? 1 : 0);
+      if (applies_h(p.mode))   // panel (unless given) + chain from the tile below + step i+1's write of (k, j)
+        deps = (p.skip_panels ? 0 : 1) + (k < p.MT - 1 ? 1 : 0) +
+               ((k > i && (j > i || p.mode == kModeApplyQ) && i + 1 < p.steps) ? 1 : 0);
       else   // panel (unless given) + the chain above in the domain + the previous step's write
         deps = (p.skip_panels ? 0 : 1) + (is_top(p, i, k) ? 0 : 1) + (i > 0 ? 1 : 0);
     }
@@ -591,7 +598,7 @@ __device__ bool release_dependents(const DagParams& p, const TaskDesc& t, int* k
     const int d = dom_of(p, t.i, t.k);
     if (d + 1 < n_domains(p, t.i)) push_id(ids, n, ttmqr_id(p, t.i, t.j, d + 1, t.c));
     push_id(ids, n, mem_consumer(p, t.i, t.j, t.k, t.c));   // the domain top's tile row is final
-  } else if (p.mode == kModeBuildQ) {
+  } else if (applies_h(p.mode)) {
     // the chain runs from the bottom tile up to the LARFB; the step before
     // (i - 1) next writes tile (k, j), which this task wrote last
     if (t.k - 1 >= t.i) push_id(ids, n, update_id(p, t.i, t.j, t.k - 1, t.c));
@@ -754,7 +761,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
           oz_bot = q.C + oc + (size_t)t.c * oz::kN * NB;
         } else {
           task_larfb(q.A + ov, q.T + ov, q.C + oc, t.c * q.sh.CB, q.sh.CB, q.sh, smem, q.sp,
-                     q.mode == kModeBuildQ);
+                     applies_h(q.mode));
         }
         break;
       }
@@ -773,7 +780,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
           oz_bot = q.C + o2 + cofs;
         } else {
           task_ssrfb(q.C + o1, q.C + o2, q.A + ov, tt ? q.T2 + slot * tsz : q.T + ov, t.c * q.sh.CB,
-                     q.sh.CB, q.sh, smem, q.sp, q.mode == kModeBuildQ, tt);
+                     q.sh.CB, q.sh, smem, q.sp, applies_h(q.mode), tt);
         }
         break;
       }
@@ -781,10 +788,10 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
         if (threadIdx.x == 0) atomicOr((int*)(q.ctl + kErr), kErrBadTask);
     }
     if (ts_a1) task_tsqrt_blk(ts_a1, ts_a2, ts_t, ts_tau, q.sh, smem, q.sp, t.c, ts_upper);
-    // Q generation applies H (M = T), the other modes H^T (M = T^T)
+    // Q generation and Q C apply H (M = T), the other modes H^T (M = T^T)
     if (OZ && prep_v)
       task_ozprep(prep_v, prep_tau, prep_g, prep_kind, prep_slices, prep_exps, reinterpret_cast<uint8_t*>(smem),
-                  s_tmem, q.ctl + kErr, q.mode != kModeBuildQ);
+                  s_tmem, q.ctl + kErr, !applies_h(q.mode));
     if (OZ && oz_bot) {
       oz::Ctx c;
       oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, q.ctl + kErr);

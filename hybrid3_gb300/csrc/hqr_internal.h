@@ -45,6 +45,22 @@ void col_norm2(const double* dR, long M, long ldr, int nrhs, double* dOut, cudaS
 // Back substitution R Y = C(1:N, :) in place (R: upper triangle of the
 // factored A's first N / NB tile rows).
 int trsm_tiles(const double* dRA, long M, long N, int NB, double* dC, int nrhs, cudaStream_t s);
+// Forward substitution R^T Y = C(1:N, :) in place.
+int trsmt_tiles(const double* dRA, long M, long N, int NB, double* dC, int nrhs, cudaStream_t s);
+// pack_rhs with rows nrows.. of the tile layout zero.
+void pack_rhs_rows(const double* dB, long ldb, int nrhs, long nrows, double* dC, long M, int NB, int CT,
+                   cudaStream_t s);
+void sub_colmajor(double* dF, long ldf, const double* dR, long ldr, long M, int nrhs, cudaStream_t s);
+// R (column-major) += the first nrhs columns of D (tile layout).
+void add_unpack(double* dR, long ldr, const double* dD, long M, int NB, int nrhs, cudaStream_t s);
+// Tile rows [ti0, ti1) of MT x CT tile grids: D <- C, or C -= D (sub).
+void tile_rows(double* dC, double* dD, long M, int NB, int CT, int ti0, int ti1, bool sub, cudaStream_t s);
+// Tile-row slices of at_times for about four blocks per SM.
+int atr_slices(long M, long N, int NB, int nrhs);
+// G (column-major N x nrhs) = alpha A^T R (R column-major M x nrhs) in FP64,
+// over S slices of tile rows summed in a fixed order (dP: S N nrhs doubles).
+int at_times(const double* dA, long M, long N, int NB, const double* dR, long ldr, int nrhs, double alpha,
+             double* dG, long ldg, double* dP, int S, cudaStream_t s);
 
 // Scheduler workspace (dependency counters, queues, control words, stats).
 struct DagWorkspace {
@@ -106,6 +122,11 @@ int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, doubl
 // rebuild_t false: the T factors / prepared operands of the factorization.
 int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT, const double* dTAU,
                    double* dQ, bool rebuild_t, long long timeout_ns, cudaStream_t stream,
+                   const OzWorkspace* oz = nullptr);
+// C <- Q C (CT tile columns, same MT/NB as A): H applied in backward order;
+// rebuild_t false: the T factors / prepared operands (of H) given.
+int launch_apply_q(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT, const double* dTAU,
+                   double* dC, int CT, bool rebuild_t, long long timeout_ns, cudaStream_t stream,
                    const OzWorkspace* oz = nullptr);
 // Batches of independent FP64 factorizations in one persistent launch.
 // Descriptors (mat_desc_bytes() each) are written to host memory by

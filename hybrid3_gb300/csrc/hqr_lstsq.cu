@@ -15,8 +15,8 @@ constexpr int kRhsChunk = 16;   // right-hand sides per thread pass
 constexpr int kRBlock = 32;     // columns of R staged per pass of the diagonal solve
 
 // C (tile layout of an M x CT*NB matrix, MT tile rows) <- B (column-major
-// M x nrhs, ld ldb), zero beyond column nrhs.
-__global__ void k_pack_rhs(const double* __restrict__ B, long ldb, int nrhs, double* __restrict__ C,
+// nrows x nrhs, ld ldb), zero beyond column nrhs and row nrows.
+__global__ void k_pack_rhs(const double* __restrict__ B, long ldb, int nrhs, long nrows, double* __restrict__ C,
                            long M, int MT, int NB, int CT) {
   const long n = M * (long)CT * NB;
   const long tile_elems = (long)NB * NB;
@@ -25,7 +25,91 @@ __global__ void k_pack_rhs(const double* __restrict__ B, long ldb, int nrhs, dou
     const int within = (int)(e - tile * tile_elems);
     const long row = (tile % MT) * NB + within % NB;
     const long col = (tile / MT) * NB + within / NB;
-    C[e] = col < nrhs ? B[row + col * ldb] : 0.0;
+    C[e] = (col < nrhs && row < nrows) ? B[row + col * ldb] : 0.0;
+  }
+}
+
+// F -= R (column-major M x nrhs, leading dimensions ldf, ldr).
+__global__ void k_sub_cm(double* __restrict__ F, long ldf, const double* __restrict__ R, long ldr, long M,
+                         int nrhs) {
+  const long n = M * (long)nrhs;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const long row = e % M, col = e / M;
+    F[row + col * ldf] -= R[row + col * ldr];
+  }
+}
+
+// R (column-major M x nrhs) += the first nrhs columns of D (tile layout, MT
+// tile rows).
+__global__ void k_add_unpack(double* __restrict__ R, long ldr, const double* __restrict__ D, long M, int MT,
+                             int NB, int nrhs) {
+  const long n = M * (long)nrhs;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const long row = e % M, col = e / M;
+    R[row + col * ldr] += D[((row / NB) + (col / NB) * (long)MT) * NB * NB + (col % NB) * NB + row % NB];
+  }
+}
+
+// Tile rows [ti0, ti1) of the MT x CT tile grids: D <- C (sub = 0) or
+// C <- C - D (sub = 1).
+__global__ void k_tile_rows(double* __restrict__ C, double* __restrict__ D, int MT, int NB, int CT, int ti0,
+                            int ti1, int sub) {
+  const long tile = (long)NB * NB;
+  const long per_col = (long)(ti1 - ti0) * tile;
+  const long n = per_col * CT;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const long tj = e / per_col, within = e % per_col;
+    const long off = (tj * MT + ti0) * tile + within;
+    if (sub)
+      C[off] -= D[off];
+    else
+      D[off] = C[off];
+  }
+}
+
+// Partial sums of A^T R over tile-row slice blockIdx.z: P[z] (column-major
+// N x nrhs) = sum over tile rows ti = z, z + S, ... of A(ti, :)^T R(ti rows, :).
+// Block (tj, q0 / kRhsChunk, z); thread c = column c of tile column tj (NB
+// threads) walks its own (contiguous) tile column; R's rows are staged.
+__global__ void k_atr(const double* __restrict__ A, long M, long N, int NB, const double* __restrict__ R,
+                      long ldr, double* __restrict__ P, int nrhs) {
+  extern __shared__ double sr[];   // NB x kRhsChunk rows of R
+  const int MT = (int)(M / NB), S = (int)gridDim.z;
+  const int tj = blockIdx.x, q0 = blockIdx.y * kRhsChunk, z = blockIdx.z;
+  const int c = threadIdx.x;
+  double acc[kRhsChunk];
+#pragma unroll
+  for (int q = 0; q < kRhsChunk; q++) acc[q] = 0.0;
+  for (int ti = z; ti < MT; ti += S) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < NB * kRhsChunk; e += blockDim.x) {
+      const int k = e % NB, q = e / NB;
+      sr[e] = (q0 + q < nrhs) ? R[(long)ti * NB + k + (long)(q0 + q) * ldr] : 0.0;
+    }
+    __syncthreads();
+    const double* Ac = A + ((long)ti + (long)tj * MT) * NB * NB + (long)c * NB;
+#pragma unroll 4
+    for (int k = 0; k < NB; k++) {
+      const double a = __ldg(Ac + k);
+#pragma unroll
+      for (int q = 0; q < kRhsChunk; q++) acc[q] = fma(a, sr[k + q * NB], acc[q]);
+    }
+  }
+  double* Pz = P + (long)z * N * nrhs;
+  const long row = (long)tj * NB + c;
+#pragma unroll
+  for (int q = 0; q < kRhsChunk; q++)
+    if (q0 + q < nrhs) Pz[row + (long)(q0 + q) * N] = acc[q];
+}
+
+// G (column-major N x nrhs, ld ldg) = alpha * sum_z P[z], z in order.
+__global__ void k_sum_partials(const double* __restrict__ P, int S, long N, int nrhs, double alpha,
+                               double* __restrict__ G, long ldg) {
+  const long n = N * (long)nrhs;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int z = 0; z < S; z++) s += P[(long)z * n + e];
+    G[(e % N) + (e / N) * ldg] = alpha * s;
   }
 }
 
@@ -180,6 +264,95 @@ __global__ void k_trsm_step(const double* __restrict__ RA, int MT, int NB, doubl
   }
 }
 
+// One step of the forward substitution R^T Y = C over the first NT tile rows
+// of C (tile layout, MT tile rows): step i first updates, in blocks k >= i,
+// C_k -= R_(i-1)k^T Y_(i-1) (Y_(i-1) solved by the step before; none at
+// i = 0), then block k = i solves R_ii^T Y_i = C_i in place (R_ii^T lower
+// triangular).  RA: the factored A (R in its upper tiles).  Thread r owns row
+// r of the tile (NB threads); R_(i-1)k^T's row r is R_(i-1)k's column r,
+// contiguous in the tile.
+__global__ void k_trsmt_step(const double* __restrict__ RA, int MT, int NB, double* __restrict__ C, int i,
+                             int nrhs) {
+  extern __shared__ double sm[];   // NB x kRhsChunk right operand / kRBlock x NB rows of R + 2 x kRhsChunk
+  const int k = i + (int)blockIdx.x;
+  const int tj = blockIdx.y;
+  const int ncol = min(NB, nrhs - tj * NB);
+  const int r = threadIdx.x;
+  const long tile = (long)NB * NB;
+  double* Ck = C + ((long)k + (long)tj * MT) * tile;
+  if (i > 0) {
+    const double* Rik = RA + ((long)(i - 1) + (long)k * MT) * tile;
+    const double* Yi = C + ((long)(i - 1) + (long)tj * MT) * tile;
+    for (int c0 = 0; c0 < ncol; c0 += kRhsChunk) {
+      const int nq = min(kRhsChunk, ncol - c0);
+      __syncthreads();
+      for (int e = threadIdx.x; e < NB * kRhsChunk; e += blockDim.x) {
+        const int kk = e % NB, q = e / NB;
+        sm[e] = q < nq ? Yi[kk + (long)(c0 + q) * NB] : 0.0;
+      }
+      __syncthreads();
+      double acc[kRhsChunk];
+#pragma unroll
+      for (int q = 0; q < kRhsChunk; q++) acc[q] = 0.0;
+      const double* Rc = Rik + (long)r * NB;   // column r of R_(i-1)k = row r of its transpose
+#pragma unroll 4
+      for (int kk = 0; kk < NB; kk++) {
+        const double a = __ldg(Rc + kk);
+#pragma unroll
+        for (int q = 0; q < kRhsChunk; q++) acc[q] = fma(a, sm[kk + q * NB], acc[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < kRhsChunk; q++)
+        if (q < nq) Ck[r + (long)(c0 + q) * NB] -= acc[q];
+    }
+  }
+  if (k != i) return;
+  // R_kk^T Y = C_k: rows from the top; thread r keeps its row's values in
+  // registers, the solved value of row j is broadcast through a double buffer
+  // (one barrier per row); R_kk's rows j (R_kk^T's column j, elements R(j, r))
+  // are staged kRBlock at a time.
+  __syncthreads();
+  const double* Rkk = RA + ((long)k + (long)k * MT) * tile;
+  double* sR = sm;                          // kRBlock x NB: sR[(j - jb) + r kRBlock] = R(j, r)
+  double* sy = sm + (long)NB * kRBlock;     // 2 x kRhsChunk
+  for (int c0 = 0; c0 < ncol; c0 += kRhsChunk) {
+    const int nq = min(kRhsChunk, ncol - c0);
+    double v[kRhsChunk];
+#pragma unroll
+    for (int q = 0; q < kRhsChunk; q++) v[q] = q < nq ? Ck[r + (long)(c0 + q) * NB] : 0.0;
+    int buf = 0;
+    for (int jb = 0; jb < NB; jb += kRBlock) {
+      const int je = min(NB, jb + kRBlock);
+      __syncthreads();
+      for (int e = threadIdx.x; e < (je - jb) * NB; e += blockDim.x) {
+        const int jj = e % (je - jb), cc = e / (je - jb);
+        sR[jj + cc * kRBlock] = Rkk[(jb + jj) + (long)cc * NB];
+      }
+      __syncthreads();
+      for (int j = jb; j < je; j++) {
+        if (r == j) {
+          const double d = sR[(j - jb) + j * kRBlock];
+#pragma unroll
+          for (int q = 0; q < kRhsChunk; q++) {
+            v[q] = v[q] / d;
+            sy[buf * kRhsChunk + q] = v[q];
+          }
+        }
+        __syncthreads();
+        if (r > j) {
+          const double rj = sR[(j - jb) + r * kRBlock];
+#pragma unroll
+          for (int q = 0; q < kRhsChunk; q++) v[q] = fma(-rj, sy[buf * kRhsChunk + q], v[q]);
+        }
+        buf ^= 1;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kRhsChunk; q++)
+      if (q < nq) Ck[r + (long)(c0 + q) * NB] = v[q];
+  }
+}
+
 int blocks_for(long n) {
   long b = (n + 255) / 256;
   return (int)(b < 1 ? 1 : (b > 4 * 152 ? 4 * 152 : b));
@@ -188,7 +361,48 @@ int blocks_for(long n) {
 }  // namespace
 
 void pack_rhs(const double* dB, long ldb, int nrhs, double* dC, long M, int NB, int CT, cudaStream_t s) {
-  k_pack_rhs<<<blocks_for(M * (long)CT * NB), 256, 0, s>>>(dB, ldb, nrhs, dC, M, (int)(M / NB), NB, CT);
+  k_pack_rhs<<<blocks_for(M * (long)CT * NB), 256, 0, s>>>(dB, ldb, nrhs, M, dC, M, (int)(M / NB), NB, CT);
+}
+
+void pack_rhs_rows(const double* dB, long ldb, int nrhs, long nrows, double* dC, long M, int NB, int CT,
+                   cudaStream_t s) {
+  k_pack_rhs<<<blocks_for(M * (long)CT * NB), 256, 0, s>>>(dB, ldb, nrhs, nrows, dC, M, (int)(M / NB), NB, CT);
+}
+
+void sub_colmajor(double* dF, long ldf, const double* dR, long ldr, long M, int nrhs, cudaStream_t s) {
+  k_sub_cm<<<blocks_for(M * (long)nrhs), 256, 0, s>>>(dF, ldf, dR, ldr, M, nrhs);
+}
+
+void add_unpack(double* dR, long ldr, const double* dD, long M, int NB, int nrhs, cudaStream_t s) {
+  k_add_unpack<<<blocks_for(M * (long)nrhs), 256, 0, s>>>(dR, ldr, dD, M, (int)(M / NB), NB, nrhs);
+}
+
+void tile_rows(double* dC, double* dD, long M, int NB, int CT, int ti0, int ti1, bool sub, cudaStream_t s) {
+  if (ti1 <= ti0) return;
+  k_tile_rows<<<blocks_for((long)(ti1 - ti0) * NB * NB * CT), 256, 0, s>>>(dC, dD, (int)(M / NB), NB, CT, ti0,
+                                                                            ti1, sub ? 1 : 0);
+}
+
+int atr_slices(long M, long N, int NB, int nrhs) {
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long base = (N / NB) * ((nrhs + kRhsChunk - 1) / kRhsChunk);
+  const long want = (4L * sms + base - 1) / base;
+  return (int)(want < 1 ? 1 : (want > M / NB ? M / NB : want));
+}
+
+int at_times(const double* dA, long M, long N, int NB, const double* dR, long ldr, int nrhs, double alpha,
+             double* dG, long ldg, double* dP, int S, cudaStream_t s) {
+  const dim3 grid((unsigned)(N / NB), (unsigned)((nrhs + kRhsChunk - 1) / kRhsChunk), (unsigned)S);
+  const size_t smem = (size_t)NB * kRhsChunk * sizeof(double);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_atr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(k_atr)");
+  }
+  k_atr<<<grid, NB, smem, s>>>(dA, M, N, NB, dR, ldr, dP, nrhs);
+  k_sum_partials<<<blocks_for(N * (long)nrhs), 256, 0, s>>>(dP, S, N, nrhs, alpha, dG, ldg);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? HQR_OK : record_cuda_error(e, "k_atr launch");
 }
 
 void update_x(const double* dC, long M, int NB, long N, int nrhs, double* dX, long ldx, bool accumulate,
@@ -233,6 +447,22 @@ int trsm_tiles(const double* dRA, long M, long N, int NB, double* dC, int nrhs, 
   }
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? HQR_OK : record_cuda_error(e, "k_trsm_step launch");
+}
+
+int trsmt_tiles(const double* dRA, long M, long N, int NB, double* dC, int nrhs, cudaStream_t s) {
+  const int MT = (int)(M / NB), NT = (int)(N / NB);
+  const int CT = (nrhs + NB - 1) / NB;
+  const size_t smem = trsm_smem_bytes(NB);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_trsmt_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(k_trsmt_step)");
+  }
+  for (int i = 0; i < NT; i++) {
+    const dim3 grid((unsigned)(NT - i), (unsigned)CT);
+    k_trsmt_step<<<grid, NB, smem, s>>>(dRA, MT, NB, dC, i, nrhs);
+  }
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? HQR_OK : record_cuda_error(e, "k_trsmt_step launch");
 }
 
 }  // namespace hqr

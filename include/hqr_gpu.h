@@ -92,9 +92,11 @@ int hqr_plan_destroy(hqr_plan_t *plan);
  * need use_plan_t = 1 (HQR_ERR_UNSUPPORTED otherwise) and Q is built by the
  * forward application.  Allocates the merges' storage. */
 int hqr_plan_set_tree(hqr_plan_t *plan, int domain_tiles);
-/* Device T factors of the last factorization: NB x NB upper-triangular tile
- * per panel tile, same tile layout as A (only the w x w diagonal blocks are
- * written by the factorization). */
+/* Device T factors: one NB x NB tile per panel tile, same tile layout as A.
+ * FP64: the last factorization's w x w diagonal blocks of T (upper
+ * triangular).  Split precision: the whole NB x NB operand of the last call
+ * that prepared operands -- T^T after hqr_geqrf / hqr_ormqr_t, T after Q
+ * generation or hqr_ormqr_n. */
 double *hqr_plan_t_factors(hqr_plan_t *plan);
 
 /* In-place factorization of dA (device), TAU to dTAU (MT*NT*NB doubles).
@@ -126,9 +128,10 @@ int hqr_plan_stats(hqr_plan_t *plan, hqr_stats_t *out, void *stream);
  * reflectors (use_plan_t = 0 here or in hqr_ormqr_t, or a drop-in Hybrid_*
  * call), they are rebuilt from dRY and dTAU instead.  use_plan_t = 0: always
  * rebuilt from dRY and dTAU (any reflectors in this plan's shape), replacing
- * the plan's.  Square Q generation with a split precision applies H itself,
- * not H^T, so it always prepares its own operands ([T V^T | T] where the
- * factorization and Q^T C use [T^T V^T | T^T]). */
+ * the plan's.  Square Q generation applies H itself, not H^T: with a split
+ * precision its prepared operands ([T V^T | T], where the factorization and
+ * Q^T C use [T^T V^T | T^T]) are made by its first call after a
+ * factorization and kept apart, so later calls reuse them. */
 int hqr_make_q(hqr_plan_t *plan, double *dQ, double *dRY, const double *dTAU, int use_plan_t,
                void *stream);
 int hqr_make_q_async(hqr_plan_t *plan, double *dQ, double *dRY, const double *dTAU,
@@ -138,6 +141,17 @@ int hqr_make_q_async(hqr_plan_t *plan, double *dQ, double *dRY, const double *dT
  * use_plan_t as for hqr_make_q.  Waits for completion. */
 int hqr_ormqr_t(hqr_plan_t *plan, const double *dRY, const double *dTAU, double *dC, int CT,
                 int use_plan_t, void *stream);
+/* No counterpart in the reference (its dormqr applies Q^T only).  dC <- Q dC
+ * (LAPACK dormqr 'L','N'): the reflectors applied as H, in backward order,
+ * to every tile column of dC (MT x CT tiles).  use_plan_t as for hqr_make_q;
+ * split precisions keep the prepared operands of H apart from those of H^T,
+ * so Q dC and Q^T dC both reuse theirs after one preparation.  Flat tree
+ * only (HQR_ERR_UNSUPPORTED with a domain tree).  The _async form only
+ * enqueues (check with hqr_plan_status). */
+int hqr_ormqr_n(hqr_plan_t *plan, const double *dRY, const double *dTAU, double *dC, int CT,
+                int use_plan_t, void *stream);
+int hqr_ormqr_n_async(hqr_plan_t *plan, const double *dRY, const double *dTAU, double *dC, int CT,
+                      int use_plan_t, void *stream);
 
 /* No counterpart in the reference (its driver stops at Q and R).  Least
  * squares min ||A x - b||_2 for a full-rank dA (M >= N, tile layout of this
@@ -152,6 +166,20 @@ int hqr_ormqr_t(hqr_plan_t *plan, const double *dRY, const double *dTAU, double 
  * TAU, the packed right-hand sides); synchronous. */
 int hqr_lstsq(hqr_plan_t *plan, const double *dA, const double *dB, int ldb, int nrhs, double *dX,
               int ldx, int refine_steps, double *resid, void *stream);
+/* No counterpart in the reference.  hqr_lstsq's arguments and result, refined
+ * on the augmented system [I A; A^T 0][r; x] = [b; 0] (Bjorck): x0 and r0 =
+ * b - A x0 as above, then each of refine_steps steps forms f = b - r - A x
+ * and g = -A^T r in FP64 and solves for the correction with the factorization:
+ * h = R^-T g, d = Q^T f (hqr_ormqr_t), x += R^-1 (d(1:N) - h), r += Q [h;
+ * d(N+1:M)] (hqr_ormqr_n).  The limit of x is the FP64 least-squares
+ * solution's accuracy (about kappa(A) u in FP64, plus kappa^2 u ||r|| /
+ * (||A|| ||x||)) whatever the factorization's precision, as long as the
+ * factorization's error times kappa(A) stays below about 0.1; hqr_lstsq's
+ * refinement stalls at the factorization's error times kappa(A) ||r|| /
+ * (||A|| ||x||) instead.  HQR_ERR_UNSUPPORTED with a domain tree.  Allocates;
+ * synchronous. */
+int hqr_lstsq_aug(hqr_plan_t *plan, const double *dA, const double *dB, int ldb, int nrhs, double *dX,
+                  int ldx, int refine_steps, double *resid, void *stream);
 
 /* No counterpart in the reference (it factors one matrix per run).  A batch
  * of independent FP64 tile QRs of uneven shapes, each run of the batch one

@@ -180,28 +180,67 @@ def dgemm_tn(A: np.ndarray, B: np.ndarray, M: int, N: int, NB: int):
 
 
 def lstsq(A_tiles: np.ndarray, B: np.ndarray, M: int, N: int, NB: int, IB: int,
-          refine_steps: int = 1) -> np.ndarray:
+          refine_steps: int = 1, factor_tiles: np.ndarray | None = None) -> np.ndarray:
     """The least-squares solve of hqr_lstsq restated on the CPU: the oracle's
     tile QR of A, c = Q^T b by its dormqr, back substitution with R, then
     ``refine_steps`` FP64 refinement steps x += R^-1 (Q^T (b - A x))(1:N).
-    B: (M, nrhs) array; returns x as an (N, nrhs) array."""
+    B: (M, nrhs) array; returns x as an (N, nrhs) array.  factor_tiles: a
+    perturbed A to factor instead (a stand-in for a lower-precision
+    factorization); residuals always use A."""
     from scipy.linalg import solve_triangular
     B = np.asarray(B, dtype=np.float64).reshape(M, -1)
     nrhs = B.shape[1]
-    CT = (nrhs + NB - 1) // NB
     A2d = from_tiles(A_tiles, M, N, NB)
-    RY, TAU = tile_qr(A_tiles, M, N, NB, IB)
-    R = np.triu(from_tiles(RY, M, N, NB)[:N, :N])
+    qt, R = _ls_factor(A_tiles if factor_tiles is None else factor_tiles, M, N, NB, IB, nrhs)
 
     def solve(rhs):
-        pad = np.zeros((M, CT * NB))
-        pad[:, :nrhs] = rhs
-        c = from_tiles(dormqr(RY, TAU, to_tiles(pad, NB), M, N, NB, CT), M, CT * NB, NB)
-        return solve_triangular(R, c[:N, :nrhs], lower=False)
+        return solve_triangular(R, qt(rhs)[:N], lower=False)
 
     x = solve(B)
     for _ in range(refine_steps):
         x = x + solve(B - A2d @ x)
+    return x
+
+
+def _ls_factor(F_tiles, M, N, NB, IB, nrhs):
+    """Tile QR of F: (x -> Q^T x through the oracle's dormqr, R)."""
+    CT = (nrhs + NB - 1) // NB
+    RY, TAU = tile_qr(F_tiles, M, N, NB, IB)
+    R = np.triu(from_tiles(RY, M, N, NB)[:N, :N])
+
+    def qt(rhs):
+        pad = np.zeros((M, CT * NB))
+        pad[:, :nrhs] = rhs
+        return from_tiles(dormqr(RY, TAU, to_tiles(pad, NB), M, N, NB, CT), M, CT * NB, NB)[:, :nrhs]
+
+    return qt, R
+
+
+def lstsq_aug(A_tiles: np.ndarray, B: np.ndarray, M: int, N: int, NB: int, IB: int,
+              refine_steps: int = 2, factor_tiles: np.ndarray | None = None) -> np.ndarray:
+    """hqr_lstsq_aug restated: x0 as in lstsq, r0 = b - A x0, then
+    ``refine_steps`` steps of refinement on the augmented system
+    [I A; A^T 0][r; x] = [b; 0] (Bjorck, BIT 7 (1967) 257-278): f = b - r -
+    A x, g = -A^T r in FP64; h = R^-T g, d = Q^T f, x += R^-1 (d(1:N) - h),
+    r += Q [h; d(N+1:M)].  Q is applied as the transpose of the oracle's
+    Q^T of the identity (small cases only).  factor_tiles as in lstsq."""
+    from scipy.linalg import solve_triangular
+    B = np.asarray(B, dtype=np.float64).reshape(M, -1)
+    nrhs = B.shape[1]
+    A2d = from_tiles(A_tiles, M, N, NB)
+    F = A_tiles if factor_tiles is None else factor_tiles
+    qt, R = _ls_factor(F, M, N, NB, IB, nrhs)
+    qt_full, _ = _ls_factor(F, M, N, NB, IB, M)
+    QT = qt_full(np.eye(M))
+    x = solve_triangular(R, qt(B)[:N], lower=False)
+    r = B - A2d @ x
+    for _ in range(refine_steps):
+        f = B - r - A2d @ x
+        g = -(A2d.T @ r)
+        h = solve_triangular(R, g, trans="T", lower=False)
+        d = qt(f)
+        x = x + solve_triangular(R, d[:N] - h, lower=False)
+        r = r + QT.T @ np.vstack([h, d[N:]])
     return x
 
 

@@ -6,9 +6,9 @@ import numpy as np
 EPS = np.finfo(np.float64).eps
 
 
-def ls_problem(M, N, nrhs, kappa, seed):
+def ls_problem(M, N, nrhs, kappa, seed, noise=1e-8):
     """A = U S V^T with Haar U, V (QR of Gaussians, signs fixed by diag R) and
-    singular values geometric from 1 to 1/kappa; x ~ N(0,1); b = A x + 1e-8 N(0,1)."""
+    singular values geometric from 1 to 1/kappa; x ~ N(0,1); b = A x + noise N(0,1)."""
     rng = np.random.default_rng(seed)
 
     def haar(m, n):
@@ -19,7 +19,7 @@ def ls_problem(M, N, nrhs, kappa, seed):
     s = kappa ** (-np.arange(N) / max(N - 1, 1))
     A = (U * s) @ V.T
     x = rng.standard_normal((N, nrhs))
-    b = A @ x + 1e-8 * rng.standard_normal((M, nrhs))
+    b = A @ x + noise * rng.standard_normal((M, nrhs))
     return A, x, b
 
 

@@ -1,9 +1,10 @@
-"""use_plan_t of hqr_make_q / hqr_ormqr_t: after hqr_geqrf on a plan, Q^T C
-reuses the factorization's T factors (FP64) or prepared operands (split
-precision) -- no panel task runs -- and so does Q generation in FP64; split
-Q generation applies H, not H^T, and prepares its own operands.  Results are
-the oracle's; once a call has rebuilt the plan's factors from other
-reflectors, use_plan_t = 1 rebuilds again instead of using stale ones.
+"""use_plan_t of hqr_make_q / hqr_ormqr_t / hqr_ormqr_n: after hqr_geqrf on a
+plan, Q^T C reuses the factorization's T factors (FP64) or prepared operands
+(split precision) -- no panel task runs -- and so does Q generation in FP64.
+Split Q generation and Q C apply H, not H^T: the first such call prepares the
+plan's H operand set, later ones reuse it.  Results are the oracle's; once a
+call has rebuilt a set from other reflectors, use_plan_t = 1 rebuilds that set
+again instead of using stale operands (the other set stays valid).
 
 Elementwise bar as in the other parity tests: n * eps * ||A||_F for Q, 4x that
 of ||C||_F for Q^T C.
@@ -63,6 +64,15 @@ def test_q_from_the_plans_factors(env, NB, IB, prec):
                 "ormqr")
         return dC.cpu().numpy(), plan.stats()
 
+    def ormqr_n(use):
+        dC = torch.from_numpy(C.copy()).cuda()
+        H.check(L.hqr_ormqr_n(plan.h, dA.data_ptr(), dTAU.data_ptr(), dC.data_ptr(), N // NB, use, None),
+                "ormqr_n")
+        return dC.cpu().numpy(), plan.stats()
+
+    # Q C = (Q^T)^T C from the oracle's Q^T (tile layout, M = N)
+    qt2d = O.from_tiles(oq, M, N, NB)
+    oqc = O.to_tiles(qt2d.T @ C2d, NB)
     panels = (M // NB) * (M // NB + 1) // 2
     # reuse: no panel tasks for Q^T C; Q generation too in FP64
     c, st = ormqr(1)
@@ -71,17 +81,37 @@ def test_q_from_the_plans_factors(env, NB, IB, prec):
     q, st = make_q(1)
     assert st["count"][panel_slot] == (panels if prec else 0)
     assert np.abs(q - oq).max() <= tol(A2d)
-    # a rebuild replaces the plan's factors; use_plan_t = 1 then rebuilds too
+    # the H set, once prepared, serves Q generation and Q C alike
+    q, st = make_q(1)
+    assert st["count"][panel_slot] == 0
+    assert np.abs(q - oq).max() <= tol(A2d)
+    c, st = ormqr_n(1)
+    assert st["count"][panel_slot] == 0
+    assert np.abs(c - oqc).max() <= 4 * tol(C2d)
+    # a rebuild replaces the set it used; use_plan_t = 1 then rebuilds that set
     q, st = make_q(0)
     assert st["count"][panel_slot] == panels
     assert np.abs(q - oq).max() <= tol(A2d)
+    c, st = ormqr_n(1)
+    assert st["count"][panel_slot] == panels
+    assert np.abs(c - oqc).max() <= 4 * tol(C2d)
+    # split: the H^T set was untouched; FP64: one set, rebuilt just now
     c, st = ormqr(1)
-    assert st["count"][panel_slot] > 0
+    assert st["count"][panel_slot] == 0
     assert np.abs(c - oc).max() <= 4 * tol(C2d)
-    # a new factorization makes them reusable again
+    c, st = ormqr(0)
+    assert st["count"][panel_slot] == panels
+    c, st = ormqr(1)
+    assert st["count"][panel_slot] == panels
+    assert np.abs(c - oc).max() <= 4 * tol(C2d)
+    # a new factorization makes both sets reusable again (the H set after its
+    # first preparation)
     dA.copy_(torch.from_numpy(A.copy()))
     H.check(L.hqr_geqrf(plan.h, dA.data_ptr(), dTAU.data_ptr(), None), "geqrf")
     c, st = ormqr(1)
     assert st["count"][panel_slot] == 0
     assert np.abs(c - oc).max() <= 4 * tol(C2d)
+    c, st = ormqr_n(1)
+    assert st["count"][panel_slot] == (panels if prec else 0)
+    assert np.abs(c - oqc).max() <= 4 * tol(C2d)
     plan.close()
