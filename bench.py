@@ -475,21 +475,27 @@ def measure_e2e(H, torch, L, precision: str, n: int, NB: int, IB: int, steps: in
             "api": "Hybrid_tile_QR + Hybrid_make_Q (page-locked host arrays from hqr_host_alloc)"}
 
 
-def lstsq_flops(m: int, n: int, nrhs: int, refine: int) -> float:
+def lstsq_flops(m: int, n: int, nrhs: int, refine: int, augmented: bool = False) -> float:
     """Algorithmic flops of hqr_lstsq: QR, then per solve Q^T b (4mn - 2n^2 per
     right-hand side) and back substitution (n^2), per refinement step a
-    residual (2mn)."""
+    residual (2mn).  hqr_lstsq_aug: the first solve and residual, then per
+    step b - A x (2mn), A^T r (2mn), Q^T f and Q [h; d2] (4mn - 2n^2 each)
+    and two triangular solves (n^2 each)."""
     per_solve = (4.0 * m * n - 2.0 * n * n + n * n) * nrhs
+    if augmented:
+        per_step = (2 * 2.0 * m * n + 2 * (4.0 * m * n - 2.0 * n * n) + 2.0 * n * n) * nrhs
+        return qr_flops(m, n) + per_solve + 2.0 * m * n * nrhs + refine * per_step
     return qr_flops(m, n) + (refine + 1) * per_solve + refine * 2.0 * m * n * nrhs
 
 
 def run_lstsq(H, torch, L, args):
-    """Least squares min ||A x - b|| through hqr_lstsq: A (m x n) = U diag(sigma)
-    V^T with Haar U, V and sigma geometric from 1 to 1/kappa, x_true ~ N(0,1),
-    b = A x_true + 1e-8 N(0,1), nrhs right-hand sides; inputs generated with
-    torch on the device, outside the timed region.  Timed: whole hqr_lstsq
-    calls (copy of A, QR, Q^T b, back substitution, refinement).  Checked
-    against an FP64 least-squares solution of the same problem
+    """Least squares min ||A x - b|| through hqr_lstsq (hqr_lstsq_aug with
+    --refine-method augmented): A (m x n) = U diag(sigma) V^T with Haar U, V
+    and sigma geometric from 1 to 1/kappa, x_true ~ N(0,1), b = A x_true +
+    noise N(0,1) (--noise, default 1e-8), nrhs right-hand sides; inputs
+    generated with torch on the device, outside the timed region.  Timed:
+    whole calls (copy of A, QR, Q^T b, back substitution, refinement).
+    Checked against an FP64 least-squares solution of the same problem
     (torch.linalg.lstsq, check only) and against x_true."""
     m, n, nrhs, NB, IB = args.m, args.n, args.nrhs, args.nb, args.ib
     kappa = args.kappa if args.kappa is not None else 1e3
@@ -509,7 +515,7 @@ def run_lstsq(H, torch, L, args):
     A = U @ haar(n, n).T
     del U
     x_true = torch.randn(n, nrhs, dtype=f64, device="cuda", generator=gen)
-    b = A @ x_true + 1e-8 * torch.randn(m, nrhs, dtype=f64, device="cuda", generator=gen)
+    b = A @ x_true + args.noise * torch.randn(m, nrhs, dtype=f64, device="cuda", generator=gen)
     cm = A.T.contiguous()                       # column-major storage of A
     dA = torch.empty(m * n, dtype=f64, device="cuda")
     H.check(L.hqr_colmajor_to_tiles(m, n, NB, cm.data_ptr(), dA.data_ptr(), None), "to tiles")
@@ -519,16 +525,18 @@ def run_lstsq(H, torch, L, args):
     plan = H.Plan(m, n, NB, IB, prec)
     if args.tree:
         plan.set_tree(args.tree)
+    aug = args.refine_method == "augmented"
     torch.cuda.synchronize()
     for _ in range(args.warmup):
-        plan.lstsq(dA.data_ptr(), dB.data_ptr(), nrhs, dX.data_ptr(), refine_steps=args.refine)
+        plan.lstsq(dA.data_ptr(), dB.data_ptr(), nrhs, dX.data_ptr(), refine_steps=args.refine, augmented=aug)
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e0.record()
     for _ in range(args.steps):
-        res = plan.lstsq(dA.data_ptr(), dB.data_ptr(), nrhs, dX.data_ptr(), refine_steps=args.refine)
+        res = plan.lstsq(dA.data_ptr(), dB.data_ptr(), nrhs, dX.data_ptr(), refine_steps=args.refine,
+                         augmented=aug)
     e1.record()
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -537,7 +545,7 @@ def run_lstsq(H, torch, L, args):
     x = dX.T
     x_ref = torch.linalg.lstsq(A, b).solution
     rel = lambda a, r: float(torch.linalg.norm(a - r) / torch.linalg.norm(r))
-    flops = lstsq_flops(m, n, nrhs, args.refine)
+    flops = lstsq_flops(m, n, nrhs, args.refine, aug)
     line = {
         "metric": "least-squares solve TFLOP/s (QR + Q^T b + back substitution + FP64 refinement)",
         "value": round(flops / elapsed / 1e12, 6), "unit": "TFLOP/s", "n_gpus": 1,
@@ -545,9 +553,11 @@ def run_lstsq(H, torch, L, args):
         "higher_is_better": True, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"least squares, A {m}x{n} = U diag(sigma) V^T (Haar U, V, sigma "
                                f"geometric 1..1/kappa), kappa={kappa:g}, {nrhs} right-hand sides, "
-                               f"b = A x_true + 1e-8 noise",
+                               f"b = A x_true + {args.noise:g} noise",
                    "m": m, "n": n, "nrhs": nrhs, "kappa": kappa, "NB": NB, "IB": IB,
                    "refine_steps": args.refine, "tree_domain_tiles": args.tree,
+                   "refine_method": ("augmented system (hqr_lstsq_aug)" if aug else
+                                     "x += R^-1 Q^T (b - A x) (hqr_lstsq)"),
                    "precision": PRECISION_TEXT[args.precision]},
         "accuracy": {"forward_error_vs_fp64_lstsq": rel(x, x_ref),
                      "forward_error_vs_x_true": rel(x, x_true),
@@ -875,6 +885,10 @@ def main():
     ap.add_argument("--m", type=int, default=32768, help="rows of A for --lstsq")
     ap.add_argument("--nrhs", type=int, default=16, help="right-hand sides for --lstsq")
     ap.add_argument("--refine", type=int, default=1, help="FP64 refinement steps for --lstsq")
+    ap.add_argument("--refine-method", default="plain", choices=["plain", "augmented"],
+                    help="--lstsq refinement: hqr_lstsq (plain) or hqr_lstsq_aug (augmented system)")
+    ap.add_argument("--noise", type=float, default=1e-8,
+                    help="--lstsq: b = A x_true + noise N(0,1) (the least-squares residual's size)")
     ap.add_argument("--rows", type=int, default=None,
                     help="rows of A for the QR + make_Q workload (default: square, --n)")
     ap.add_argument("--batched", action="store_true",

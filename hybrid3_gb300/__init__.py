@@ -134,6 +134,7 @@ SIGNATURES = {
     "hqr_dropin_phase_ms": (_I, [ctypes.POINTER(ctypes.c_double)]),
     "hqr_host_alloc": (_I, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]),
     "hqr_ormqr_n": (_I, [_vp, _vp, _vp, _vp, _I, _I, _vp]),
+    "hqr_ormqr_t_async": (_I, [_vp, _vp, _vp, _vp, _I, _I, _vp]),
     "hqr_ormqr_n_async": (_I, [_vp, _vp, _vp, _vp, _I, _I, _vp]),
     "hqr_host_free": (_I, [_vp]),
     "hqr_ozaki_product": (_I, [_I, _vp, _vp, _vp, _vp]),

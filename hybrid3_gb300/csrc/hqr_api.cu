@@ -34,6 +34,10 @@ struct hqr_plan {
   // replaces them)
   int factors_valid = 0;
   int h_valid = 0;
+  // least-squares workspace (hqr_lstsq, hqr_lstsq_aug), grow-only, kept
+  // between calls so that a solve allocates nothing after the first
+  double* ls[9] = {};
+  size_t ls_cap[9] = {};
 };
 
 namespace {
@@ -372,6 +376,7 @@ int hqr_plan_destroy(hqr_plan_t* plan) {
   if (plan->ozh.slices) cudaFree(plan->ozh.slices);
   if (plan->ozh.sexp) cudaFree(plan->ozh.sexp);
   hqr::dag_workspace_free(&plan->ws);
+  for (double* p : plan->ls) cudaFree(p);
   delete plan;
   return HQR_OK;
 }
@@ -426,19 +431,23 @@ int hqr_make_q(hqr_plan_t* plan, double* dQ, double* dRY, const double* dTAU, in
   return hqr_plan_status(plan, stream);
 }
 
-int hqr_ormqr_t(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT,
-                int use_plan_t, void* stream) {
+int hqr_ormqr_t_async(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT,
+                      int use_plan_t, void* stream) {
   if (!plan || !dRY || !dTAU || !dC || CT <= 0) return HQR_ERR_INVALID;
   if (plan->tree.S > 0) {
     if (!use_plan_t) return HQR_ERR_UNSUPPORTED;   // the merges' T factors live in the plan
-    TRY(hqr::launch_apply_qt_tree(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, g_timeout_ns,
-                                  (cudaStream_t)stream, &plan->oz, &plan->tree));
-  } else {
-    bool rebuild;
-    const hqr::OzWorkspace* oz = apply_operands(plan, false, use_plan_t != 0, &rebuild);
-    TRY(hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, rebuild, g_timeout_ns,
-                             (cudaStream_t)stream, oz));
+    return hqr::launch_apply_qt_tree(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, g_timeout_ns,
+                                     (cudaStream_t)stream, &plan->oz, &plan->tree);
   }
+  bool rebuild;
+  const hqr::OzWorkspace* oz = apply_operands(plan, false, use_plan_t != 0, &rebuild);
+  return hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, rebuild, g_timeout_ns,
+                              (cudaStream_t)stream, oz);
+}
+
+int hqr_ormqr_t(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT,
+                int use_plan_t, void* stream) {
+  TRY(hqr_ormqr_t_async(plan, dRY, dTAU, dC, CT, use_plan_t, stream));
   return hqr_plan_status(plan, stream);
 }
 
@@ -460,24 +469,60 @@ int hqr_ormqr_n(hqr_plan_t* plan, const double* dRY, const double* dTAU, double*
 }
 
 namespace {
-// Device workspace of one least-squares call, freed on every return path.
-struct LstsqWork {
-  double* Af = nullptr;   // the factored copy of A
-  double* tau = nullptr;
-  double* C = nullptr;    // right-hand sides / residuals in tile layout
-  double* R = nullptr;    // residual, column-major M x nrhs
-  double* nrm = nullptr;
-  // augmented-system refinement only
-  double* G = nullptr;    // [h; d2] in tile layout, then the residual's correction
-  double* r = nullptr;    // the refined least-squares residual, column-major M x nrhs
-  double* g = nullptr;    // -A^T r, column-major N x nrhs
-  double* P = nullptr;    // partial sums of A^T r
-  ~LstsqWork() {
-    for (double* p : {Af, tau, C, R, nrm, G, r, g, P}) cudaFree(p);
-  }
+// The plan's least-squares buffers.
+enum LsBuf {
+  kLsAf,    // the factored copy of A
+  kLsTau,
+  kLsC,     // right-hand sides / residuals in tile layout
+  kLsG,     // [h; d2] in tile layout, then the residual's correction (augmented)
+  kLsRes,   // b - A x, column-major M x nrhs
+  kLsR,     // the refined least-squares residual r, column-major M x nrhs (augmented)
+  kLsAtr,   // -A^T r, column-major N x nrhs (augmented)
+  kLsPart,  // partial sums of A^T r (augmented)
+  kLsNrm,
 };
-int dmalloc(double** p, size_t n) {
-  return cudaMalloc(p, n * sizeof(double)) == cudaSuccess ? HQR_OK : HQR_ERR_NOMEM;
+int ls_buf(hqr_plan* plan, LsBuf which, size_t n, double** out) {
+  if (plan->ls_cap[which] < n) {
+    cudaFree(plan->ls[which]);
+    plan->ls[which] = nullptr;
+    plan->ls_cap[which] = 0;
+    if (cudaMalloc(&plan->ls[which], n * sizeof(double)) != cudaSuccess) return HQR_ERR_NOMEM;
+    plan->ls_cap[which] = n;
+  }
+  *out = plan->ls[which];
+  return HQR_OK;
+}
+
+// Common start of both solves: A copied and factored, x0 = R^-1 (Q^T b)(1:N)
+// in dX; all enqueued on s.
+int ls_start(hqr_plan* plan, const double* dA, const double* dB, int ldb, int nrhs, double* dX, int ldx,
+             double* Af, double* tau, double* C, cudaStream_t s) {
+  const hqr::Geometry& g = plan->g;
+  const int CT = (nrhs + g.NB - 1) / g.NB;
+  TRY(cuda_rc(cudaMemcpyAsync(Af, dA, (size_t)g.M * g.N * sizeof(double), cudaMemcpyDeviceToDevice, s)));
+  TRY(hqr_geqrf_async(plan, Af, tau, s));
+  hqr::pack_rhs(dB, ldb, nrhs, C, g.M, g.NB, CT, s);
+  TRY(cuda_rc(cudaGetLastError()));
+  TRY(hqr_ormqr_t_async(plan, Af, tau, C, CT, 1, s));
+  TRY(hqr::trsm_tiles(Af, g.M, g.N, g.NB, C, nrhs, s));
+  hqr::update_x(C, g.M, g.NB, g.N, nrhs, dX, ldx, false, s);
+  return cuda_rc(cudaGetLastError());
+}
+
+// End of both solves: the scheduler's status, then ||b - A x||_2 per
+// right-hand side into resid (host) if it is not null.
+int ls_finish(hqr_plan* plan, const double* dA, const double* dB, int ldb, int nrhs, const double* dX,
+              int ldx, double* Res, double* nrm, double* resid, cudaStream_t s) {
+  const hqr::Geometry& g = plan->g;
+  if (resid) {
+    TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, Res, g.M, nrhs, s));
+    hqr::col_norm2(Res, g.M, g.M, nrhs, nrm, s);
+    TRY(cuda_rc(cudaMemcpyAsync(resid, nrm, (size_t)nrhs * sizeof(double), cudaMemcpyDeviceToHost, s)));
+  }
+  TRY(hqr_plan_status(plan, s));
+  if (resid)
+    for (int q = 0; q < nrhs; q++) resid[q] = sqrt(resid[q]);
+  return HQR_OK;
 }
 }  // namespace
 
@@ -488,36 +533,23 @@ int hqr_lstsq(hqr_plan_t* plan, const double* dA, const double* dB, int ldb, int
   if (g.M < g.N || ldb < g.M || ldx < g.N) return HQR_ERR_INVALID;
   cudaStream_t s = (cudaStream_t)stream;
   const int CT = (nrhs + g.NB - 1) / g.NB;
-  LstsqWork w;
-  TRY(dmalloc(&w.Af, (size_t)g.M * g.N));
-  TRY(dmalloc(&w.tau, tau_len(g)));
-  TRY(dmalloc(&w.C, (size_t)g.M * CT * g.NB));
-  TRY(dmalloc(&w.R, (size_t)g.M * nrhs));
-  TRY(dmalloc(&w.nrm, (size_t)nrhs));
-  TRY(cuda_rc(cudaMemcpyAsync(w.Af, dA, (size_t)g.M * g.N * sizeof(double), cudaMemcpyDeviceToDevice, s)));
-  TRY(hqr_geqrf(plan, w.Af, w.tau, stream));
-  for (int it = 0; it <= refine_steps; it++) {
-    if (it == 0) {
-      hqr::pack_rhs(dB, ldb, nrhs, w.C, g.M, g.NB, CT, s);
-    } else {
-      TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, w.R, g.M, nrhs, s));
-      hqr::pack_rhs(w.R, g.M, nrhs, w.C, g.M, g.NB, CT, s);
-    }
+  double *Af, *tau, *C, *Res, *nrm;
+  TRY(ls_buf(plan, kLsAf, (size_t)g.M * g.N, &Af));
+  TRY(ls_buf(plan, kLsTau, tau_len(g), &tau));
+  TRY(ls_buf(plan, kLsC, (size_t)g.M * CT * g.NB, &C));
+  TRY(ls_buf(plan, kLsRes, (size_t)g.M * nrhs, &Res));
+  TRY(ls_buf(plan, kLsNrm, (size_t)nrhs, &nrm));
+  TRY(ls_start(plan, dA, dB, ldb, nrhs, dX, ldx, Af, tau, C, s));
+  for (int it = 1; it <= refine_steps; it++) {
+    TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, Res, g.M, nrhs, s));
+    hqr::pack_rhs(Res, g.M, nrhs, C, g.M, g.NB, CT, s);
     TRY(cuda_rc(cudaGetLastError()));
-    TRY(hqr_ormqr_t(plan, w.Af, w.tau, w.C, CT, 1, stream));
-    TRY(hqr::trsm_tiles(w.Af, g.M, g.N, g.NB, w.C, nrhs, s));
-    hqr::update_x(w.C, g.M, g.NB, g.N, nrhs, dX, ldx, it > 0, s);
+    TRY(hqr_ormqr_t_async(plan, Af, tau, C, CT, 1, s));
+    TRY(hqr::trsm_tiles(Af, g.M, g.N, g.NB, C, nrhs, s));
+    hqr::update_x(C, g.M, g.NB, g.N, nrhs, dX, ldx, true, s);
     TRY(cuda_rc(cudaGetLastError()));
   }
-  if (resid) {
-    TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, w.R, g.M, nrhs, s));
-    hqr::col_norm2(w.R, g.M, g.M, nrhs, w.nrm, s);
-    TRY(cuda_rc(cudaMemcpyAsync(resid, w.nrm, (size_t)nrhs * sizeof(double), cudaMemcpyDeviceToHost, s)));
-  }
-  TRY(cuda_rc(cudaStreamSynchronize(s)));
-  if (resid)
-    for (int q = 0; q < nrhs; q++) resid[q] = sqrt(resid[q]);
-  return HQR_OK;
+  return ls_finish(plan, dA, dB, ldb, nrhs, dX, ldx, Res, nrm, resid, s);
 }
 
 // Bjorck's refinement on the augmented system [I A; A^T 0][r; x] = [b; 0]:
@@ -534,57 +566,42 @@ int hqr_lstsq_aug(hqr_plan_t* plan, const double* dA, const double* dB, int ldb,
   cudaStream_t s = (cudaStream_t)stream;
   const int CT = (nrhs + g.NB - 1) / g.NB;
   const int S = hqr::atr_slices(g.M, g.N, g.NB, nrhs);
-  LstsqWork w;
-  TRY(dmalloc(&w.Af, (size_t)g.M * g.N));
-  TRY(dmalloc(&w.tau, tau_len(g)));
-  TRY(dmalloc(&w.C, (size_t)g.M * CT * g.NB));
-  TRY(dmalloc(&w.G, (size_t)g.M * CT * g.NB));
-  TRY(dmalloc(&w.R, (size_t)g.M * nrhs));
-  TRY(dmalloc(&w.r, (size_t)g.M * nrhs));
-  TRY(dmalloc(&w.g, (size_t)g.N * nrhs));
-  TRY(dmalloc(&w.P, (size_t)S * g.N * nrhs));
-  TRY(dmalloc(&w.nrm, (size_t)nrhs));
-  TRY(cuda_rc(cudaMemcpyAsync(w.Af, dA, (size_t)g.M * g.N * sizeof(double), cudaMemcpyDeviceToDevice, s)));
-  TRY(hqr_geqrf(plan, w.Af, w.tau, stream));
-  // x0 = R^-1 (Q^T b)(1:N), r0 = b - A x0
-  hqr::pack_rhs(dB, ldb, nrhs, w.C, g.M, g.NB, CT, s);
-  TRY(cuda_rc(cudaGetLastError()));
-  TRY(hqr_ormqr_t(plan, w.Af, w.tau, w.C, CT, 1, stream));
-  TRY(hqr::trsm_tiles(w.Af, g.M, g.N, g.NB, w.C, nrhs, s));
-  hqr::update_x(w.C, g.M, g.NB, g.N, nrhs, dX, ldx, false, s);
-  TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, w.r, g.M, nrhs, s));
+  double *Af, *tau, *C, *G, *Res, *r, *atr, *part, *nrm;
+  TRY(ls_buf(plan, kLsAf, (size_t)g.M * g.N, &Af));
+  TRY(ls_buf(plan, kLsTau, tau_len(g), &tau));
+  TRY(ls_buf(plan, kLsC, (size_t)g.M * CT * g.NB, &C));
+  TRY(ls_buf(plan, kLsG, (size_t)g.M * CT * g.NB, &G));
+  TRY(ls_buf(plan, kLsRes, (size_t)g.M * nrhs, &Res));
+  TRY(ls_buf(plan, kLsR, (size_t)g.M * nrhs, &r));
+  TRY(ls_buf(plan, kLsAtr, (size_t)g.N * nrhs, &atr));
+  TRY(ls_buf(plan, kLsPart, (size_t)S * g.N * nrhs, &part));
+  TRY(ls_buf(plan, kLsNrm, (size_t)nrhs, &nrm));
+  TRY(ls_start(plan, dA, dB, ldb, nrhs, dX, ldx, Af, tau, C, s));
+  TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, r, g.M, nrhs, s));   // r0 = b - A x0
   const int MT = (int)(g.M / g.NB), NT = (int)(g.N / g.NB);
   for (int it = 0; it < refine_steps; it++) {
     // f = b - A x - r, g = -A^T r
-    TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, w.R, g.M, nrhs, s));
-    hqr::sub_colmajor(w.R, g.M, w.r, g.M, g.M, nrhs, s);
-    TRY(hqr::at_times(dA, g.M, g.N, g.NB, w.r, g.M, nrhs, -1.0, w.g, g.N, w.P, S, s));
+    TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, Res, g.M, nrhs, s));
+    hqr::sub_colmajor(Res, g.M, r, g.M, g.M, nrhs, s);
+    TRY(hqr::at_times(dA, g.M, g.N, g.NB, r, g.M, nrhs, -1.0, atr, g.N, part, S, s));
     // d = Q^T f; h = R^-T g
-    hqr::pack_rhs(w.R, g.M, nrhs, w.C, g.M, g.NB, CT, s);
+    hqr::pack_rhs(Res, g.M, nrhs, C, g.M, g.NB, CT, s);
     TRY(cuda_rc(cudaGetLastError()));
-    TRY(hqr_ormqr_t(plan, w.Af, w.tau, w.C, CT, 1, stream));
-    hqr::pack_rhs_rows(w.g, g.N, nrhs, g.N, w.G, g.M, g.NB, CT, s);
-    TRY(hqr::trsmt_tiles(w.Af, g.M, g.N, g.NB, w.G, nrhs, s));
+    TRY(hqr_ormqr_t_async(plan, Af, tau, C, CT, 1, s));
+    hqr::pack_rhs_rows(atr, g.N, nrhs, g.N, G, g.M, g.NB, CT, s);
+    TRY(hqr::trsmt_tiles(Af, g.M, g.N, g.NB, G, nrhs, s));
     // G = [h; d2], C = [d1 - h; d2]
-    hqr::tile_rows(w.C, w.G, g.M, g.NB, CT, NT, MT, false, s);
-    hqr::tile_rows(w.C, w.G, g.M, g.NB, CT, 0, NT, true, s);
+    hqr::tile_rows(C, G, g.M, g.NB, CT, NT, MT, false, s);
+    hqr::tile_rows(C, G, g.M, g.NB, CT, 0, NT, true, s);
     // x += R^-1 (d1 - h); r += Q [h; d2]
-    TRY(hqr::trsm_tiles(w.Af, g.M, g.N, g.NB, w.C, nrhs, s));
-    hqr::update_x(w.C, g.M, g.NB, g.N, nrhs, dX, ldx, true, s);
+    TRY(hqr::trsm_tiles(Af, g.M, g.N, g.NB, C, nrhs, s));
+    hqr::update_x(C, g.M, g.NB, g.N, nrhs, dX, ldx, true, s);
     TRY(cuda_rc(cudaGetLastError()));
-    TRY(hqr_ormqr_n(plan, w.Af, w.tau, w.G, CT, 1, stream));
-    hqr::add_unpack(w.r, g.M, w.G, g.M, g.NB, nrhs, s);
+    TRY(hqr_ormqr_n_async(plan, Af, tau, G, CT, 1, s));
+    hqr::add_unpack(r, g.M, G, g.M, g.NB, nrhs, s);
     TRY(cuda_rc(cudaGetLastError()));
   }
-  if (resid) {
-    TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, w.R, g.M, nrhs, s));
-    hqr::col_norm2(w.R, g.M, g.M, nrhs, w.nrm, s);
-    TRY(cuda_rc(cudaMemcpyAsync(resid, w.nrm, (size_t)nrhs * sizeof(double), cudaMemcpyDeviceToHost, s)));
-  }
-  TRY(cuda_rc(cudaStreamSynchronize(s)));
-  if (resid)
-    for (int q = 0; q < nrhs; q++) resid[q] = sqrt(resid[q]);
-  return HQR_OK;
+  return ls_finish(plan, dA, dB, ldb, nrhs, dX, ldx, Res, nrm, resid, s);
 }
 
 int hqr_dgemm_tn(long N, int NB, const double* dA, const double* dB, double* dC, void* stream) {

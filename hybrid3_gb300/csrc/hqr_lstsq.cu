@@ -177,180 +177,123 @@ __global__ void k_col_norm2(const double* __restrict__ R, long M, long ldr, doub
   }
 }
 
+// The two triangular solves give each block ONE right-hand side: FP64 issues
+// at about one warp instruction per 70 cycles per SM sub-partition on this
+// part, so a block that carried several columns through the serial diagonal
+// solve spent most of each step there; one column per block spreads a step
+// over nrhs times more SMs.  The diagonal solve multiplies by the reciprocal
+// of each diagonal element, taken once per row by its own thread.
+//
 // One step of the back substitution R Y = C over the first NT tile rows of C
-// (tile layout, MT tile rows; tile column blockIdx.y holds ncol(y) valid
-// columns).  For i < NT, block k < i first updates C_k -= R_ki Y_i (Y_i =
-// tile row i of C, solved by the step before); then block k = i - 1 solves
-// R_kk Y_k = C_k in place.  i = NT: only the diagonal solve of tile row NT-1.
-// RA: the factored A, R in the upper triangle of its tiles (k <= i).
-// Thread r owns row r of the tile (NB threads).
+// (tile layout, MT tile rows), right-hand side q = blockIdx.y: step i < NT
+// first updates blocks k < i, C_k -= R_ki Y_i (Y_i solved by the step before),
+// then block k = i - 1 solves R_kk Y_k = C_k in place; step NT only solves
+// block NT - 1.  RA: the factored A (R in its upper tiles).  Thread r owns
+// row r of the tile (NB threads).
 __global__ void k_trsm_step(const double* __restrict__ RA, int MT, int NB, double* __restrict__ C,
-                            int i, int NT, int nrhs) {
-  extern __shared__ double sm[];   // NB x kRhsChunk right operand / NB x kRBlock R columns + 2 x kRhsChunk
+                            int i, int NT) {
+  extern __shared__ double sm[];   // NB values of Y_i / NB x kRBlock columns of R_kk + 2
   const int k = (i < NT) ? (int)blockIdx.x : NT - 1;
-  const int tj = blockIdx.y;
-  const int ncol = min(NB, nrhs - tj * NB);
+  const int q = blockIdx.y, tj = q / NB, cw = q % NB;
   const int r = threadIdx.x;
   const long tile = (long)NB * NB;
-  double* Ck = C + ((long)k + (long)tj * MT) * tile;
+  double* Ck = C + ((long)k + (long)tj * MT) * tile + (long)cw * NB;
   if (i < NT) {
     const double* Rki = RA + ((long)k + (long)i * MT) * tile;
-    const double* Yi = C + ((long)i + (long)tj * MT) * tile;
-    for (int c0 = 0; c0 < ncol; c0 += kRhsChunk) {
-      const int nq = min(kRhsChunk, ncol - c0);
-      __syncthreads();
-      for (int e = threadIdx.x; e < NB * kRhsChunk; e += blockDim.x) {
-        const int kk = e % NB, q = e / NB;
-        sm[e] = q < nq ? Yi[kk + (long)(c0 + q) * NB] : 0.0;
-      }
-      __syncthreads();
-      double acc[kRhsChunk];
-#pragma unroll
-      for (int q = 0; q < kRhsChunk; q++) acc[q] = 0.0;
-#pragma unroll 4
-      for (int kk = 0; kk < NB; kk++) {
-        const double a = Rki[r + (long)kk * NB];
-#pragma unroll
-        for (int q = 0; q < kRhsChunk; q++) acc[q] = fma(a, sm[kk + q * NB], acc[q]);
-      }
-#pragma unroll
-      for (int q = 0; q < kRhsChunk; q++)
-        if (q < nq) Ck[r + (long)(c0 + q) * NB] -= acc[q];
+    sm[r] = C[((long)i + (long)tj * MT) * tile + (long)cw * NB + r];
+    __syncthreads();
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    for (int kk = 0; kk < NB; kk += 4) {
+      a0 = fma(Rki[r + (long)kk * NB], sm[kk], a0);
+      a1 = fma(Rki[r + (long)(kk + 1) * NB], sm[kk + 1], a1);
+      a2 = fma(Rki[r + (long)(kk + 2) * NB], sm[kk + 2], a2);
+      a3 = fma(Rki[r + (long)(kk + 3) * NB], sm[kk + 3], a3);
     }
+    Ck[r] -= (a0 + a1) + (a2 + a3);
   }
   if (k != ((i < NT) ? i - 1 : NT - 1) || k < 0) return;
-  // R_kk Y = C_k: rows from the bottom; thread r keeps its row's values in
-  // registers, the solved value of row j is broadcast through a double buffer
-  // (one barrier per row), R's columns are staged kRBlock at a time.
+  // R_kk y = c_k from the bottom row: the solved value of row j is broadcast
+  // through a double buffer (one barrier per row); R's columns are staged
+  // kRBlock at a time (sR[rr + cc NB] = R(rr, jb + cc)).
   __syncthreads();
   const double* Rkk = RA + ((long)k + (long)k * MT) * tile;
-  double* sR = sm;                          // NB x kRBlock
-  double* sy = sm + (long)NB * kRBlock;     // 2 x kRhsChunk
-  for (int c0 = 0; c0 < ncol; c0 += kRhsChunk) {
-    const int nq = min(kRhsChunk, ncol - c0);
-    double v[kRhsChunk];
-#pragma unroll
-    for (int q = 0; q < kRhsChunk; q++) v[q] = q < nq ? Ck[r + (long)(c0 + q) * NB] : 0.0;
-    int buf = 0;
-    for (int jend = NB; jend > 0; jend -= kRBlock) {
-      const int jb = jend > kRBlock ? jend - kRBlock : 0;
-      __syncthreads();
-      for (int e = threadIdx.x; e < NB * (jend - jb); e += blockDim.x) {
-        const int rr = e % NB, cc = e / NB;
-        sR[e] = Rkk[rr + (long)(jb + cc) * NB];
+  double* sR = sm;
+  double* sy = sm + (long)NB * kRBlock;
+  double v = Ck[r];
+  const double inv = 1.0 / Rkk[r + (long)r * NB];
+  int buf = 0;
+  for (int jend = NB; jend > 0; jend -= kRBlock) {
+    const int jb = jend > kRBlock ? jend - kRBlock : 0;
+    __syncthreads();
+    for (int e = threadIdx.x; e < NB * (jend - jb); e += blockDim.x)
+      sR[e] = Rkk[(e % NB) + (long)(jb + e / NB) * NB];
+    __syncthreads();
+    for (int j = jend - 1; j >= jb; j--) {
+      if (r == j) {
+        v *= inv;
+        sy[buf] = v;
       }
       __syncthreads();
-      for (int j = jend - 1; j >= jb; j--) {
-        if (r == j) {
-          const double d = sR[j + (j - jb) * NB];
-#pragma unroll
-          for (int q = 0; q < kRhsChunk; q++) {
-            v[q] = v[q] / d;
-            sy[buf * kRhsChunk + q] = v[q];
-          }
-        }
-        __syncthreads();
-        if (r < j) {
-          const double rj = sR[r + (j - jb) * NB];
-#pragma unroll
-          for (int q = 0; q < kRhsChunk; q++) v[q] = fma(-rj, sy[buf * kRhsChunk + q], v[q]);
-        }
-        buf ^= 1;
-      }
+      if (r < j) v = fma(-sR[r + (j - jb) * NB], sy[buf], v);
+      buf ^= 1;
     }
-#pragma unroll
-    for (int q = 0; q < kRhsChunk; q++)
-      if (q < nq) Ck[r + (long)(c0 + q) * NB] = v[q];
   }
+  Ck[r] = v;
 }
 
 // One step of the forward substitution R^T Y = C over the first NT tile rows
-// of C (tile layout, MT tile rows): step i first updates, in blocks k >= i,
-// C_k -= R_(i-1)k^T Y_(i-1) (Y_(i-1) solved by the step before; none at
-// i = 0), then block k = i solves R_ii^T Y_i = C_i in place (R_ii^T lower
-// triangular).  RA: the factored A (R in its upper tiles).  Thread r owns row
-// r of the tile (NB threads); R_(i-1)k^T's row r is R_(i-1)k's column r,
-// contiguous in the tile.
-__global__ void k_trsmt_step(const double* __restrict__ RA, int MT, int NB, double* __restrict__ C, int i,
-                             int nrhs) {
-  extern __shared__ double sm[];   // NB x kRhsChunk right operand / kRBlock x NB rows of R + 2 x kRhsChunk
+// of C, right-hand side q = blockIdx.y: step i first updates blocks k >= i,
+// C_k -= R_(i-1)k^T Y_(i-1) (none at i = 0), then block k = i solves
+// R_ii^T Y_i = C_i in place (R_ii^T lower triangular).  Row r of
+// R_(i-1)k^T is column r of R_(i-1)k, contiguous in the tile.
+__global__ void k_trsmt_step(const double* __restrict__ RA, int MT, int NB, double* __restrict__ C, int i) {
+  extern __shared__ double sm[];   // NB values of Y_(i-1) / kRBlock x NB rows of R_kk + 2
   const int k = i + (int)blockIdx.x;
-  const int tj = blockIdx.y;
-  const int ncol = min(NB, nrhs - tj * NB);
+  const int q = blockIdx.y, tj = q / NB, cw = q % NB;
   const int r = threadIdx.x;
   const long tile = (long)NB * NB;
-  double* Ck = C + ((long)k + (long)tj * MT) * tile;
+  double* Ck = C + ((long)k + (long)tj * MT) * tile + (long)cw * NB;
   if (i > 0) {
-    const double* Rik = RA + ((long)(i - 1) + (long)k * MT) * tile;
-    const double* Yi = C + ((long)(i - 1) + (long)tj * MT) * tile;
-    for (int c0 = 0; c0 < ncol; c0 += kRhsChunk) {
-      const int nq = min(kRhsChunk, ncol - c0);
-      __syncthreads();
-      for (int e = threadIdx.x; e < NB * kRhsChunk; e += blockDim.x) {
-        const int kk = e % NB, q = e / NB;
-        sm[e] = q < nq ? Yi[kk + (long)(c0 + q) * NB] : 0.0;
-      }
-      __syncthreads();
-      double acc[kRhsChunk];
-#pragma unroll
-      for (int q = 0; q < kRhsChunk; q++) acc[q] = 0.0;
-      const double* Rc = Rik + (long)r * NB;   // column r of R_(i-1)k = row r of its transpose
-#pragma unroll 4
-      for (int kk = 0; kk < NB; kk++) {
-        const double a = __ldg(Rc + kk);
-#pragma unroll
-        for (int q = 0; q < kRhsChunk; q++) acc[q] = fma(a, sm[kk + q * NB], acc[q]);
-      }
-#pragma unroll
-      for (int q = 0; q < kRhsChunk; q++)
-        if (q < nq) Ck[r + (long)(c0 + q) * NB] -= acc[q];
+    const double* Rc = RA + ((long)(i - 1) + (long)k * MT) * tile + (long)r * NB;
+    sm[r] = C[((long)(i - 1) + (long)tj * MT) * tile + (long)cw * NB + r];
+    __syncthreads();
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    for (int kk = 0; kk < NB; kk += 4) {
+      a0 = fma(Rc[kk], sm[kk], a0);
+      a1 = fma(Rc[kk + 1], sm[kk + 1], a1);
+      a2 = fma(Rc[kk + 2], sm[kk + 2], a2);
+      a3 = fma(Rc[kk + 3], sm[kk + 3], a3);
     }
+    Ck[r] -= (a0 + a1) + (a2 + a3);
   }
   if (k != i) return;
-  // R_kk^T Y = C_k: rows from the top; thread r keeps its row's values in
-  // registers, the solved value of row j is broadcast through a double buffer
-  // (one barrier per row); R_kk's rows j (R_kk^T's column j, elements R(j, r))
-  // are staged kRBlock at a time.
+  // R_kk^T y = c_k from the top row; sR[(j - jb) + r kRBlock] = R(j, r).
   __syncthreads();
   const double* Rkk = RA + ((long)k + (long)k * MT) * tile;
-  double* sR = sm;                          // kRBlock x NB: sR[(j - jb) + r kRBlock] = R(j, r)
-  double* sy = sm + (long)NB * kRBlock;     // 2 x kRhsChunk
-  for (int c0 = 0; c0 < ncol; c0 += kRhsChunk) {
-    const int nq = min(kRhsChunk, ncol - c0);
-    double v[kRhsChunk];
-#pragma unroll
-    for (int q = 0; q < kRhsChunk; q++) v[q] = q < nq ? Ck[r + (long)(c0 + q) * NB] : 0.0;
-    int buf = 0;
-    for (int jb = 0; jb < NB; jb += kRBlock) {
-      const int je = min(NB, jb + kRBlock);
-      __syncthreads();
-      for (int e = threadIdx.x; e < (je - jb) * NB; e += blockDim.x) {
-        const int jj = e % (je - jb), cc = e / (je - jb);
-        sR[jj + cc * kRBlock] = Rkk[(jb + jj) + (long)cc * NB];
-      }
-      __syncthreads();
-      for (int j = jb; j < je; j++) {
-        if (r == j) {
-          const double d = sR[(j - jb) + j * kRBlock];
-#pragma unroll
-          for (int q = 0; q < kRhsChunk; q++) {
-            v[q] = v[q] / d;
-            sy[buf * kRhsChunk + q] = v[q];
-          }
-        }
-        __syncthreads();
-        if (r > j) {
-          const double rj = sR[(j - jb) + r * kRBlock];
-#pragma unroll
-          for (int q = 0; q < kRhsChunk; q++) v[q] = fma(-rj, sy[buf * kRhsChunk + q], v[q]);
-        }
-        buf ^= 1;
-      }
+  double* sR = sm;
+  double* sy = sm + (long)NB * kRBlock;
+  double v = Ck[r];
+  const double inv = 1.0 / Rkk[r + (long)r * NB];
+  int buf = 0;
+  for (int jb = 0; jb < NB; jb += kRBlock) {
+    const int je = min(NB, jb + kRBlock);
+    __syncthreads();
+    for (int e = threadIdx.x; e < (je - jb) * NB; e += blockDim.x) {
+      const int jj = e % (je - jb), cc = e / (je - jb);
+      sR[jj + cc * kRBlock] = Rkk[(jb + jj) + (long)cc * NB];
     }
-#pragma unroll
-    for (int q = 0; q < kRhsChunk; q++)
-      if (q < nq) Ck[r + (long)(c0 + q) * NB] = v[q];
+    __syncthreads();
+    for (int j = jb; j < je; j++) {
+      if (r == j) {
+        v *= inv;
+        sy[buf] = v;
+      }
+      __syncthreads();
+      if (r > j) v = fma(-sR[(j - jb) + r * kRBlock], sy[buf], v);
+      buf ^= 1;
+    }
   }
+  Ck[r] = v;
 }
 
 int blocks_for(long n) {
@@ -428,22 +371,18 @@ void col_norm2(const double* dR, long M, long ldr, int nrhs, double* dOut, cudaS
   k_col_norm2<<<nrhs, 256, 0, s>>>(dR, M, ldr, dOut);
 }
 
-size_t trsm_smem_bytes(int NB) {
-  const size_t a = (size_t)NB * kRhsChunk, b = (size_t)NB * kRBlock + 2 * kRhsChunk;
-  return (a > b ? a : b) * sizeof(double);
-}
+size_t trsm_smem_bytes(int NB) { return ((size_t)NB * kRBlock + 2) * sizeof(double); }
 
 int trsm_tiles(const double* dRA, long M, long N, int NB, double* dC, int nrhs, cudaStream_t s) {
   const int MT = (int)(M / NB), NT = (int)(N / NB);
-  const int CT = (nrhs + NB - 1) / NB;
   const size_t smem = trsm_smem_bytes(NB);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_trsm_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(k_trsm_step)");
   }
   for (int i = NT; i >= 1; i--) {
-    const dim3 grid((unsigned)(i < NT ? i : 1), (unsigned)CT);
-    k_trsm_step<<<grid, NB, smem, s>>>(dRA, MT, NB, dC, i, NT, nrhs);
+    const dim3 grid((unsigned)(i < NT ? i : 1), (unsigned)nrhs);
+    k_trsm_step<<<grid, NB, smem, s>>>(dRA, MT, NB, dC, i, NT);
   }
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? HQR_OK : record_cuda_error(e, "k_trsm_step launch");
@@ -451,15 +390,14 @@ int trsm_tiles(const double* dRA, long M, long N, int NB, double* dC, int nrhs, 
 
 int trsmt_tiles(const double* dRA, long M, long N, int NB, double* dC, int nrhs, cudaStream_t s) {
   const int MT = (int)(M / NB), NT = (int)(N / NB);
-  const int CT = (nrhs + NB - 1) / NB;
   const size_t smem = trsm_smem_bytes(NB);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_trsmt_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(k_trsmt_step)");
   }
   for (int i = 0; i < NT; i++) {
-    const dim3 grid((unsigned)(NT - i), (unsigned)CT);
-    k_trsmt_step<<<grid, NB, smem, s>>>(dRA, MT, NB, dC, i, nrhs);
+    const dim3 grid((unsigned)(NT - i), (unsigned)nrhs);
+    k_trsmt_step<<<grid, NB, smem, s>>>(dRA, MT, NB, dC, i);
   }
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? HQR_OK : record_cuda_error(e, "k_trsmt_step launch");

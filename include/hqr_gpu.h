@@ -138,9 +138,12 @@ int hqr_make_q_async(hqr_plan_t *plan, double *dQ, double *dRY, const double *dT
                      int use_plan_t, void *stream);
 /* Hybrid_dormqr semantics: dC <- Q^T dC, dC an MT x CT tile grid (CT tile
  * columns of NB, e.g. CT = 1 for up to NB right-hand sides padded to NB).
- * use_plan_t as for hqr_make_q.  Waits for completion. */
+ * use_plan_t as for hqr_make_q.  hqr_ormqr_t waits for completion;
+ * hqr_ormqr_t_async only enqueues (check with hqr_plan_status). */
 int hqr_ormqr_t(hqr_plan_t *plan, const double *dRY, const double *dTAU, double *dC, int CT,
                 int use_plan_t, void *stream);
+int hqr_ormqr_t_async(hqr_plan_t *plan, const double *dRY, const double *dTAU, double *dC, int CT,
+                      int use_plan_t, void *stream);
 /* No counterpart in the reference (its dormqr applies Q^T only).  dC <- Q dC
  * (LAPACK dormqr 'L','N'): the reflectors applied as H, in backward order,
  * to every tile column of dC (MT x CT tiles).  use_plan_t as for hqr_make_q;
@@ -162,8 +165,10 @@ int hqr_ormqr_n_async(hqr_plan_t *plan, const double *dRY, const double *dTAU, d
  * FP64 iterative refinement: r = b - A x with the original A in FP64, x +=
  * R^-1 (Q^T r)(1:N).  dX: column-major N x nrhs (ld ldx >= N, device).
  * resid (host, nrhs doubles, may be NULL) receives ||b - A x||_2 of the
- * returned x per right-hand side.  Allocates its workspace (the copy of A,
- * TAU, the packed right-hand sides); synchronous. */
+ * returned x per right-hand side.  Its workspace (the copy of A, TAU, the
+ * packed right-hand sides) is allocated on the plan by the first call, kept
+ * for later calls (grown if they need more) and freed with the plan.
+ * Synchronous: returns the scheduler's status. */
 int hqr_lstsq(hqr_plan_t *plan, const double *dA, const double *dB, int ldb, int nrhs, double *dX,
               int ldx, int refine_steps, double *resid, void *stream);
 /* No counterpart in the reference.  hqr_lstsq's arguments and result, refined
@@ -176,8 +181,9 @@ int hqr_lstsq(hqr_plan_t *plan, const double *dA, const double *dB, int ldb, int
  * (||A|| ||x||)) whatever the factorization's precision, as long as the
  * factorization's error times kappa(A) stays below about 0.1; hqr_lstsq's
  * refinement stalls at the factorization's error times kappa(A) ||r|| /
- * (||A|| ||x||) instead.  HQR_ERR_UNSUPPORTED with a domain tree.  Allocates;
- * synchronous. */
+ * (||A|| ||x||) instead.  HQR_ERR_UNSUPPORTED with a domain tree.  Workspace
+ * as for hqr_lstsq (plus two tile grids of the right-hand sides and the
+ * residual r); synchronous. */
 int hqr_lstsq_aug(hqr_plan_t *plan, const double *dA, const double *dB, int ldb, int nrhs, double *dX,
                   int ldx, int refine_steps, double *resid, void *stream);
 
