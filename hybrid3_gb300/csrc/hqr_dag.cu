@@ -135,11 +135,17 @@ static int run_dag(DagParams& p, DagWorkspace* ws, const Geometry& g, cudaStream
   return p.oz_groups == 4 ? launch_exec<true, 4>(p, g, stream) : launch_exec<true, 8>(p, g, stream);
 }
 
+// 64-column chunks per split update task, run one after the other: two (a
+// whole 128-column tile) halve the number of update tasks and with them the
+// scheduling round trips (a queue claim and the dependents' releases, about
+// 6 us per task), at the price of half the tasks per step.
+constexpr int kOzChunksPerTask = 2;
 static void set_oz(DagParams& p, const Geometry& g, const OzWorkspace* oz) {
   if (oz && oz->slices) {
     p.oz = 1;
     p.oz_groups = oz->groups;
-    p.NC = g.NB / oz::kN;
+    p.oz_cpt = kOzChunksPerTask;
+    p.NC = g.NB / oz::kN / p.oz_cpt;
     p.slices = oz->slices;
     p.sexp = oz->sexp;
   } else {

@@ -114,7 +114,8 @@ struct DagParams {
   long long timeout_ns;
   unsigned long long* stats;   // [type][0] = count, [type][1] = SM cycles
   // split precision
-  int oz;           // 1: OZPREP/OZAPPLY tasks (NC = NB / 64)
+  int oz;           // 1: OZPREP/OZAPPLY tasks (NC * oz_cpt = NB / 64)
+  int oz_cpt;       // 64-column chunks one OZAPPLY task updates, one after the other
   int oz_groups;    // t-groups of the split updates (8 or 4; host side: picks the kernel)
   int prep;         // 1: separate OZPREP ids after the panel ids (factorization)
   uint8_t* slices;  // sliced left operands, one block per panel tile
@@ -758,7 +759,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
           const size_t slot = panel_slot(q.MT, t.i, t.k);
           oz_slices = q.slices + slot * oz::panel_slice_bytes();
           oz_exps = q.sexp + slot * oz::kSlots * NB;
-          oz_bot = q.C + oc + (size_t)t.c * oz::kN * NB;
+          oz_bot = q.C + oc + (size_t)t.c * q.oz_cpt * oz::kN * NB;
         } else {
           task_larfb(q.A + ov, q.T + ov, q.C + oc, t.c * q.sh.CB, q.sh.CB, q.sh, smem, q.sp,
                      applies_h(q.mode));
@@ -773,7 +774,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
         const size_t o1 = tile_off(top, t.j, q.MT, NB), o2 = tile_off(t.k, t.j, q.MT, NB);
         const size_t slot = tt ? merge_slot(q, t.i, dom_of(q, t.i, t.k)) : panel_slot(q.MT, t.i, t.k);
         if (OZ) {
-          const size_t cofs = (size_t)t.c * oz::kN * NB;
+          const size_t cofs = (size_t)t.c * q.oz_cpt * oz::kN * NB;
           oz_slices = (tt ? q.slices2 : q.slices) + slot * oz::panel_slice_bytes();
           oz_exps = (tt ? q.sexp2 : q.sexp) + slot * oz::kSlots * NB;
           oz_top = q.C + o1 + cofs;
@@ -793,9 +794,12 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
       task_ozprep(prep_v, prep_tau, prep_g, prep_kind, prep_slices, prep_exps, reinterpret_cast<uint8_t*>(smem),
                   s_tmem, q.ctl + kErr, !applies_h(q.mode));
     if (OZ && oz_bot) {
-      oz::Ctx c;
-      oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, q.ctl + kErr);
-      task_ozapply<OZG>(c, oz_slices, oz_exps, oz_top, oz_bot);
+      for (int cc = 0; cc < q.oz_cpt; cc++) {
+        const size_t co = (size_t)cc * oz::kN * NB;
+        oz::Ctx c;
+        oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, q.ctl + kErr);
+        if (!task_ozapply<OZG>(c, oz_slices, oz_exps, oz_top ? oz_top + co : nullptr, oz_bot + co)) break;
+      }
     }
     fence_acq_rel_gpu();   // release: this task's writes before its dependents' counters
     __syncthreads();
