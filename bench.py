@@ -902,6 +902,9 @@ def main():
                     help="batches the --batched end-to-end run is cut into (copies overlap compute)")
     ap.add_argument("--batch-ctas", type=int, default=0,
                     help="executor CTAs per SM (1 or 2) for --batched with --batch-nb")
+    ap.add_argument("--autotune", action="store_true",
+                    help="choose precision, NB and IB for the QR + make_Q workload by measuring the "
+                         "candidates first (hybrid3_gb300.autotune.tune_single)")
     ap.add_argument("--tree", type=int, default=0,
                     help="domain tree of this many tiles for the TS reduction (0: the flat tree)")
     args = ap.parse_args()
@@ -945,6 +948,17 @@ def main():
         if rank == 0:
             run_batched(H, torch, L, args)
         return
+    tuned = None
+    if args.autotune:
+        # precision, NB and IB for this shape, measured on it (or a scaled
+        # sample) before anything is timed; FP64-level precisions only
+        from hybrid3_gb300 import autotune as AT
+        rows_ = args.rows if args.rows is not None else args.n
+        table = AT.tune_single(H, torch, rows_, args.n, want_q=True, reps=1)
+        args.precision, args.nb, args.ib = AT.choose_single(table, rows_, args.n)
+        e = table["shapes"][0]
+        tuned = {"choice": [args.precision, args.nb, args.ib], "sample": e["sample"],
+                 "tflops": {f"{p}/{b}/{i}": round(r, 4) for (p, b, i), r in e["rates"].items()}}
     n, NB, IB = args.n, args.nb, args.ib
 
     # FP64 rates of this GPU: FMA on the CUDA cores and the FP64 tensor cores
@@ -1031,6 +1045,7 @@ def main():
                                 f"graded A = U diag(sigma) V^T, U, V Haar, kappa={args.kappa:g}"),
                    "n": n, "rows": M, "NB": NB, "IB": IB, "tree_domain_tiles": args.tree,
                    "precision": PRECISION_TEXT[args.precision],
+                   "autotuned": tuned,
                    "l2": f"inputs ({8 * M * n / 2**30:.0f} GiB per matrix) exceed the 129 MB L2; no flush",
                    "parallelism": f"replicas x{world}"},
         "phases_ms": {"factor": round(1e3 * fact_mean, 3),

@@ -223,3 +223,130 @@ def describe(table):
                                  "padded_tflops": {f"{k[0]}/{k[1]}/{ctas}": round(v, 4)
                                                    for ctas, r in e["rates"].items() for k, v in r.items()}}
                         for c, e in table["classes"].items()}}
+
+
+# ---------------------------------------------------------------------------
+# Single matrices (hqr_plan_*): precision, NB and IB per shape
+# ---------------------------------------------------------------------------
+# The split precisions run one tile order (128, the engine's K); their inner
+# block is 16 whatever IB says (FP64 panels narrowed for the tensor-core
+# updates), so IB only matters for plain FP64.
+SINGLE_CANDIDATES = (
+    ("split", 128, 32),
+    ("fp64", 128, 32), ("fp64", 192, 32), ("fp64", 256, 32), ("fp64", 256, 64),
+    ("fp64", 384, 32), ("fp64", 512, 64),
+)
+# Precisions that give an FP64-level backward error; "fast" (10 of the 36
+# slice products) is considered only when the caller allows it (least squares
+# refined on the augmented system).
+FP64_LEVEL = ("split", "fp64")
+
+
+def single_flops(m: int, n: int, want_q: bool) -> float:
+    """Algorithmic flops of one factorization, plus Q generation (the same
+    count again: 4/3 n^3 each for a square matrix) when want_q."""
+    f = qr_flops(m, n)
+    return f + (2.0 * m * n * n - 2.0 * n ** 3 / 3.0) if want_q else f
+
+
+def sample_shape(m: int, n: int, budget: float, want_q: bool, quantum: int = 1536):
+    """The shape the candidates are timed on: (m, n) itself when its flops fit
+    the budget, else the same aspect ratio scaled down to fit, in multiples of
+    `quantum` (a multiple of every candidate tile order)."""
+    f = single_flops(m, n, want_q)
+    if f <= budget:
+        return m, n
+    s = (budget / f) ** (1.0 / 3.0)
+    ms = max(quantum, int(m * s) // quantum * quantum)
+    ns = max(quantum, int(n * s) // quantum * quantum)
+    return min(ms, padded(m, quantum)), min(ns, padded(n, quantum))
+
+
+def predicted_single(rates, m: int, n: int, want_q: bool):
+    """{candidate: predicted seconds} for an m x n matrix: its flops zero-padded
+    to the candidate's tile order over the candidate's measured rate."""
+    return {k: single_flops(padded(m, k[1]), padded(n, k[1]), want_q) / (r * 1e12)
+            for k, r in rates.items() if r > 0}
+
+
+def choose_single(table, m: int, n: int, want_q: bool = True, allow=FP64_LEVEL):
+    """(precision, NB, IB) for an m x n matrix: the least predicted time over
+    the allowed candidates, with the rates measured on the table's shape
+    nearest to (m, n) (log distance) for the same want_q."""
+    entries = [e for e in table["shapes"] if bool(e["want_q"]) == bool(want_q)]
+    if not entries:
+        raise KeyError("no measured shape with want_q=%s" % want_q)
+    e = min(entries, key=lambda e: (np.log(e["m"] / m)) ** 2 + (np.log(e["n"] / n)) ** 2)
+    rates = {k: r for k, r in e["rates"].items() if k[0] in allow}
+    if not rates:
+        raise KeyError("no allowed candidate measured")
+    t = predicted_single(rates, m, n, want_q)
+    return min(t, key=t.get)
+
+
+def tune_single(H, torch, m: int, n: int, want_q: bool = True, candidates=SINGLE_CANDIDATES,
+                budget: float = 3e12, reps: int = 2, seed: int = 11):
+    """Measured rates (TFLOP/s of padded flops) of every candidate (precision,
+    NB, IB) on an m x n matrix, or on a scaled sample of it (sample_shape):
+    one warm-up and `reps` timed runs of hqr_geqrf (+ hqr_make_q) per
+    candidate on a uniform[-1, 1) matrix, CUDA events on the current stream.
+    Returns {"shapes": [{"m", "n", "sample", "want_q", "rates": {cand: rate}}]}."""
+    L = H.lib()
+    f64 = torch.float64
+    sm, sn = sample_shape(m, n, budget, want_q)
+    prec_code = {"fp64": H.HQR_PREC_FP64, "split": H.HQR_PREC_OZAKI, "fast": H.HQR_PREC_OZAKI_FAST}
+    rates = {}
+    for cand in candidates:
+        prec, nb, ib = cand
+        mp, np_ = padded(sm, nb), padded(sn, nb)
+        try:
+            plan = H.Plan(mp, np_, nb, ib, prec_code[prec])
+        except RuntimeError:   # shape or tile order not supported by this precision
+            continue
+        try:
+            A0 = torch.empty(mp * np_, dtype=f64, device="cuda")
+            H.check(L.hqr_fill_uniform(mp, np_, nb, seed, A0.data_ptr(), None), "hqr_fill_uniform")
+            A = torch.empty_like(A0)
+            tau = torch.zeros((mp // nb) * (np_ // nb) * nb, dtype=f64, device="cuda")
+            Q = torch.empty(mp * np_, dtype=f64, device="cuda") if want_q else None
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            times = []
+            for rep in range(reps + 1):
+                A.copy_(A0)
+                ev[0].record()
+                H.check(L.hqr_geqrf(plan.h, A.data_ptr(), tau.data_ptr(), None), "hqr_geqrf")
+                if want_q:
+                    H.check(L.hqr_make_q(plan.h, Q.data_ptr(), A.data_ptr(), tau.data_ptr(), 1, None),
+                            "hqr_make_q")
+                ev[1].record()
+                torch.cuda.synchronize()
+                if rep > 0:
+                    times.append(ev[0].elapsed_time(ev[1]) / 1e3)
+            rates[cand] = single_flops(mp, np_, want_q) / min(times) / 1e12
+        finally:
+            plan.close()
+            del A0
+            torch.cuda.empty_cache()
+    return {"shapes": [{"m": int(m), "n": int(n), "sample": [int(sm), int(sn)], "want_q": bool(want_q),
+                        "rates": rates}]}
+
+
+def merge_single(*tables):
+    """One table holding every measured shape of the given tables."""
+    return {"shapes": [e for t in tables for e in t["shapes"]]}
+
+
+def save_single(table, path: str) -> None:
+    import json
+    enc = {"shapes": [dict(e, rates=[[k[0], k[1], k[2], r] for k, r in e["rates"].items()])
+                      for e in table["shapes"]]}
+    with open(path, "w") as f:
+        json.dump(enc, f, indent=1)
+
+
+def load_single(path: str):
+    import json
+    with open(path) as f:
+        enc = json.load(f)
+    return {"shapes": [dict(e, rates={(p, int(nb), int(ib)): float(r) for p, nb, ib, r in e["rates"]})
+                       for e in enc["shapes"]]}

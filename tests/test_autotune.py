@@ -99,3 +99,55 @@ def test_batch_layout():
     assert list(c_off) == [0, 128 * 64, 128 * 64 + 64 * 32, 128 * 64 + 64 * 32 + 2048 * 128]
     # every offset is a whole number of 8-byte elements, tiles start on 16-byte boundaries
     assert all(int(x) % 2 == 0 for x in a_off)
+
+
+# --- single matrices --------------------------------------------------------
+def test_single_flops_match_the_bench_definition():
+    # factorization + Q generation: 8/3 n^3 square; tall: twice 2 m n^2 - 2/3 n^3
+    assert AT.single_flops(300, 300, True) == pytest.approx(8.0 / 3.0 * 300 ** 3)
+    assert AT.single_flops(600, 200, True) == pytest.approx(2 * AT.qr_flops(600, 200))
+    assert AT.single_flops(600, 200, False) == pytest.approx(AT.qr_flops(600, 200))
+
+
+def test_sample_shape_keeps_the_aspect_and_the_budget():
+    assert AT.sample_shape(2048, 2048, 1e12, True) == (2048, 2048)
+    ms, ns = AT.sample_shape(16384, 16384, 3e12, True)
+    assert ms == ns and ms % 1536 == 0
+    assert AT.single_flops(ms, ns, True) <= 3e12
+    ms, ns = AT.sample_shape(65536, 16384, 3e12, True)
+    assert ms % 1536 == 0 and ns % 1536 == 0 and 3.0 <= ms / ns <= 5.0
+
+
+def single_table(shapes):
+    return {"shapes": [{"m": m, "n": n, "sample": [m, n], "want_q": q, "rates": r} for m, n, q, r in shapes]}
+
+
+def test_single_choice_trades_padding_against_rate_and_respects_precision():
+    rates = {("split", 128, 32): 10.0, ("fp64", 256, 32): 1.0, ("fp64", 192, 32): 0.9,
+             ("fast", 128, 32): 13.0}
+    t = single_table([(8192, 8192, True, rates)])
+    # the fastest FP64-level candidate; "fast" only when allowed
+    assert AT.choose_single(t, 8192, 8192) == ("split", 128, 32)
+    assert AT.choose_single(t, 8192, 8192, allow=("split", "fp64", "fast")) == ("fast", 128, 32)
+    # FP64 only: 192 x 192 padding to 256 costs 2.4x the flops, 192 wins at 0.9 vs 1.0
+    assert AT.choose_single(t, 192, 192, allow=("fp64",)) == ("fp64", 192, 32)
+    assert AT.choose_single(t, 256, 256, allow=("fp64",)) == ("fp64", 256, 32)
+    with pytest.raises(KeyError):
+        AT.choose_single(t, 8192, 8192, want_q=False)
+
+
+def test_single_choice_takes_the_nearest_measured_shape():
+    near = {("split", 128, 32): 2.0, ("fp64", 256, 32): 1.0}
+    far = {("split", 128, 32): 0.1, ("fp64", 256, 32): 1.0}
+    t = single_table([(2048, 2048, True, near), (32768, 32768, True, far)])
+    assert AT.choose_single(t, 3072, 3072) == ("split", 128, 32)
+    assert AT.choose_single(t, 24576, 24576) == ("fp64", 256, 32)
+
+
+def test_single_table_round_trip(tmp_path):
+    t = single_table([(4096, 1024, False, {("split", 128, 32): 3.5, ("fp64", 256, 64): 0.8})])
+    p = str(tmp_path / "single.json")
+    AT.save_single(t, p)
+    u = AT.load_single(p)
+    assert u["shapes"][0]["rates"] == t["shapes"][0]["rates"]
+    assert AT.merge_single(t, u)["shapes"][1]["m"] == 4096
