@@ -41,11 +41,13 @@ DP = ctypes.POINTER(ctypes.c_double)
 
 PRECISION_TEXT = {"split": "split (Ozaki BF16 slices on tcgen05, FP64 panels)",
                   "fast": "reduced split (the 10 slice products of weight <= 3 on tcgen05, FP64 panels)",
+                  "fp32": "FP32-class (FP32 panel arithmetic, the reduced split updates)",
                   "fp64": "fp64 (plain)"}
 
 
 def prec_code(H, precision: str) -> int:
-    return {"split": H.HQR_PREC_OZAKI, "fast": H.HQR_PREC_OZAKI_FAST}.get(precision, H.HQR_PREC_FP64)
+    return {"split": H.HQR_PREC_OZAKI, "fast": H.HQR_PREC_OZAKI_FAST,
+            "fp32": H.HQR_PREC_FP32}.get(precision, H.HQR_PREC_FP64)
 
 
 def max_over_ranks(x: float, dist, device: str = "cuda") -> float:
@@ -865,7 +867,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=None, help="order (default 16384; 8192 columns with --lstsq)")
-    ap.add_argument("--precision", default="split", choices=["split", "fast", "fp64"])
+    ap.add_argument("--precision", default="split", choices=["split", "fast", "fp32", "fp64"])
     ap.add_argument("--nb", type=int, default=None, help="tile order (default 128 split, 256 fp64)")
     ap.add_argument("--ib", type=int, default=32)
     ap.add_argument("--fp64-nb", type=int, default=256, help="tile order of the plain-FP64 comparison")
@@ -911,7 +913,7 @@ def main():
     if args.n is None:
         args.n = 8192 if args.lstsq else 16384
     if args.nb is None:
-        args.nb = 128 if args.precision in ("split", "fast") else 256
+        args.nb = 128 if args.precision in ("split", "fast", "fp32") else 256
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -969,7 +971,7 @@ def main():
     peak_fp64 = max(fp64_rates.values())
     init = init64 = None
     if args.kappa is not None:
-        compare_too = args.precision in ("split", "fast") and not args.no_compare
+        compare_too = args.precision in ("split", "fast", "fp32") and not args.no_compare
         t = graded_tiles(H, torch, L, n, sorted({NB, args.fp64_nb} if compare_too else {NB}),
                          args.kappa, 1000 + rank)
         init = t[NB]
@@ -988,7 +990,7 @@ def main():
         e2e = measure_e2e(H, torch, L, args.precision, n, NB, IB, e2e_steps, dist, world, args.e2e_clocks)
 
     compare = None
-    if args.precision in ("split", "fast") and not args.no_compare:
+    if args.precision in ("split", "fast", "fp32") and not args.no_compare:
         fp = measure(H, torch, L, args, "fp64", n, args.fp64_nb, IB, args.fp64_steps, 1, dist, world, False,
                      not args.no_check, init64, rows)
         fv = fp["flops"] / fp["elapsed"] / 1e12
@@ -1010,7 +1012,7 @@ def main():
     fact_mean = float(np.mean(main_run["fact_s"]))
     achieved = qr_flops(M, n) / fact_mean / 1e12
     peaks = measured_peaks()
-    if args.precision in ("split", "fast"):
+    if args.precision in ("split", "fast", "fp32"):
         bf16 = peaks.get("bf16_tflops_sustained") or 1700.0
         prods = split_products(NB) if args.precision == "split" else 10
         peak = bf16 / prods

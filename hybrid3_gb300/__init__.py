@@ -25,6 +25,7 @@ HQR_ERR_DEVICE = -6
 HQR_PREC_FP64 = 0
 HQR_PREC_OZAKI = 1
 HQR_PREC_OZAKI_FAST = 2
+HQR_PREC_FP32 = 3
 HQR_ERRORS_ABORT = 0
 HQR_ERRORS_RETURN = 1
 

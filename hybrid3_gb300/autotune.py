@@ -294,7 +294,8 @@ def tune_single(H, torch, m: int, n: int, want_q: bool = True, candidates=SINGLE
     L = H.lib()
     f64 = torch.float64
     sm, sn = sample_shape(m, n, budget, want_q)
-    prec_code = {"fp64": H.HQR_PREC_FP64, "split": H.HQR_PREC_OZAKI, "fast": H.HQR_PREC_OZAKI_FAST}
+    prec_code = {"fp64": H.HQR_PREC_FP64, "split": H.HQR_PREC_OZAKI, "fast": H.HQR_PREC_OZAKI_FAST,
+                 "fp32": H.HQR_PREC_FP32}
     rates = {}
     for cand in candidates:
         prec, nb, ib = cand

@@ -149,7 +149,9 @@ int check_status(const mat_stat_t* st, int my_rank, int Proc_num) {
 
 size_t tau_len(const hqr::Geometry& g) { return (size_t)g.MT * g.NT * g.NB; }
 
-bool split_precision(int precision) { return precision == HQR_PREC_OZAKI || precision == HQR_PREC_OZAKI_FAST; }
+bool split_precision(int precision) {
+  return precision == HQR_PREC_OZAKI || precision == HQR_PREC_OZAKI_FAST || precision == HQR_PREC_FP32;
+}
 
 #define TRY(x)                      \
   do {                              \
@@ -173,6 +175,7 @@ const hqr::OzWorkspace* apply_operands(hqr_plan* plan, bool h, bool plan_refl, b
   const bool split = plan->oz.slices != nullptr;
   if (split && h && !plan->ozh.slices) {
     plan->ozh.groups = plan->oz.groups;
+    plan->ozh.fp32_panels = plan->oz.fp32_panels;
     if (cudaMalloc(&plan->ozh.slices, hqr::oz_slice_bytes(plan->g)) != cudaSuccess ||
         cudaMalloc(&plan->ozh.sexp, hqr::oz_exp_bytes(plan->g)) != cudaSuccess) {
       cudaFree(plan->ozh.slices);
@@ -290,6 +293,7 @@ int hqr_get_default_precision(void) {
     const char* e = getenv("HQR_PRECISION");
     g_default_precision = (e && (!strcmp(e, "ozaki") || !strcmp(e, "split")))  ? HQR_PREC_OZAKI
                           : (e && !strcmp(e, "fast"))                             ? HQR_PREC_OZAKI_FAST
+                          : (e && !strcmp(e, "fp32"))                             ? HQR_PREC_FP32
                                                                                   : HQR_PREC_FP64;
   }
   return g_default_precision;
@@ -319,7 +323,8 @@ int hqr_plan_create(hqr_plan_t** plan, long M, long N, int NB, int IB, int preci
   }
   cudaMemset(p->dT, 0, (size_t)M * N * sizeof(double));
   if (split_precision(precision)) {
-    p->oz.groups = precision == HQR_PREC_OZAKI_FAST ? 4 : 8;
+    p->oz.groups = precision == HQR_PREC_OZAKI ? 8 : 4;
+    p->oz.fp32_panels = precision == HQR_PREC_FP32 ? 1 : 0;
     if (cudaMalloc(&p->oz.slices, hqr::oz_slice_bytes(g)) != cudaSuccess ||
         cudaMalloc(&p->oz.sexp, hqr::oz_exp_bytes(g)) != cudaSuccess) {
       hqr_plan_destroy(p);

@@ -94,18 +94,18 @@ static size_t dag_smem_bytes(const Geometry& g, bool oz) {
   return b;
 }
 
-template <bool OZ, int G = 8>
+template <bool OZ, int G = 8, bool P32 = false>
 static int launch_exec(const DagParams& p, const Geometry& g, cudaStream_t stream) {
   static size_t attr_bytes = 0;   // dynamic shared memory opted in so far
   const size_t smem = dag_smem_bytes(g, OZ);
   if (smem > attr_bytes) {
-    cudaError_t e = cudaFuncSetAttribute(dag_exec_kernel<OZ, false, G>,
+    cudaError_t e = cudaFuncSetAttribute(dag_exec_kernel<OZ, false, G, P32>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(dag_exec_kernel)");
     attr_bytes = smem;
   }
   const int grid = std::min(dag_sm_count(), std::max(1, p.n_tasks));
-  dag_exec_kernel<OZ, false, G><<<grid, kThreads, smem, stream>>>(p);
+  dag_exec_kernel<OZ, false, G, P32><<<grid, kThreads, smem, stream>>>(p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return record_cuda_error(e, "dag_exec_kernel launch");
   return HQR_OK;
@@ -132,7 +132,8 @@ static int run_dag(DagParams& p, DagWorkspace* ws, const Geometry& g, cudaStream
   dag_init_kernel<<<blocks, 256, 0, stream>>>(p);
   dag_seed_kernel<<<blocks, 256, 0, stream>>>(p);
   if (!p.oz) return launch_exec<false>(p, g, stream);
-  return p.oz_groups == 4 ? launch_exec<true, 4>(p, g, stream) : launch_exec<true, 8>(p, g, stream);
+  if (p.oz_groups == 8) return launch_exec<true, 8>(p, g, stream);
+  return p.oz_p32 ? launch_exec<true, 4, true>(p, g, stream) : launch_exec<true, 4>(p, g, stream);
 }
 
 // 64-column chunks per split update task, run one after the other: two (a
@@ -144,6 +145,7 @@ static void set_oz(DagParams& p, const Geometry& g, const OzWorkspace* oz) {
   if (oz && oz->slices) {
     p.oz = 1;
     p.oz_groups = oz->groups;
+    p.oz_p32 = oz->fp32_panels;
     p.oz_cpt = kOzChunksPerTask;
     p.NC = g.NB / oz::kN / p.oz_cpt;
     p.slices = oz->slices;

@@ -29,6 +29,7 @@
 // steps deep instead of MT NB/w.  Every wait is bounded in time: when a wait runs out the kernel sets
 // an error bit and every CTA returns, so a broken DAG never hangs the GPU.
 #pragma once
+#include <type_traits>
 #include "hqr_oztasks.cuh"
 #include "hqr_tile_fp64.cuh"
 
@@ -117,6 +118,7 @@ struct DagParams {
   int oz;           // 1: OZPREP/OZAPPLY tasks (NC * oz_cpt = NB / 64)
   int oz_cpt;       // 64-column chunks one OZAPPLY task updates, one after the other
   int oz_groups;    // t-groups of the split updates (8 or 4; host side: picks the kernel)
+  int oz_p32;       // 1: FP32 panel arithmetic (host side: picks the kernel)
   int prep;         // 1: separate OZPREP ids after the panel ids (factorization)
   uint8_t* slices;  // sliced left operands, one block per panel tile
   int* sexp;        // their row exponents (oz::kSlots * NB ints per panel tile)
@@ -646,8 +648,10 @@ __device__ void task_tbuild(const double* V, const double* tau_g, double* T, boo
 // registers per thread): while one runs a latency-bound panel column loop,
 // the other's update keeps the FP64 pipe busy.
 // OZG: t-groups of the split updates (8: FP64-level; 4: the reduced form).
-template <bool OZ, bool BATCH = false, int OZG = 8>
+// P32: the panel blocks compute in FP32 (HQR_PREC_FP32).
+template <bool OZ, bool BATCH = false, int OZG = 8, bool P32 = false>
 __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagParams p) {
+  using PanelT = typename std::conditional<P32, float, double>::type;
   extern __shared__ __align__(1024) double smem[];
   __shared__ int s_id;
   __shared__ uint32_t s_tmem;
@@ -706,7 +710,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
     switch (t.type) {
       case kGEQRT: {   // the diagonal tile or a domain's top tile
         const size_t o = tile_off(t.k, t.i, q.MT, NB);
-        task_geqrt_blk(q.A + o, q.T + o, q.TAU + tau_off(t.k, t.i, q.MT, NB), q.sh, smem, q.sp, t.c);
+        task_geqrt_blk<PanelT>(q.A + o, q.T + o, q.TAU + tau_off(t.k, t.i, q.MT, NB), q.sh, smem, q.sp, t.c);
         break;
       }
       case kTSQRT: {   // R of the domain's top tile over tile (k, i)
@@ -788,7 +792,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
       default:
         if (threadIdx.x == 0) atomicOr((int*)(q.ctl + kErr), kErrBadTask);
     }
-    if (ts_a1) task_tsqrt_blk(ts_a1, ts_a2, ts_t, ts_tau, q.sh, smem, q.sp, t.c, ts_upper);
+    if (ts_a1) task_tsqrt_blk<PanelT>(ts_a1, ts_a2, ts_t, ts_tau, q.sh, smem, q.sp, t.c, ts_upper);
     // Q generation and Q C apply H (M = T), the other modes H^T (M = T^T)
     if (OZ && prep_v)
       task_ozprep(prep_v, prep_tau, prep_g, prep_kind, prep_slices, prep_exps, reinterpret_cast<uint8_t*>(smem),

@@ -80,6 +80,7 @@ struct OzWorkspace {
   uint8_t* slices = nullptr;   // sliced V^T, T^T, V, T of every panel tile
   int* sexp = nullptr;         // their row exponents
   int groups = 8;              // t-groups of the updates: 8 (FP64-level) or 4 (reduced)
+  int fp32_panels = 0;         // 1: the factorization's panel blocks compute in FP32
 };
 // Bytes of the split-precision workspace for a geometry (NB = 128).
 size_t oz_slice_bytes(const Geometry& g);

@@ -73,14 +73,31 @@ struct SmemPlan {
 // alpha: shared scalar; x: shared vector of n elements (unit stride).
 // On return *alpha = beta, x is scaled to v(1:n), *tau_out = tau.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double block_max(double v, double* red) {
+// Range constants of the panel arithmetic R (double; float for the FP32-class
+// panels of HQR_PREC_FP32): the smallest normal number and the unit roundoff
+// of dlarfg's safe minimum, the magnitudes whose squares stay in range (plain
+// path), and the range of a sum of squares whose square root needs no
+// scaling.  The panel kernels hold their tile in shared memory as R and
+// convert once on the way in and out (the stored values are R's).
+template <typename R> struct PanelReal;
+template <> struct PanelReal<double> {
+  static constexpr double kMin = DBL_MIN, kEps = DBL_EPSILON, kBig = 1e140, kTiny = 1e-140;
+  static constexpr double kSsLo = 1e-290, kSsHi = 1e290;
+};
+template <> struct PanelReal<float> {
+  static constexpr float kMin = FLT_MIN, kEps = FLT_EPSILON, kBig = 1e17f, kTiny = 1e-17f;
+  static constexpr float kSsLo = 1e-34f, kSsHi = 1e34f;
+};
+
+template <typename R>
+__device__ __forceinline__ R block_max(R v, R* red) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   __syncthreads();
   if (l == 0) red[w] = v;
   __syncthreads();
-  double s = 0.0;
+  R s = R(0);
 #pragma unroll
   for (int i = 0; i < kWarps; i++) s = fmax(s, red[i]);
   return s;
@@ -90,23 +107,25 @@ __device__ __forceinline__ double block_max(double v, double* red) {
 // ss lies where its square root needs no scaling.  beta = -sign(a) ||[a; x]||,
 // tau = (beta - a) / beta, scal = 1 / (a - beta) (x is scaled by scal after
 // knt rescalings by 1/safmin, as LAPACK does for tiny columns).
-__device__ __forceinline__ void larfg_scalars(double a, double xnorm, double ss, bool plain,
-                                              double& tau, double& scal, int& knt, double& beta) {
-  tau = 0.0;
+template <typename R>
+__device__ __forceinline__ void larfg_scalars(R a, R xnorm, R ss, bool plain, R& tau, R& scal, int& knt,
+                                              R& beta) {
+  using K = PanelReal<R>;
+  tau = R(0);
   beta = a;
-  scal = 1.0;
+  scal = R(1);
   knt = 0;
-  const double aa = fabs(a);
-  if (xnorm != 0.0 && plain && aa < 1e140 && (aa > 1e-140 || a == 0.0)) {
+  const R aa = fabs(a);
+  if (xnorm != R(0) && plain && aa < K::kBig && (aa > K::kTiny || a == R(0))) {
     // dlapy2(alpha, ||x||) as sqrt(alpha^2 + ||x||^2): no overflow or
     // underflow in this range, one square root instead of two
     beta = -copysign(sqrt(fma(a, a, ss)), a);
     tau = (beta - a) / beta;
-    scal = 1.0 / (a - beta);
-  } else if (xnorm != 0.0) {
-    const double safmin = DBL_MIN / (DBL_EPSILON * 0.5);
-    const double rsafmn = 1.0 / safmin;
-    double xn = xnorm;
+    scal = R(1) / (a - beta);
+  } else if (xnorm != R(0)) {
+    const R safmin = K::kMin / (K::kEps * R(0.5));
+    const R rsafmn = R(1) / safmin;
+    R xn = xnorm;
     beta = -copysign(hypot(a, xn), a);
     while (fabs(beta) < safmin && knt < 20) {
       knt++;
@@ -115,7 +134,7 @@ __device__ __forceinline__ void larfg_scalars(double a, double xnorm, double ss,
       beta = -copysign(hypot(a, xn), a);
     }
     tau = (beta - a) / beta;
-    scal = 1.0 / (a - beta);
+    scal = R(1) / (a - beta);
     for (int j = 0; j < knt; j++) beta *= safmin;
   }
 }
@@ -176,41 +195,43 @@ __device__ void block_larfg(double* alpha, double* x, int n, double* tau_out, do
 
 // dlarfg on [alpha; x] by one warp (x: n contiguous shared doubles), with the
 // arithmetic of block_larfg; every lane computes the (identical) scalars.
-__device__ void warp_larfg(double* alpha, double* x, int n, double* tau_out) {
+template <typename R>
+__device__ void warp_larfg(R* alpha, R* x, int n, R* tau_out) {
+  using K = PanelReal<R>;
   const int lane = threadIdx.x & 31;
-  double ss = 0.0;
+  R ss = R(0);
   for (int r = lane; r < n; r += 32) {
-    const double v = x[r];
+    const R v = x[r];
     ss = fma(v, v, ss);
   }
   ss = warp_sum(ss);
-  double xnorm;
+  R xnorm;
   bool plain = false;
-  if (ss == 0.0) {
-    xnorm = 0.0;
-  } else if (ss >= 1e-290 && ss <= 1e290) {
+  if (ss == R(0)) {
+    xnorm = R(0);
+  } else if (ss >= K::kSsLo && ss <= K::kSsHi) {
     xnorm = sqrt(ss);
     plain = true;
   } else {
-    double amax = 0.0;
+    R amax = R(0);
     for (int r = lane; r < n; r += 32) amax = fmax(amax, fabs(x[r]));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-    double s2 = 0.0;
+    R s2 = R(0);
     for (int r = lane; r < n; r += 32) {
-      const double v = x[r] / amax;
+      const R v = x[r] / amax;
       s2 = fma(v, v, s2);
     }
     s2 = warp_sum(s2);
     xnorm = amax * sqrt(s2);
   }
-  double tau, scal, beta;
+  R tau, scal, beta;
   int knt;
   larfg_scalars(*alpha, xnorm, ss, plain, tau, scal, knt, beta);
-  if (tau != 0.0) {
-    const double rsafmn = 1.0 / (DBL_MIN / (DBL_EPSILON * 0.5));
+  if (tau != R(0)) {
+    const R rsafmn = R(1) / (K::kMin / (K::kEps * R(0.5)));
     for (int r = lane; r < n; r += 32) {
-      double v = x[r];
+      R v = x[r];
       for (int j = 0; j < knt; j++) v *= rsafmn;
       x[r] = v * scal;
     }
@@ -237,24 +258,25 @@ __device__ __forceinline__ bool panel_item_mine(int it, int warp) {
 // step c, the warp that applies reflector c to column c + 1 also forms
 // reflector c + 1 (warp_larfg), the other warps apply reflector c to the
 // remaining columns and compute G(:, c): one barrier per column.
-__device__ void panel_qr_ts_fused(double* R, int ldr, double* A, int lda, int m, int w, double* tau,
-                                  double* G) {
+template <typename RT = double>
+__device__ void panel_qr_ts_fused(RT* R, int ldr, RT* A, int lda, int m, int w, RT* tau,
+                                  RT* G) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (warp == 0) warp_larfg(R, A, m, tau);
   __syncthreads();
   for (int c = 0; c < w; c++) {
-    const double t = tau[c];
-    const double* ac = A + (size_t)c * lda;
+    const RT t = tau[c];
+    const RT* ac = A + (size_t)c * lda;
     const int nupd = w - 1 - c;   // items 0..nupd-1: columns c+1..w-1; then G(b, c), b < c
     for (int it = 0; it < nupd + c; it++) {
       if (!panel_item_mine(it, warp)) continue;
       if (it < nupd) {
         const int j = c + 1 + it;
-        double* aj = A + (size_t)j * lda;
-        if (t != 0.0) {
-          double* rcj = R + c + (size_t)j * ldr;
-          const double r0 = *rcj;
-          double s = 0.0;
+        RT* aj = A + (size_t)j * lda;
+        if (t != RT(0)) {
+          RT* rcj = R + c + (size_t)j * ldr;
+          const RT r0 = *rcj;
+          RT s = RT(0);
           for (int r = lane; r < m; r += 32) s = fma(ac[r], aj[r], s);
           s = (warp_sum(s) + r0) * t;
           if (lane == 0) *rcj = r0 - s;
@@ -266,8 +288,8 @@ __device__ void panel_qr_ts_fused(double* R, int ldr, double* A, int lda, int m,
         }
       } else {
         const int b = it - nupd;
-        const double* vb = A + (size_t)b * lda;
-        double s = 0.0;
+        const RT* vb = A + (size_t)b * lda;
+        RT s = RT(0);
         for (int r = lane; r < m; r += 32) s = fma(vb[r], ac[r], s);
         s = warp_sum(s);
         if (lane == 0) G[b + c * w] = s;
@@ -281,22 +303,23 @@ __device__ void panel_qr_ts_fused(double* R, int ldr, double* A, int lda, int m,
 // with the Gram matrix of the unit-lower reflectors, G(b, c) = v_b . v_c =
 // P(c, b) + sum_{r > c} P(r, b) P(r, c), b < c (ld w); the same one-barrier
 // column step as panel_qr_ts_fused.
-__device__ void panel_qr_ge_fused(double* P, int ldp, int m, int w, double* tau, double* G) {
+template <typename RT = double>
+__device__ void panel_qr_ge_fused(RT* P, int ldp, int m, int w, RT* tau, RT* G) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (warp == 0) warp_larfg(P, P + 1, m - 1, tau);
   __syncthreads();
   for (int c = 0; c < w; c++) {
-    const double t = tau[c];
-    const double* pc = P + (size_t)c * ldp;
+    const RT t = tau[c];
+    const RT* pc = P + (size_t)c * ldp;
     const int nupd = w - 1 - c;
     for (int it = 0; it < nupd + c; it++) {
       if (!panel_item_mine(it, warp)) continue;
       if (it < nupd) {
         const int j = c + 1 + it;
-        double* pj = P + (size_t)j * ldp;
-        if (t != 0.0) {
-          const double pcj = pj[c];
-          double s = 0.0;
+        RT* pj = P + (size_t)j * ldp;
+        if (t != RT(0)) {
+          const RT pcj = pj[c];
+          RT s = RT(0);
           for (int r = c + 1 + lane; r < m; r += 32) s = fma(pc[r], pj[r], s);
           s = (warp_sum(s) + pcj) * t;
           if (lane == 0) pj[c] = pcj - s;
@@ -308,8 +331,8 @@ __device__ void panel_qr_ge_fused(double* P, int ldp, int m, int w, double* tau,
         }
       } else {
         const int b = it - nupd;
-        const double* pb = P + (size_t)b * ldp;
-        double s = 0.0;
+        const RT* pb = P + (size_t)b * ldp;
+        RT s = RT(0);
         for (int r = c + 1 + lane; r < m; r += 32) s = fma(pb[r], pc[r], s);
         s = warp_sum(s);
         if (lane == 0) G[b + c * w] = s + pb[c];
@@ -323,17 +346,18 @@ __device__ void panel_qr_ge_fused(double* P, int ldp, int m, int w, double* tau,
 // and the Gram G(b, c), b < c: T(c, c) = tau_c, T(0:c, c) = -tau_c T(0:c,
 // 0:c) G(0:c, c).  One warp, lane a owns row a of T: a row depends only on
 // itself, so no synchronisation between the columns.
-__device__ void t_from_gram(const double* G, const double* tau, double* T, int w) {
+template <typename RT = double>
+__device__ void t_from_gram(const RT* G, const RT* tau, RT* T, int w) {
   const int a = threadIdx.x & 31;
   if (a >= w) return;
   for (int c = 0; c < w; c++) {
-    double v;
+    RT v;
     if (a < c) {
-      double s = 0.0;
+      RT s = RT(0);
       for (int b = a; b < c; b++) s = fma(T[a + b * w], G[b + c * w], s);
-      v = (tau[c] == 0.0) ? 0.0 : -tau[c] * s;
+      v = (tau[c] == RT(0)) ? RT(0) : -tau[c] * s;
     } else {
-      v = (a == c) ? tau[c] : 0.0;
+      v = (a == c) ? tau[c] : RT(0);
     }
     T[a + c * w] = v;
   }
@@ -388,24 +412,25 @@ __device__ void build_t_block(const double* V, int ldv, int m, int w, bool unit,
 // upper triangle of a tile whose lower part holds other data): element
 // (mb_off + r, c) is used when mb_off + r <= v_col0 + c, else taken as zero.
 // ---------------------------------------------------------------------------
+template <typename RT = double>
 __device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off,
                               const double* __restrict__ gT, int ldt, int w, int mb, bool unit_top,
-                              double* Ct, int ldct, double* Cb, int ldcb, int ncol, double* smem,
+                              RT* Ct, int ldct, RT* Cb, int ldcb, int ncol, RT* smem,
                               const SmemPlan& sp, int RC, bool notrans = false, int v_col0 = -1) {
-  double* sVb = smem + sp.off_vb;
-  double* sVt = smem + sp.off_vt;
-  double* sT = smem + sp.off_t;
-  double* sW = smem + sp.off_w;
-  double* sW2 = smem + sp.off_w2;
-  double* sPart = smem + sp.off_part;
+  RT* sVb = smem + sp.off_vb;
+  RT* sVt = smem + sp.off_vt;
+  RT* sT = smem + sp.off_t;
+  RT* sW = smem + sp.off_w;
+  RT* sW2 = smem + sp.off_w2;
+  RT* sPart = smem + sp.off_part;
   const int tid = threadIdx.x;
   const int ldvs = RC + 1;
 
   // T block and the unit-lower top of V
   for (int e = tid; e < w * w; e += kThreads) {
     const int r = e % w, c = e / w;
-    sT[e] = (r <= c) ? ldg_cg(gT + r + (size_t)c * ldt) : 0.0;
-    if (unit_top) sVt[e] = (r > c) ? ldg_cg(gV + r + (size_t)c * ldv) : (r == c ? 1.0 : 0.0);
+    sT[e] = (r <= c) ? RT(ldg_cg(gT + r + (size_t)c * ldt)) : RT(0);
+    if (unit_top) sVt[e] = (r > c) ? RT(ldg_cg(gV + r + (size_t)c * ldv)) : (r == c ? RT(1) : RT(0));
   }
 
   // ---- W = Vt^T Ct + Vb^T Cb -------------------------------------------
@@ -418,22 +443,22 @@ __device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off
   const int g = (item / w) % (G8 > 0 ? G8 : 1);
   const int s = item / outs;
   const bool active = (outs > 0) && (item < outs * S) && (s < S);
-  double acc[8];
+  RT acc[8];
 #pragma unroll
-  for (int q = 0; q < 8; q++) acc[q] = 0.0;
+  for (int q = 0; q < 8; q++) acc[q] = RT(0);
   for (int r0 = 0; r0 < mb; r0 += RC) {
     const int rc = min(RC, mb - r0);
     __syncthreads();
     for (int e = tid; e < rc * w; e += kThreads) {
       const int r = e % rc, c = e / rc;
       sVb[r + c * ldvs] = (v_col0 < 0 || mb_off + r0 + r <= v_col0 + c)
-                              ? ldg_cg(gV + mb_off + r0 + r + (size_t)c * ldv) : 0.0;
+                              ? RT(ldg_cg(gV + mb_off + r0 + r + (size_t)c * ldv)) : RT(0);
     }
     __syncthreads();
     if (active) {
-      const double* cb = Cb + r0 + (size_t)(8 * g) * ldcb;
+      const RT* cb = Cb + r0 + (size_t)(8 * g) * ldcb;
       for (int r = s; r < rc; r += S) {
-        const double v = sVb[r + a * ldvs];
+        const RT v = sVb[r + a * ldvs];
 #pragma unroll
         for (int q = 0; q < 8; q++) acc[q] = fma(v, cb[r + (size_t)q * ldcb], acc[q]);
       }
@@ -447,9 +472,9 @@ __device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off
   __syncthreads();
   for (int e = tid; e < w * ncol; e += kThreads) {
     const int aa = e % w, j = e / w;
-    double v = 0.0;
+    RT v = RT(0);
     for (int ss = 0; ss < S; ss++) v += sPart[(ss * w + aa) * 8 * G8 + j];
-    double top = Ct[aa + (size_t)j * ldct];
+    RT top = Ct[aa + (size_t)j * ldct];
     if (unit_top)
       for (int r = aa + 1; r < w; r++) top = fma(sVt[r + aa * w], Ct[r + (size_t)j * ldct], top);
     sW[aa + j * w] = v + top;
@@ -459,7 +484,7 @@ __device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off
   // ---- W2 = T^T W (notrans: T W) --------------------------------------------
   for (int e = tid; e < w * ncol; e += kThreads) {
     const int aa = e % w, j = e / w;
-    double v = 0.0;
+    RT v = RT(0);
     if (notrans)
       for (int b = aa; b < w; b++) v = fma(sT[aa + b * w], sW[b + j * w], v);
     else
@@ -471,7 +496,7 @@ __device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off
   // ---- Ct -= Vt W2 ----------------------------------------------------------
   for (int e = tid; e < w * ncol; e += kThreads) {
     const int aa = e % w, j = e / w;
-    double v = sW2[aa + j * w];
+    RT v = sW2[aa + j * w];
     if (unit_top)
       for (int b = 0; b < aa; b++) v = fma(sVt[aa + b * w], sW2[b + j * w], v);
     Ct[aa + (size_t)j * ldct] -= v;
@@ -484,20 +509,20 @@ __device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off
     for (int e = tid; e < rc * w; e += kThreads) {
       const int r = e % rc, c = e / rc;
       sVb[r + c * ldvs] = (v_col0 < 0 || mb_off + r0 + r <= v_col0 + c)
-                              ? ldg_cg(gV + mb_off + r0 + r + (size_t)c * ldv) : 0.0;
+                              ? RT(ldg_cg(gV + mb_off + r0 + r + (size_t)c * ldv)) : RT(0);
     }
     __syncthreads();
     for (int e = tid; e < rc * G8; e += kThreads) {
       const int r = e % rc, gg = e / rc;
-      double acc2[8];
+      RT acc2[8];
 #pragma unroll
-      for (int q = 0; q < 8; q++) acc2[q] = 0.0;
+      for (int q = 0; q < 8; q++) acc2[q] = RT(0);
       for (int b = 0; b < w; b++) {
-        const double v = sVb[r + b * ldvs];
+        const RT v = sVb[r + b * ldvs];
 #pragma unroll
         for (int q = 0; q < 8; q++) acc2[q] = fma(v, sW2[b + (8 * gg + q) * w], acc2[q]);
       }
-      double* cb = Cb + r0 + r + (size_t)(8 * gg) * ldcb;
+      RT* cb = Cb + r0 + r + (size_t)(8 * gg) * ldcb;
 #pragma unroll
       for (int q = 0; q < 8; q++) cb[(size_t)q * ldcb] -= acc2[q];
     }
@@ -510,30 +535,34 @@ __device__ void apply_block_t(const double* __restrict__ gV, int ldv, int mb_off
 // the factorization writes their diagonal w x w blocks.
 // ---------------------------------------------------------------------------
 
-__device__ void load_block(double* s, int lds, const double* g, int ldg, int m, int n) {
+template <typename RT = double>
+__device__ void load_block(RT* s, int lds, const double* g, int ldg, int m, int n) {
   for (int e = threadIdx.x; e < m * n; e += kThreads) {
     const int r = e % m, c = e / m;
-    s[r + (size_t)c * lds] = ldg_cg(g + r + (size_t)c * ldg);
+    s[r + (size_t)c * lds] = RT(ldg_cg(g + r + (size_t)c * ldg));
   }
 }
-__device__ void store_block(double* g, int ldg, const double* s, int lds, int m, int n) {
+template <typename RT = double>
+__device__ void store_block(double* g, int ldg, const RT* s, int lds, int m, int n) {
   for (int e = threadIdx.x; e < m * n; e += kThreads) {
     const int r = e % m, c = e / m;
-    stg_cg(g + r + (size_t)c * ldg, s[r + (size_t)c * lds]);
+    stg_cg(g + r + (size_t)c * ldg, double(s[r + (size_t)c * lds]));
   }
 }
 // The upper part (row r <= col0 + c) of an m x n block, zero below; and its
 // store (a TT merge's panel columns).
-__device__ void load_block_upper(double* s, int lds, const double* g, int ldg, int m, int n, int col0) {
+template <typename RT = double>
+__device__ void load_block_upper(RT* s, int lds, const double* g, int ldg, int m, int n, int col0) {
   for (int e = threadIdx.x; e < m * n; e += kThreads) {
     const int r = e % m, c = e / m;
-    s[r + (size_t)c * lds] = (r <= col0 + c) ? ldg_cg(g + r + (size_t)c * ldg) : 0.0;
+    s[r + (size_t)c * lds] = (r <= col0 + c) ? RT(ldg_cg(g + r + (size_t)c * ldg)) : RT(0);
   }
 }
-__device__ void store_block_upper(double* g, int ldg, const double* s, int lds, int m, int n, int col0) {
+template <typename RT = double>
+__device__ void store_block_upper(double* g, int ldg, const RT* s, int lds, int m, int n, int col0) {
   for (int e = threadIdx.x; e < m * n; e += kThreads) {
     const int r = e % m, c = e / m;
-    if (r <= col0 + c) stg_cg(g + r + (size_t)c * ldg, s[r + (size_t)c * lds]);
+    if (r <= col0 + c) stg_cg(g + r + (size_t)c * ldg, double(s[r + (size_t)c * lds]));
   }
 }
 
@@ -541,13 +570,15 @@ __device__ void store_block_upper(double* g, int ldg, const double* s, int lds, 
 // columns [b w, (b+1) w) from row b w down (blocks 0..b-1 done), its T block,
 // and its application to the columns right of it.  It writes rows >= b w of
 // the tile only: rows [b w, (b+1) w) of R are final afterwards.
+template <typename RT = double>
 __device__ void task_geqrt_blk(double* A, double* T, double* tau_g, const TileShape& sh, double* smem,
                                const SmemPlan& sp, int b) {
   const int NB = sh.NB, w = sh.w;
-  double* sP = smem + sp.off_c1;
-  double* sTau = smem + sp.off_tau;
-  double* sG = smem + sp.off_g;
-  double* sTb = smem + sp.off_t;
+  RT* sm = reinterpret_cast<RT*>(smem);
+  RT* sP = sm + sp.off_c1;
+  RT* sTau = sm + sp.off_tau;
+  RT* sG = sm + sp.off_g;
+  RT* sTb = sm + sp.off_t;
   {
     const int i0 = b * w;
     const int m = NB - i0;
@@ -559,16 +590,16 @@ __device__ void task_geqrt_blk(double* A, double* T, double* tau_g, const TileSh
     __syncthreads();
     store_block(A + i0 + (size_t)i0 * NB, NB, sP, NB, m, w);
     store_block(T + i0 + (size_t)i0 * NB, NB, sTb, w, w, w);
-    for (int e = threadIdx.x; e < w; e += kThreads) stg_cg(tau_g + i0 + e, sTau[e]);
+    for (int e = threadIdx.x; e < w; e += kThreads) stg_cg(tau_g + i0 + e, double(sTau[e]));
     __syncthreads();
     for (int c0 = i0 + w; c0 < NB; c0 += sh.CB) {
       const int ncol = min(sh.CB, NB - c0);
-      double* sC = smem + sp.off_c1;
+      RT* sC = sm + sp.off_c1;
       __syncthreads();
       load_block(sC, NB, A + i0 + (size_t)c0 * NB, NB, m, ncol);
       __syncthreads();
       apply_block_t(A + i0 + (size_t)i0 * NB, NB, w, T + i0 + (size_t)i0 * NB, NB, w, m - w, true,
-                    sC, NB, sC + w, NB, ncol, smem, sp, sh.RC);
+                    sC, NB, sC + w, NB, ncol, sm, sp, sh.RC);
       store_block(A + i0 + (size_t)c0 * NB, NB, sC, NB, m, ncol);
     }
   }
@@ -593,14 +624,16 @@ __device__ void task_geqrt(double* A, double* T, double* tau_g, const TileShape&
 // and is neither read nor written).  The reflectors keep A2's shape, so the
 // same arithmetic on A2 with zeros below the diagonal is exact, and only the
 // upper triangle is stored back.
+template <typename RT = double>
 __device__ void task_tsqrt_blk(double* A1, double* A2, double* T, double* tau_g, const TileShape& sh,
                                double* smem, const SmemPlan& sp, int b, bool a2_upper = false) {
   const int NB = sh.NB, w = sh.w;
-  double* sA = smem + sp.off_c1;     // NB x w panel of A2
-  double* sR = smem + sp.off_vt;     // w x w block of R
-  double* sTau = smem + sp.off_tau;
-  double* sG = smem + sp.off_g;
-  double* sTb = smem + sp.off_t;
+  RT* sm = reinterpret_cast<RT*>(smem);
+  RT* sA = sm + sp.off_c1;     // NB x w panel of A2
+  RT* sR = sm + sp.off_vt;     // w x w block of R
+  RT* sTau = sm + sp.off_tau;
+  RT* sG = sm + sp.off_g;
+  RT* sTb = sm + sp.off_t;
   {
     const int i0 = b * w;
     __syncthreads();
@@ -619,15 +652,15 @@ __device__ void task_tsqrt_blk(double* A1, double* A2, double* T, double* tau_g,
       store_block(A2 + (size_t)i0 * NB, NB, sA, NB, NB, w);
     for (int e = threadIdx.x; e < w * w; e += kThreads) {
       const int r = e % w, c = e / w;
-      if (r <= c) stg_cg(A1 + i0 + r + (size_t)(i0 + c) * NB, sR[r + c * w]);
+      if (r <= c) stg_cg(A1 + i0 + r + (size_t)(i0 + c) * NB, double(sR[r + c * w]));
     }
     store_block(T + i0 + (size_t)i0 * NB, NB, sTb, w, w, w);
-    for (int e = threadIdx.x; e < w; e += kThreads) stg_cg(tau_g + i0 + e, sTau[e]);
+    for (int e = threadIdx.x; e < w; e += kThreads) stg_cg(tau_g + i0 + e, double(sTau[e]));
     __syncthreads();
     for (int c0 = i0 + w; c0 < NB; c0 += sh.CB) {
       const int ncol = min(sh.CB, NB - c0);
-      double* sCt = smem + sp.off_c1;  // w x ncol rows of R (the panel area is free now)
-      double* sCb = smem + sp.off_c1 + w * sh.CB;  // NB x ncol of A2 after the R rows
+      RT* sCt = sm + sp.off_c1;  // w x ncol rows of R (the panel area is free now)
+      RT* sCb = sm + sp.off_c1 + w * sh.CB;  // NB x ncol of A2 after the R rows
       __syncthreads();
       // A TT merge's block reflectors reach rows < i0 + w of A2 only: the rows
       // below belong to the domain top's own later blocks, which its chain may
@@ -637,7 +670,7 @@ __device__ void task_tsqrt_blk(double* A1, double* A2, double* T, double* tau_g,
       load_block(sCb, NB, A2 + (size_t)c0 * NB, NB, mrows, ncol);
       __syncthreads();
       apply_block_t(A2 + (size_t)i0 * NB, NB, 0, T + i0 + (size_t)i0 * NB, NB, w, mrows, false, sCt, w,
-                    sCb, NB, ncol, smem, sp, sh.RC, false, a2_upper ? i0 : -1);
+                    sCb, NB, ncol, sm, sp, sh.RC, false, a2_upper ? i0 : -1);
       store_block(A1 + i0 + (size_t)c0 * NB, NB, sCt, w, w, ncol);
       store_block(A2 + (size_t)c0 * NB, NB, sCb, NB, mrows, ncol);
     }

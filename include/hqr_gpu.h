@@ -30,7 +30,7 @@ extern "C" {
 #define HQR_ERR_UNSUPPORTED (-5) /* shape outside what the kernels support */
 #define HQR_ERR_DEVICE (-6)      /* a device-side consistency check failed */
 
-/* Arithmetic of the trailing updates (panels are always FP64). */
+/* Arithmetic of the trailing updates (and, for HQR_PREC_FP32, of the panels). */
 #define HQR_PREC_FP64 0    /* FP64 on CUDA cores */
 #define HQR_PREC_OZAKI 1   /* split-precision slices on the tensor cores, FP64 recombination;
                               NB = 128 only (HQR_ERR_UNSUPPORTED otherwise) */
@@ -39,7 +39,13 @@ extern "C" {
                               column maxima, an FP32-class factorization (FP64 panels, NB = 128
                               only).  For least squares with FP64 iterative refinement
                               (hqr_lstsq, refine_steps >= 2) on well-conditioned problems: the
-                              refinement ends near kappa^2 * 5e-9 * ||r|| / (||A|| ||x||) */
+                              refinement ends near kappa^2 * 5e-9 * ||r|| / (||A|| ||x||);
+                              hqr_lstsq_aug refines to the FP64 solution instead */
+#define HQR_PREC_FP32 3       /* an FP32-class factorization: the panel blocks (GEQRT / TSQRT
+                              and their in-tile updates) compute in FP32 on values kept in
+                              FP64 arrays, the updates are those of HQR_PREC_OZAKI_FAST; the
+                              reference's FP32 factorization for least squares refined in
+                              FP64 (hqr_lstsq_aug).  NB = 128 only */
 
 /* Error behaviour of the drop-in (Hybrid_*, tile_*) entry points. */
 #define HQR_ERRORS_ABORT 0   /* print to stderr and exit(1) (the reference's MPI_Abort) */
