@@ -436,18 +436,37 @@ int hqr_make_q(hqr_plan_t* plan, double* dQ, double* dRY, const double* dTAU, in
   return hqr_plan_status(plan, stream);
 }
 
-int hqr_ormqr_t_async(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT,
-                      int use_plan_t, void* stream) {
+namespace {
+// Q^T C and Q C on C's first ccols columns (0: all CT tile columns); the
+// columns beyond are zero and stay so.
+int ormqr_t_cols(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT, int use_plan_t,
+                 cudaStream_t s, long long ccols) {
   if (!plan || !dRY || !dTAU || !dC || CT <= 0) return HQR_ERR_INVALID;
   if (plan->tree.S > 0) {
     if (!use_plan_t) return HQR_ERR_UNSUPPORTED;   // the merges' T factors live in the plan
-    return hqr::launch_apply_qt_tree(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, g_timeout_ns,
-                                     (cudaStream_t)stream, &plan->oz, &plan->tree);
+    return hqr::launch_apply_qt_tree(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, g_timeout_ns, s,
+                                     &plan->oz, &plan->tree);
   }
   bool rebuild;
   const hqr::OzWorkspace* oz = apply_operands(plan, false, use_plan_t != 0, &rebuild);
-  return hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, rebuild, g_timeout_ns,
-                              (cudaStream_t)stream, oz);
+  return hqr::launch_apply_qt(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, rebuild, g_timeout_ns, s, oz,
+                              ccols);
+}
+int ormqr_n_cols(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT, int use_plan_t,
+                 cudaStream_t s, long long ccols) {
+  if (!plan || !dRY || !dTAU || !dC || CT <= 0) return HQR_ERR_INVALID;
+  if (plan->tree.S > 0) return HQR_ERR_UNSUPPORTED;
+  bool rebuild;
+  const hqr::OzWorkspace* oz = apply_operands(plan, true, use_plan_t != 0, &rebuild);
+  if (!oz) return HQR_ERR_NOMEM;
+  return hqr::launch_apply_q(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, rebuild, g_timeout_ns, s, oz,
+                             ccols);
+}
+}  // namespace
+
+int hqr_ormqr_t_async(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT,
+                      int use_plan_t, void* stream) {
+  return ormqr_t_cols(plan, dRY, dTAU, dC, CT, use_plan_t, (cudaStream_t)stream, 0);
 }
 
 int hqr_ormqr_t(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT,
@@ -458,13 +477,7 @@ int hqr_ormqr_t(hqr_plan_t* plan, const double* dRY, const double* dTAU, double*
 
 int hqr_ormqr_n_async(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT,
                       int use_plan_t, void* stream) {
-  if (!plan || !dRY || !dTAU || !dC || CT <= 0) return HQR_ERR_INVALID;
-  if (plan->tree.S > 0) return HQR_ERR_UNSUPPORTED;
-  bool rebuild;
-  const hqr::OzWorkspace* oz = apply_operands(plan, true, use_plan_t != 0, &rebuild);
-  if (!oz) return HQR_ERR_NOMEM;
-  return hqr::launch_apply_q(plan->g, &plan->ws, dRY, plan->dT, dTAU, dC, CT, rebuild, g_timeout_ns,
-                             (cudaStream_t)stream, oz);
+  return ormqr_n_cols(plan, dRY, dTAU, dC, CT, use_plan_t, (cudaStream_t)stream, 0);
 }
 
 int hqr_ormqr_n(hqr_plan_t* plan, const double* dRY, const double* dTAU, double* dC, int CT, int use_plan_t,
@@ -508,7 +521,7 @@ int ls_start(hqr_plan* plan, const double* dA, const double* dB, int ldb, int nr
   TRY(hqr_geqrf_async(plan, Af, tau, s));
   hqr::pack_rhs(dB, ldb, nrhs, C, g.M, g.NB, CT, s);
   TRY(cuda_rc(cudaGetLastError()));
-  TRY(hqr_ormqr_t_async(plan, Af, tau, C, CT, 1, s));
+  TRY(ormqr_t_cols(plan, Af, tau, C, CT, 1, s, nrhs));
   TRY(hqr::trsm_tiles(Af, g.M, g.N, g.NB, C, nrhs, s));
   hqr::update_x(C, g.M, g.NB, g.N, nrhs, dX, ldx, false, s);
   return cuda_rc(cudaGetLastError());
@@ -549,7 +562,7 @@ int hqr_lstsq(hqr_plan_t* plan, const double* dA, const double* dB, int ldb, int
     TRY(hqr::residual(dA, g.M, g.N, g.NB, dX, ldx, dB, ldb, Res, g.M, nrhs, s));
     hqr::pack_rhs(Res, g.M, nrhs, C, g.M, g.NB, CT, s);
     TRY(cuda_rc(cudaGetLastError()));
-    TRY(hqr_ormqr_t_async(plan, Af, tau, C, CT, 1, s));
+    TRY(ormqr_t_cols(plan, Af, tau, C, CT, 1, s, nrhs));
     TRY(hqr::trsm_tiles(Af, g.M, g.N, g.NB, C, nrhs, s));
     hqr::update_x(C, g.M, g.NB, g.N, nrhs, dX, ldx, true, s);
     TRY(cuda_rc(cudaGetLastError()));
@@ -592,7 +605,7 @@ int hqr_lstsq_aug(hqr_plan_t* plan, const double* dA, const double* dB, int ldb,
     // d = Q^T f; h = R^-T g
     hqr::pack_rhs(Res, g.M, nrhs, C, g.M, g.NB, CT, s);
     TRY(cuda_rc(cudaGetLastError()));
-    TRY(hqr_ormqr_t_async(plan, Af, tau, C, CT, 1, s));
+    TRY(ormqr_t_cols(plan, Af, tau, C, CT, 1, s, nrhs));
     hqr::pack_rhs_rows(atr, g.N, nrhs, g.N, G, g.M, g.NB, CT, s);
     TRY(hqr::trsmt_tiles(Af, g.M, g.N, g.NB, G, nrhs, s));
     // G = [h; d2], C = [d1 - h; d2]
@@ -602,7 +615,7 @@ int hqr_lstsq_aug(hqr_plan_t* plan, const double* dA, const double* dB, int ldb,
     TRY(hqr::trsm_tiles(Af, g.M, g.N, g.NB, C, nrhs, s));
     hqr::update_x(C, g.M, g.NB, g.N, nrhs, dX, ldx, true, s);
     TRY(cuda_rc(cudaGetLastError()));
-    TRY(hqr_ormqr_n_async(plan, Af, tau, G, CT, 1, s));
+    TRY(ormqr_n_cols(plan, Af, tau, G, CT, 1, s, nrhs));
     hqr::add_unpack(r, g.M, G, g.M, g.NB, nrhs, s);
     TRY(cuda_rc(cudaGetLastError()));
   }

@@ -206,10 +206,11 @@ int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, d
 
 int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT,
                     const double* dTAU, double* dC, int CT, bool rebuild_t, long long timeout_ns,
-                    cudaStream_t stream, const OzWorkspace* ozw) {
+                    cudaStream_t stream, const OzWorkspace* ozw, long long ccols) {
   if (CT <= 0) return HQR_ERR_INVALID;
   DagParams p{};
   p.mode = kModeApplyQt;
+  p.c_cols = ccols;
   p.MT = g.MT;
   p.NT = g.NT;
   p.CT = CT;
@@ -289,10 +290,11 @@ int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double
 
 int launch_apply_q(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT, const double* dTAU,
                    double* dC, int CT, bool rebuild_t, long long timeout_ns, cudaStream_t stream,
-                   const OzWorkspace* ozw) {
+                   const OzWorkspace* ozw, long long ccols) {
   if (CT <= 0) return HQR_ERR_INVALID;
   DagParams p{};
   p.mode = kModeApplyQ;
+  p.c_cols = ccols;
   p.MT = g.MT;
   p.NT = g.NT;
   p.CT = CT;

@@ -117,6 +117,9 @@ struct DagParams {
   // split precision
   int oz;           // 1: OZPREP/OZAPPLY tasks (NC * oz_cpt = NB / 64)
   int oz_cpt;       // 64-column chunks one OZAPPLY task updates, one after the other
+  // Q applications: columns of C that hold data (0: all); the column blocks
+  // from there on are zero, stay zero, and their updates are skipped
+  long long c_cols;
   int oz_groups;    // t-groups of the split updates (8 or 4; host side: picks the kernel)
   int oz_p32;       // 1: FP32 panel arithmetic (host side: picks the kernel)
   int prep;         // 1: separate OZPREP ids after the panel ids (factorization)
@@ -700,6 +703,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
     const uint8_t* oz_slices = nullptr;   // an update on the tensor cores
     const int* oz_exps = nullptr;
     double *oz_top = nullptr, *oz_bot = nullptr;
+    long long oz_col0 = 0;   // column of C where the update's first chunk starts
     const double *prep_v = nullptr, *prep_tau = nullptr;   // a split panel preparation
     double* prep_g = nullptr;
     uint8_t* prep_slices = nullptr;
@@ -764,7 +768,8 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
           oz_slices = q.slices + slot * oz::panel_slice_bytes();
           oz_exps = q.sexp + slot * oz::kSlots * NB;
           oz_bot = q.C + oc + (size_t)t.c * q.oz_cpt * oz::kN * NB;
-        } else {
+          oz_col0 = (long long)t.j * NB + (long long)t.c * q.oz_cpt * oz::kN;
+        } else if (q.c_cols <= 0 || (long long)t.j * NB + (long long)t.c * q.sh.CB < q.c_cols) {
           task_larfb(q.A + ov, q.T + ov, q.C + oc, t.c * q.sh.CB, q.sh.CB, q.sh, smem, q.sp,
                      applies_h(q.mode));
         }
@@ -783,7 +788,8 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
           oz_exps = (tt ? q.sexp2 : q.sexp) + slot * oz::kSlots * NB;
           oz_top = q.C + o1 + cofs;
           oz_bot = q.C + o2 + cofs;
-        } else {
+          oz_col0 = (long long)t.j * NB + (long long)t.c * q.oz_cpt * oz::kN;
+        } else if (q.c_cols <= 0 || (long long)t.j * NB + (long long)t.c * q.sh.CB < q.c_cols) {
           task_ssrfb(q.C + o1, q.C + o2, q.A + ov, tt ? q.T2 + slot * tsz : q.T + ov, t.c * q.sh.CB,
                      q.sh.CB, q.sh, smem, q.sp, applies_h(q.mode), tt);
         }
@@ -799,6 +805,7 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
                   s_tmem, q.ctl + kErr, !applies_h(q.mode));
     if (OZ && oz_bot) {
       for (int cc = 0; cc < q.oz_cpt; cc++) {
+        if (q.c_cols > 0 && oz_col0 + (long long)cc * oz::kN >= q.c_cols) break;
         const size_t co = (size_t)cc * oz::kN * NB;
         oz::Ctx c;
         oz::ctx_init(c, reinterpret_cast<uint8_t*>(smem), s_tmem, q.ctl + kErr);

@@ -115,9 +115,11 @@ int launch_apply_qt_tree(const Geometry& g, DagWorkspace* ws, const double* dA, 
                          const OzWorkspace* oz, const TreeWorkspace* tw);
 // Enqueue C <- Q^T C (C has CT tile columns, same MT/NB as A); the panel
 // tasks rebuild T from V/TAU (FP64: diagonal blocks; split: full T + slices).
+// ccols > 0: only C's first ccols columns hold data (the rest are zero and
+// stay so); the updates of column blocks beyond them are skipped.
 int launch_apply_qt(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT,
                     const double* dTAU, double* dC, int CT, bool rebuild_t, long long timeout_ns,
-                    cudaStream_t stream, const OzWorkspace* oz = nullptr);
+                    cudaStream_t stream, const OzWorkspace* oz = nullptr, long long ccols = 0);
 // Q = H_0 H_1 ... H_{steps-1} dQ for dQ = I (square matrices): backward
 // accumulation, skipping the tile columns that are still unit vectors.
 // rebuild_t false: the T factors / prepared operands of the factorization.
@@ -128,7 +130,7 @@ int launch_build_q(const Geometry& g, DagWorkspace* ws, const double* dA, double
 // rebuild_t false: the T factors / prepared operands (of H) given.
 int launch_apply_q(const Geometry& g, DagWorkspace* ws, const double* dA, double* dT, const double* dTAU,
                    double* dC, int CT, bool rebuild_t, long long timeout_ns, cudaStream_t stream,
-                   const OzWorkspace* oz = nullptr);
+                   const OzWorkspace* oz = nullptr, long long ccols = 0);
 // Batches of independent FP64 factorizations in one persistent launch.
 // Descriptors (mat_desc_bytes() each) are written to host memory by
 // batch_describe and must be on the device (d_desc) for launch_batch.
