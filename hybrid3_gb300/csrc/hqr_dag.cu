@@ -77,15 +77,47 @@ void dag_workspace_free(DagWorkspace* ws) {
   *ws = DagWorkspace{};
 }
 
+// Per-device caches: cudaFuncSetAttribute applies to the current device only,
+// and the SM count is a property of the device, so both are kept per device
+// ordinal (devices beyond kCacheDevices are simply not cached).
+constexpr int kCacheDevices = 64;
+static int current_device() {
+  int dev = 0;
+  return cudaGetDevice(&dev) == cudaSuccess ? dev : -1;
+}
+
 int dag_sm_count() {
-  static int n = 0;
-  if (n == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
+  static int n[kCacheDevices] = {};
+  const int dev = current_device();
+  const bool cached = dev >= 0 && dev < kCacheDevices;
+  if (cached && n[dev] > 0) return n[dev];
+  int v = 0;
+  cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev < 0 ? 0 : dev);
+  if (v <= 0) v = 1;
+  if (cached) n[dev] = v;
+  return v;
+}
+
+// The largest dynamic shared memory a kernel has been opted in to, per device.
+struct SmemOptIn {
+  std::mutex mu;
+  size_t bytes[kCacheDevices] = {};
+};
+// Opt `kernel` in to smem bytes of dynamic shared memory on the current device
+// (once per device and size); extra(): further attribute calls made with it.
+template <class Kernel, class Extra>
+static cudaError_t opt_in(SmemOptIn& o, Kernel kernel, size_t smem, Extra extra) {
+  const int dev = current_device();
+  std::lock_guard<std::mutex> lk(o.mu);
+  if (dev >= 0 && dev < kCacheDevices && smem <= o.bytes[dev]) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = extra();
+  if (e == cudaSuccess && dev >= 0 && dev < kCacheDevices) o.bytes[dev] = smem;
+  return e;
+}
+template <class Kernel>
+static cudaError_t opt_in(SmemOptIn& o, Kernel kernel, size_t smem) {
+  return opt_in(o, kernel, smem, [] { return cudaSuccess; });
 }
 
 static size_t dag_smem_bytes(const Geometry& g, bool oz) {
@@ -96,13 +128,11 @@ static size_t dag_smem_bytes(const Geometry& g, bool oz) {
 
 template <bool OZ, int G = 8, bool P32 = false>
 static int launch_exec(const DagParams& p, const Geometry& g, cudaStream_t stream) {
-  static size_t attr_bytes = 0;   // dynamic shared memory opted in so far
+  static SmemOptIn opted;
   const size_t smem = dag_smem_bytes(g, OZ);
-  if (smem > attr_bytes) {
-    cudaError_t e = cudaFuncSetAttribute(dag_exec_kernel<OZ, false, G, P32>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  {
+    const cudaError_t e = opt_in(opted, dag_exec_kernel<OZ, false, G, P32>, smem);
     if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(dag_exec_kernel)");
-    attr_bytes = smem;
   }
   const int grid = std::min(dag_sm_count(), std::max(1, p.n_tasks));
   dag_exec_kernel<OZ, false, G, P32><<<grid, kThreads, smem, stream>>>(p);
@@ -434,23 +464,15 @@ int launch_batch(bool apply, int count, const void* d_desc, int n_ids, int n_tas
   cudaError_t e = cudaMemsetAsync(ws->ctl, 0, kErr * sizeof(unsigned), stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(ws->stats, 0, 2 * kNumStats * sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return record_cuda_error(e, "DAG workspace reset");
-  static std::mutex mu;
-  static size_t attr_bytes = 0;
+  static SmemOptIn opted;
   int occ = 1;
-  {
-    std::lock_guard<std::mutex> lk(mu);
-    if (smem > attr_bytes) {
-      e = cudaFuncSetAttribute(dag_exec_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem);
-      if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(dag_exec_kernel<false, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared);
-      if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(dag_exec_kernel batch)");
-      attr_bytes = smem;
-    }
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dag_exec_kernel<false, true>, kThreads, smem);
-    if (e != cudaSuccess) return record_cuda_error(e, "occupancy of dag_exec_kernel batch");
-  }
+  e = opt_in(opted, dag_exec_kernel<false, true>, smem, [] {
+    return cudaFuncSetAttribute(dag_exec_kernel<false, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                (int)cudaSharedmemCarveoutMaxShared);
+  });
+  if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(dag_exec_kernel batch)");
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dag_exec_kernel<false, true>, kThreads, smem);
+  if (e != cudaSuccess) return record_cuda_error(e, "occupancy of dag_exec_kernel batch");
   if (occ < 1) return HQR_ERR_UNSUPPORTED;
   if (ctas_per_sm > 0) occ = std::min(occ, ctas_per_sm);
   dag_init_batch_kernel<<<count, 256, 0, stream>>>(p);
@@ -523,17 +545,10 @@ int launch_factor_external(const Geometry& g, const ExternalScratch& x, double* 
   p.ctl = x.ctl;
   p.stats = x.stats;
   p.timeout_ns = timeout_ns;
-  static std::mutex mu;
-  static size_t attr_bytes = 0;
+  static SmemOptIn opted;
   {
-    std::lock_guard<std::mutex> lk(mu);
-    if (g.smem_bytes > attr_bytes) {
-      cudaError_t e = cudaFuncSetAttribute(dag_exec_kernel<false>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)g.smem_bytes);
-      if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(dag_exec_kernel)");
-      attr_bytes = g.smem_bytes;
-    }
+    const cudaError_t e = opt_in(opted, dag_exec_kernel<false>, g.smem_bytes);
+    if (e != cudaSuccess) return record_cuda_error(e, "cudaFuncSetAttribute(dag_exec_kernel)");
   }
   const int blocks = (p.n_ids + 255) / 256;
   dag_init_kernel<<<blocks, 256, 0, stream>>>(p);
