@@ -58,6 +58,7 @@ int dag_workspace_reserve(DagWorkspace* ws, size_t n_ids) {
   if (ws->cap_ids >= n_ids && ws->ctl) return HQR_OK;
   dag_workspace_free(ws);
   if (cudaMalloc(&ws->cnt, n_ids * sizeof(int)) != cudaSuccess) return HQR_ERR_NOMEM;
+  if (cudaMalloc(&ws->flag, n_ids * sizeof(int)) != cudaSuccess) return HQR_ERR_NOMEM;
   if (cudaMalloc(&ws->qhi, n_ids * sizeof(int)) != cudaSuccess) return HQR_ERR_NOMEM;
   if (cudaMalloc(&ws->qlo, n_ids * sizeof(int)) != cudaSuccess) return HQR_ERR_NOMEM;
   if (cudaMalloc(&ws->ctl, kCtlWords * sizeof(unsigned)) != cudaSuccess) return HQR_ERR_NOMEM;
@@ -70,6 +71,7 @@ int dag_workspace_reserve(DagWorkspace* ws, size_t n_ids) {
 
 void dag_workspace_free(DagWorkspace* ws) {
   if (ws->cnt) cudaFree(ws->cnt);
+  if (ws->flag) cudaFree(ws->flag);
   if (ws->qhi) cudaFree(ws->qhi);
   if (ws->qlo) cudaFree(ws->qlo);
   if (ws->ctl) cudaFree(ws->ctl);
@@ -148,6 +150,7 @@ static int run_dag(DagParams& p, DagWorkspace* ws, const Geometry& g, cudaStream
   int rc = dag_workspace_reserve(ws, (size_t)p.n_ids);
   if (rc != HQR_OK) return rc;
   p.cnt = ws->cnt;
+  p.tsflag = ws->flag;
   p.qhi = ws->qhi;
   p.qlo = ws->qlo;
   p.ctl = ws->ctl;
@@ -165,6 +168,10 @@ static int run_dag(DagParams& p, DagWorkspace* ws, const Geometry& g, cudaStream
   if (p.oz_groups == 8) return launch_exec<true, 8>(p, g, stream);
   return p.oz_p32 ? launch_exec<true, 4, true>(p, g, stream) : launch_exec<true, 4>(p, g, stream);
 }
+
+// Update tiles left in a step below which the factorization's panel blocks
+// run in phases (DagParams::ts_split).
+constexpr long long kPhasedWork = 6000;
 
 // 64-column chunks per split update task, run one after the other: two (a
 // whole 128-column tile) halve the number of update tasks and with them the
@@ -221,6 +228,19 @@ int launch_factor(const Geometry& g, DagWorkspace* ws, double* dA, double* dT, d
   p.prep = p.oz;
   p.nblk = g.NB / g.w;
   set_tree(p, g, tw);
+  // split precision, flat tree: panel blocks release their panel dependents
+  // in phases (the first trailing column block is then w wide, which changes
+  // the rounding of the FP64 panels' trailing sums, so FP64 plans keep the
+  // whole-block releases and their results)
+  p.ts_split = (p.tree == 0 && p.oz) ? 1 : 0;
+  // only in the steps whose panel chain, not their update work, sets the
+  // pace: few update tiles left ((NT - i - 1) (MT - i - 1) at most
+  // kPhasedWork); before them the phases' waits and narrower first column
+  // block cost more than the shorter chain gains
+  p.ts_split_from = 0;
+  while (p.ts_split_from < g.steps &&
+         (long long)(g.NT - p.ts_split_from - 1) * (g.MT - p.ts_split_from - 1) > kPhasedWork)
+    p.ts_split_from++;
   // tasks: per step i, nblk inner blocks of each of the MT-i panel tiles [+ one
   // OZPREP per panel tile] + NC*(NT-1-i)*(MT-i) updates; a tree adds per merge
   // nblk blocks [+ one OZPREP] + NC*(NT-1-i) merge updates

@@ -107,6 +107,15 @@ struct DagParams {
   double* TAU;
   double* C;        // target of the update tasks (A itself when factoring)
   int* cnt;         // dependency counters, one per task id
+  // Factorization with the flat tree (ts_split): a panel block (GEQRT or
+  // TSQRT inner block b of tile k at step i) releases the same block of the
+  // tile below once its reflectors are stored, and the next block of its
+  // own tile once the next block's w columns are updated; tsflag[its id]
+  // is set when its whole trailing update is done, which the later blocks
+  // that share those columns or R's rows wait for (bounded) before theirs.
+  int ts_split;
+  int ts_split_from;   // the first step whose panel blocks use the phases
+  int* tsflag;
   int* qhi;         // ready FIFOs, capacity n_ids each
   int* qlo;
   unsigned* ctl;
@@ -442,6 +451,7 @@ __global__ void dag_init_kernel(DagParams p) {
   p.qhi[id] = -1;
   p.qlo[id] = -1;
   p.cnt[id] = init_deps(p, id);
+  if (p.ts_split && id < panel_end(p)) p.tsflag[id] = 0;
 }
 
 __global__ void dag_seed_kernel(DagParams p) {
@@ -567,11 +577,13 @@ __device__ bool release_dependents(const DagParams& p, const TaskDesc& t, int* k
       // the next inner block of this tile; the same block of the tile below in
       // the domain, or, from a domain's last tile, of the domain's merge
       const int d = dom_of(p, t.i, t.k);
-      if (t.c + 1 < p.nblk) release(p, panel_id(p, t.i, t.k, t.c + 1));
-      if (t.k + 1 < dom_end(p, t.i, d))
-        release(p, panel_id(p, t.i, t.k + 1, t.c));
-      else if (n_domains(p, t.i) > 1)
-        release(p, merge_id(p, t.i, d >= 1 ? d : 1, t.c));
+      if (!p.ts_split || t.i < p.ts_split_from) {   // (else the task's phases released these)
+        if (t.c + 1 < p.nblk) release(p, panel_id(p, t.i, t.k, t.c + 1));
+        if (t.k + 1 < dom_end(p, t.i, d))
+          release(p, panel_id(p, t.i, t.k + 1, t.c));
+        else if (n_domains(p, t.i) > 1)
+          release(p, merge_id(p, t.i, d >= 1 ? d : 1, t.c));
+      }
       if (t.c + 1 < p.nblk) return true;   // the tile's V, T, TAU are complete after its last block
     }
     if (feeds_prep) {
@@ -651,6 +663,64 @@ __device__ void task_tbuild(const double* V, const double* tau_g, double* T, boo
 // registers per thread): while one runs a latency-bound panel column loop,
 // the other's update keeps the FP64 pipe busy.
 // OZG: t-groups of the split updates (8: FP64-level; 4: the reduced form).
+// Thread 0: wait (bounded) until panel block `id` has finished its trailing
+// update; false (error word set) when the wait ran out or the DAG failed.
+__device__ bool wait_ts_flag(const DagParams& p, int id) {
+  const uint64_t t0 = global_ns();
+  while (*((volatile const int*)(p.tsflag + id)) == 0) {
+    if (*((volatile const unsigned*)(p.ctl + kErr)) != 0u) return false;
+    if ((long long)(global_ns() - t0) > p.timeout_ns) {
+      atomicOr((int*)(p.ctl + kErr), kErrTimeout);
+      return false;
+    }
+    __nanosleep(64);
+  }
+  return true;
+}
+
+// The phases of a factorization panel block with ts_split (see DagParams):
+// called by every thread of the CTA at the points task_geqrt_blk /
+// task_tsqrt_blk name.  Every wait is on a block that has already released
+// this one (so it is running, past that release) and that waits only on
+// blocks of smaller b or k itself: no cycle, and each wait is bounded.
+// on == false: no phases (the block releases at its end, as without
+// ts_split), and the trailing update keeps its usual column blocks.
+struct PanelPhases {
+  const DagParams* p;
+  int i, k, b;
+  bool on;
+  __device__ int first_cols(int cb, int w) const { return on ? w : cb; }
+  __device__ void publish() const {   // this CTA's writes, then thread 0 releases
+    fence_acq_rel_gpu();
+    __syncthreads();
+  }
+  __device__ void after_panel() const {   // R's diagonal block is final: the tile below's block b
+    if (!on) return;
+    publish();
+    if (threadIdx.x == 0 && k + 1 < p->MT) release(*p, panel_id(*p, i, k + 1, b));
+  }
+  __device__ void before_trailing() const {
+    if (!on) return;
+    if (threadIdx.x == 0) {
+      bool ok = true;
+      if (b > 0) ok = wait_ts_flag(*p, panel_id(*p, i, k, b - 1));   // the same columns, earlier block
+      if (ok && k > i) ok = wait_ts_flag(*p, panel_id(*p, i, k - 1, b));   // R's rows, tile above
+      fence_acq_rel_gpu();   // acquire: their writes are visible
+    }
+    __syncthreads();
+  }
+  __device__ void after_first() const {   // the next block's columns are updated
+    if (!on) return;
+    publish();
+    if (threadIdx.x == 0 && b + 1 < p->nblk) release(*p, panel_id(*p, i, k, b + 1));
+  }
+  __device__ void after_trailing() const {
+    if (!on) return;
+    publish();
+    if (threadIdx.x == 0) atomicExch(p->tsflag + panel_id(*p, i, k, b), 1);
+  }
+};
+
 // P32: the panel blocks compute in FP32 (HQR_PREC_FP32).
 template <bool OZ, bool BATCH = false, int OZG = 8, bool P32 = false>
 __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagParams p) {
@@ -714,7 +784,8 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
     switch (t.type) {
       case kGEQRT: {   // the diagonal tile or a domain's top tile
         const size_t o = tile_off(t.k, t.i, q.MT, NB);
-        task_geqrt_blk<PanelT>(q.A + o, q.T + o, q.TAU + tau_off(t.k, t.i, q.MT, NB), q.sh, smem, q.sp, t.c);
+        task_geqrt_blk<PanelT>(q.A + o, q.T + o, q.TAU + tau_off(t.k, t.i, q.MT, NB), q.sh, smem, q.sp, t.c,
+                               PanelPhases{&q, t.i, t.k, t.c, q.ts_split != 0 && t.i >= q.ts_split_from});
         break;
       }
       case kTSQRT: {   // R of the domain's top tile over tile (k, i)
@@ -798,7 +869,9 @@ __global__ void __launch_bounds__(kThreads, BATCH ? 2 : 1) dag_exec_kernel(DagPa
       default:
         if (threadIdx.x == 0) atomicOr((int*)(q.ctl + kErr), kErrBadTask);
     }
-    if (ts_a1) task_tsqrt_blk<PanelT>(ts_a1, ts_a2, ts_t, ts_tau, q.sh, smem, q.sp, t.c, ts_upper);
+    if (ts_a1)
+      task_tsqrt_blk<PanelT>(ts_a1, ts_a2, ts_t, ts_tau, q.sh, smem, q.sp, t.c, ts_upper,
+                             PanelPhases{&q, t.i, t.k, t.c, q.ts_split != 0 && t.i >= q.ts_split_from && !ts_upper});
     // Q generation and Q C apply H (M = T), the other modes H^T (M = T^T)
     if (OZ && prep_v)
       task_ozprep(prep_v, prep_tau, prep_g, prep_kind, prep_slices, prep_exps, reinterpret_cast<uint8_t*>(smem),

@@ -65,6 +65,7 @@ int at_times(const double* dA, long M, long N, int NB, const double* dR, long ld
 // Scheduler workspace (dependency counters, queues, control words, stats).
 struct DagWorkspace {
   int* cnt = nullptr;
+  int* flag = nullptr;   // per panel block: its trailing update is done (factorization)
   int* qhi = nullptr;
   int* qlo = nullptr;
   unsigned* ctl = nullptr;

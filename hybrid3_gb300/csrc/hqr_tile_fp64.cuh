@@ -566,13 +566,25 @@ __device__ void store_block_upper(double* g, int ldg, const RT* s, int lds, int 
   }
 }
 
+// Points in a panel block where the DAG may act (see the executor's
+// PanelPhases): after the block's reflectors are stored, before its trailing
+// update, after the trailing update's first column block (first_cols wide)
+// and after the whole trailing update.  These do nothing.
+struct NoPanelPhases {
+  __device__ int first_cols(int cb, int) const { return cb; }
+  __device__ void after_panel() const {}
+  __device__ void before_trailing() const {}
+  __device__ void after_first() const {}
+  __device__ void after_trailing() const {}
+};
+
 // Inner block b of CORE_dgeqrt(NB, NB, IB, A, NB, T, NB, TAU): the QR of
 // columns [b w, (b+1) w) from row b w down (blocks 0..b-1 done), its T block,
 // and its application to the columns right of it.  It writes rows >= b w of
 // the tile only: rows [b w, (b+1) w) of R are final afterwards.
-template <typename RT = double>
+template <typename RT = double, class Phases = NoPanelPhases>
 __device__ void task_geqrt_blk(double* A, double* T, double* tau_g, const TileShape& sh, double* smem,
-                               const SmemPlan& sp, int b) {
+                               const SmemPlan& sp, int b, const Phases& ph = Phases()) {
   const int NB = sh.NB, w = sh.w;
   RT* sm = reinterpret_cast<RT*>(smem);
   RT* sP = sm + sp.off_c1;
@@ -592,8 +604,10 @@ __device__ void task_geqrt_blk(double* A, double* T, double* tau_g, const TileSh
     store_block(T + i0 + (size_t)i0 * NB, NB, sTb, w, w, w);
     for (int e = threadIdx.x; e < w; e += kThreads) stg_cg(tau_g + i0 + e, double(sTau[e]));
     __syncthreads();
-    for (int c0 = i0 + w; c0 < NB; c0 += sh.CB) {
-      const int ncol = min(sh.CB, NB - c0);
+    ph.after_panel();
+    ph.before_trailing();
+    for (int c0 = i0 + w, nc = ph.first_cols(sh.CB, w), first = 1; c0 < NB; c0 += nc, nc = sh.CB) {
+      const int ncol = min(nc, NB - c0);
       RT* sC = sm + sp.off_c1;
       __syncthreads();
       load_block(sC, NB, A + i0 + (size_t)c0 * NB, NB, m, ncol);
@@ -601,7 +615,12 @@ __device__ void task_geqrt_blk(double* A, double* T, double* tau_g, const TileSh
       apply_block_t(A + i0 + (size_t)i0 * NB, NB, w, T + i0 + (size_t)i0 * NB, NB, w, m - w, true,
                     sC, NB, sC + w, NB, ncol, sm, sp, sh.RC);
       store_block(A + i0 + (size_t)c0 * NB, NB, sC, NB, m, ncol);
+      if (first) {
+        first = 0;
+        ph.after_first();
+      }
     }
+    ph.after_trailing();
   }
   __syncthreads();
 }
@@ -624,9 +643,10 @@ __device__ void task_geqrt(double* A, double* T, double* tau_g, const TileShape&
 // and is neither read nor written).  The reflectors keep A2's shape, so the
 // same arithmetic on A2 with zeros below the diagonal is exact, and only the
 // upper triangle is stored back.
-template <typename RT = double>
+template <typename RT = double, class Phases = NoPanelPhases>
 __device__ void task_tsqrt_blk(double* A1, double* A2, double* T, double* tau_g, const TileShape& sh,
-                               double* smem, const SmemPlan& sp, int b, bool a2_upper = false) {
+                               double* smem, const SmemPlan& sp, int b, bool a2_upper = false,
+                               const Phases& ph = Phases()) {
   const int NB = sh.NB, w = sh.w;
   RT* sm = reinterpret_cast<RT*>(smem);
   RT* sA = sm + sp.off_c1;     // NB x w panel of A2
@@ -657,8 +677,10 @@ __device__ void task_tsqrt_blk(double* A1, double* A2, double* T, double* tau_g,
     store_block(T + i0 + (size_t)i0 * NB, NB, sTb, w, w, w);
     for (int e = threadIdx.x; e < w; e += kThreads) stg_cg(tau_g + i0 + e, double(sTau[e]));
     __syncthreads();
-    for (int c0 = i0 + w; c0 < NB; c0 += sh.CB) {
-      const int ncol = min(sh.CB, NB - c0);
+    ph.after_panel();
+    ph.before_trailing();
+    for (int c0 = i0 + w, nc = ph.first_cols(sh.CB, w), first = 1; c0 < NB; c0 += nc, nc = sh.CB) {
+      const int ncol = min(nc, NB - c0);
       RT* sCt = sm + sp.off_c1;  // w x ncol rows of R (the panel area is free now)
       RT* sCb = sm + sp.off_c1 + w * sh.CB;  // NB x ncol of A2 after the R rows
       __syncthreads();
@@ -673,7 +695,12 @@ __device__ void task_tsqrt_blk(double* A1, double* A2, double* T, double* tau_g,
                     sCb, NB, ncol, sm, sp, sh.RC, false, a2_upper ? i0 : -1);
       store_block(A1 + i0 + (size_t)c0 * NB, NB, sCt, w, w, ncol);
       store_block(A2 + (size_t)c0 * NB, NB, sCb, NB, mrows, ncol);
+      if (first) {
+        first = 0;
+        ph.after_first();
+      }
     }
+    ph.after_trailing();
   }
   __syncthreads();
 }
